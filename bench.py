@@ -1,0 +1,329 @@
+"""Benchmark of the CRaystal hot path on GB300.
+
+Workload (the ray-cast microbenchmark): 1,048,576 random FP32 triangles
+(centroids U[0,1]^3, edges N(0, 0.01) per component), binned-SAH BVH with 32
+bins built on the GPU, 16,777,216 rays from the sphere of radius 2 towards
+U[0,1]^3 (tmin 1e-4, tmax inf), closest hit (prim, t, u, v) per ray.  One
+step = one closest-hit pass over the 16M rays.
+
+  value : Mrays/s with rays and hits resident in HBM (cr_trace_closest_device),
+          CUDA events on the launching stream.
+  e2e   : Mrays/s through cr_trace_closest with pinned host buffers; every step
+          copies the 512 MiB of rays in and the 256 MiB of hits out.
+  roofline : algorithmic bytes per ray counted by the oracle on the
+          reference BVH (32 B ray + 16 B hit + 24 B per child box tested +
+          48 B per triangle tested + 4 B per leaf-map read) over the kernel's
+          measured time, against the measured HBM copy bandwidth.
+  cpu_baseline : the oracle (a CPU restatement of the reference path; the
+          reference itself cannot be built) on all host cores, on a sample of
+          the same rays.
+
+--impl reference times that CPU path on its own (the reference arm).
+Under torchrun (N > 1) every rank runs its own replica (the path does not
+need to exchange data); value sums the rays of all ranks over the slowest
+rank's time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_TRIS = 1 << 20
+N_RAYS = 1 << 24
+TRI_SEED, RAY_SEED = 0, 1
+METRIC = "Mrays/s (closest-hit ray cast, 1M triangles, 16M rays)"
+WORKLOAD = "raycast_1M_tris_16M_rays"
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.file = None
+
+    def start(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.file, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait(timeout=10)
+        self.file.flush()
+        rows = []
+        with open(self.file.name) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.file.name)
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def algorithmic_bytes_per_ray(flat, rays_sample, threads):
+    """Oracle counts on the reference BVH (independent of the GPU's tree)."""
+    import oracle
+    osc = oracle.OracleScene(flat)
+    _, _, c = osc.trace_closest(rays_sample, threads=threads, counters=True)
+    n = c["rays"]
+    per = {"boxes": c["boxes"] / n, "tris": c["tris"] / n, "map_reads": c["map_reads"] / n}
+    bpr = 32 + 16 + 24 * per["boxes"] + 48 * per["tris"] + 4 * per["map_reads"]
+    return bpr, per, osc
+
+
+def cpu_baseline(osc, rays, threads, target_s=6.0):
+    """Times the oracle's closest-hit traversal on a bounded sample."""
+    probe = rays[: 1 << 16]
+    t0 = time.perf_counter()
+    osc.trace_closest(probe, threads=threads)
+    rate = len(probe) / max(time.perf_counter() - t0, 1e-6)
+    n = int(min(len(rays), max(1 << 18, rate * target_s)))
+    n -= n % 1024
+    sample = rays[:n]
+    t0 = time.perf_counter()
+    osc.trace_closest(sample, threads=threads)
+    dt = time.perf_counter() - t0
+    return n / dt / 1e6, n, dt
+
+
+def traffic_from_profile():
+    """DRAM bytes per launch of the trace kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "trace_closest_raycast.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        p = json.load(f)
+    return p.get("dram_bytes_per_launch_full_size")
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import oracle
+    from craystal_gb300 import scenes
+    from craystal_gb300.api import flatten_scene
+    threads = oracle.hardware_threads()
+    osc = oracle.OracleScene(flatten_scene(scenes.random_triangle_scene(N_TRIS, TRI_SEED)))
+    sample = 1 << 20
+    rays = scenes.random_rays(sample * 2, RAY_SEED)
+    for i in range(args.warmup):
+        osc.trace_closest(rays[(i % 2) * sample:(i % 2 + 1) * sample], threads=threads)
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        osc.trace_closest(rays[(i % 2) * sample:(i % 2 + 1) * sample], threads=threads)
+    dt = time.perf_counter() - t0
+    v = sample * args.steps / dt / 1e6
+    out = {"metric": METRIC, "value": round(v, 3), "unit": "Mrays/s", "impl": "reference", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * dt / args.steps, 3),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (seeded)",
+           "config": {"workload": WORKLOAD, "triangles": N_TRIS, "rays": N_RAYS,
+                      "step_sample_rays": sample, "bvh": "binned SAH, 32 bins (reference CPU build)"},
+           "cpu_baseline": {"value": round(v, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
+                            "sample": f"{sample} of the {N_RAYS} rays per step"},
+           "e2e": {"value": round(v, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def cornell_extra(torch):
+    """The plain path tracer on the procedural Cornell box, 256x256, 16 spp,
+    max depth 8, NEE + MIS: Mpaths/s and Mrays/s of the render."""
+    from craystal_gb300 import scenes
+    from craystal_gb300.api import PathTraceIntegrator, Scene
+    data, cam = scenes.cornell_box(seed=0, width=256, height=256)
+    sc = Scene(data)
+    sc.setCamera(cam)
+    integ = PathTraceIntegrator(PathTraceIntegrator.Configs(maxDepth=8, rrThreshold=0.05, useMIS=True), compat=False)
+    integ.dispatch(sc, 16, readback=False)
+    torch.cuda.synchronize()
+    sc.film_clear()
+    spp = 16
+    s = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 5
+    e0.record(s)
+    for r in range(reps):
+        integ.dispatch(sc, spp, first_sample=r * spp, stream=s.cuda_stream, readback=False)
+    e1.record(s)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    rays = sc.render_ray_count()
+    paths = 256 * 256 * spp * reps
+    return {"config": "cornell 256x256, 16 spp, max depth 8, NEE+MIS", "Mpaths_s": round(paths / ms / 1e3, 2),
+            "Mrays_s": round(rays / ms / 1e3, 2), "ms_per_16spp": round(ms / reps, 3),
+            "rays_per_path": round(rays / paths, 3)}
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+    rank, world, local = dist_env()
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    import craystal_gb300 as cg
+    from craystal_gb300 import scenes
+    from craystal_gb300.api import Scene, flatten_scene
+    cg.load().cr_set_device(local)
+
+    data = scenes.random_triangle_scene(N_TRIS, TRI_SEED)
+    t0 = time.perf_counter()
+    sc = Scene(data)
+    build_wall = time.perf_counter() - t0
+    st = sc.bvh_stats()
+    rays = scenes.random_rays(N_RAYS, RAY_SEED)
+    raw = torch.from_numpy(rays.view(np.uint8))
+    d_rays = raw.to(f"cuda:{local}")
+    d_hits = torch.empty(N_RAYS * 16, dtype=torch.uint8, device=f"cuda:{local}")
+    s = torch.cuda.current_stream()
+
+    def step():
+        sc.trace_closest_device(d_rays.data_ptr(), N_RAYS, d_hits.data_ptr(), s.cuda_stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    launches0 = cg.kernel_launch_count()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(args.steps):
+        step()
+    e1.record(s)
+    e1.synchronize()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    launches = cg.kernel_launch_count() - launches0
+    clk = clocks.stop()
+    if world > 1:
+        t = torch.tensor([ms], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = N_RAYS * args.steps * world / (ms * 1e-3) / 1e6
+    kernel_ms = ms / args.steps  # one launch per step
+
+    # e2e: host buffers through the C ABI, copies inside the timed region
+    pin_r = torch.empty(N_RAYS * 32, dtype=torch.uint8).pin_memory()
+    pin_r.numpy()[:] = rays.view(np.uint8)
+    pin_h = torch.empty(N_RAYS * 16, dtype=torch.uint8).pin_memory()
+    from craystal_gb300._lib import check, load
+    lib = load()
+    rp, hp = pin_r.data_ptr(), pin_h.data_ptr()
+    check(lib.cr_trace_closest(sc.handle, rp, N_RAYS, hp))
+    e2e_steps = max(3, min(args.steps, 10))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        check(lib.cr_trace_closest(sc.handle, rp, N_RAYS, hp))
+    e2e_s = time.perf_counter() - t0
+    e2e = N_RAYS * e2e_steps * world / e2e_s / 1e6
+    # the host-path result is the device-path result
+    hits_host = pin_h.numpy().view(cg.HIT_DTYPE)
+    hits_dev = d_hits.cpu().numpy().view(cg.HIT_DTYPE)
+    same = bool(np.array_equal(hits_host.view(np.uint32), hits_dev.view(np.uint32)))
+
+    extra = {"bvh": {"nodes": st["node_count"], "leaves": st["leaf_count"], "max_depth": st["max_depth"],
+                     "gpu_build_ms": round(st["build_ms"], 2), "scene_create_wall_s": round(build_wall, 3),
+                     "device_mib": round(st["device_bytes"] / 2 ** 20, 1)},
+             "host_path_matches_device_path": same,
+             "hit_fraction": round(float((hits_dev["prim"] != cg.CR_MISS).mean()), 4)}
+    if not args.skip_extra:
+        extra["path_tracer"] = cornell_extra(torch)
+
+    out = {"metric": METRIC, "value": round(value, 2), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+           "config": {"workload": WORKLOAD, "triangles": N_TRIS, "rays_per_step": N_RAYS,
+                      "parallelism": "replicas" if world > 1 else "single", "bvh": "GPU binned SAH, 32 bins",
+                      "l2": "inputs larger than L2 (512 MiB of rays per step)"},
+             "e2e": {"value": round(e2e, 2), "unit": "Mrays/s", "h2d_bytes_per_step": N_RAYS * 32,
+                     "d2h_bytes_per_step": N_RAYS * 16},
+             "gpu_launches": int(launches), "clocks": clk, "extra": extra}
+
+    if rank == 0:
+        import oracle
+        threads = oracle.hardware_threads()
+        flat = flatten_scene(data)
+        bpr, per, osc = algorithmic_bytes_per_ray(flat, rays[: 1 << 18], threads)
+        achieved = bpr * N_RAYS / (kernel_ms * 1e-3) / 1e9
+        peak, src = peaks()
+        traffic = traffic_from_profile()
+        out["roofline"] = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                           "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": src,
+                           "kernel": "kTraceClosest", "kernel_ms": round(kernel_ms, 4),
+                           "bytes_per_ray": round(bpr, 1),
+                           "per_ray": {k: round(v, 2) for k, v in per.items()},
+                           "note": f"of {src}; per-ray counts from the oracle on 262144 rays"}
+        if not args.skip_cpu:
+            v, n, dt = cpu_baseline(osc, rays, threads)
+            out["cpu_baseline"] = {"value": round(v, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
+                                   "sample": f"first {n} of the {N_RAYS} rays ({dt:.1f} s wall)"}
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU baseline leg")
+    ap.add_argument("--skip-extra", action="store_true", help="omit the path-tracer figures")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

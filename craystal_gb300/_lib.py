@@ -1,0 +1,115 @@
+"""ctypes binding of libcraystal_gb300.so (declarations in include/craystal_c.h).
+
+The library is the product: there is no Python or CPU fallback.  Loading
+fails loudly when the shared library has not been built.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "_build", "libcraystal_gb300.so")
+
+CR_OK = 0
+CR_ERR_INVALID_ARGUMENT = 1
+CR_ERR_CUDA = 2
+CR_ERR_OUT_OF_MEMORY = 3
+CR_ERR_DEVICE = 4
+CR_ERR_UNSUPPORTED = 5
+CR_MISS = 0xFFFFFFFF
+
+RAY_DTYPE = np.dtype([("o", "<f4", 3), ("tmin", "<f4"), ("d", "<f4", 3), ("tmax", "<f4")])
+HIT_DTYPE = np.dtype([("prim", "<u4"), ("t", "<f4"), ("u", "<f4"), ("v", "<f4")])
+MATERIAL_DTYPE = np.dtype([("diffuse", "<f4", 3), ("specular", "<f4", 3), ("emission", "<f4", 3),
+                           ("shininess", "<f4"), ("type", "<u4"), ("flags", "<u4")])
+MESH_DTYPE = np.dtype([("index_offset", "<u4"), ("index_count", "<u4"), ("vertex_offset", "<u4"),
+                       ("material_id", "<u4")])
+BVH_NODE_DTYPE = np.dtype([("bmin", "<f4", 3), ("bmax", "<f4", 3), ("is_leaf", "<u4"), ("a", "<u4"), ("b", "<u4")])
+
+
+class CrCamera(ctypes.Structure):
+    _fields_ = [("pos", ctypes.c_float * 3), ("target", ctypes.c_float * 3), ("up", ctypes.c_float * 3),
+                ("fov_y", ctypes.c_float), ("width", ctypes.c_uint32), ("height", ctypes.c_uint32)]
+
+
+class CrIntegratorConfig(ctypes.Structure):
+    _fields_ = [("max_depth", ctypes.c_uint32), ("rr_threshold", ctypes.c_float), ("use_mis", ctypes.c_uint32),
+                ("flags", ctypes.c_uint32)]
+
+
+class CrBvhStats(ctypes.Structure):
+    _fields_ = [("node_count", ctypes.c_uint32), ("leaf_count", ctypes.c_uint32), ("max_depth", ctypes.c_uint32),
+                ("max_leaf_size", ctypes.c_uint32), ("max_leaf_depth", ctypes.c_uint32),
+                ("levels", ctypes.c_uint32), ("root_min", ctypes.c_float * 3), ("root_max", ctypes.c_float * 3),
+                ("build_ms", ctypes.c_double), ("device_bytes", ctypes.c_uint64)]
+
+
+class CrayError(RuntimeError):
+    """Raised for a non-zero status of the C ABI (the reference throws
+    RuntimeError from CRAYSTAL_CHECK / CRAYSTAL_CUDA_CHECK)."""
+
+    def __init__(self, code, msg):
+        super().__init__(f"craystal_gb300 error {code}: {msg}")
+        self.code = code
+
+
+# (name, restype, argtypes)
+_P = ctypes.c_void_p
+_U32 = ctypes.c_uint32
+_U64 = ctypes.c_uint64
+SIGNATURES = [
+    ("cr_last_error", ctypes.c_char_p, []),
+    ("cr_version", ctypes.c_char_p, []),
+    ("cr_set_device", ctypes.c_int, [ctypes.c_int]),
+    ("cr_scene_create", ctypes.c_int, [_P, _P, _P, _U64, _P, _U64, _P, _U32, _P, _U32, _P, _U32,
+                                       ctypes.POINTER(ctypes.c_void_p)]),
+    ("cr_scene_destroy", ctypes.c_int, [_P]),
+    ("cr_scene_bvh_stats", ctypes.c_int, [_P, ctypes.POINTER(CrBvhStats)]),
+    ("cr_scene_bvh_export", ctypes.c_int, [_P, _P, _P]),
+    ("cr_scene_set_camera", ctypes.c_int, [_P, ctypes.POINTER(CrCamera)]),
+    ("cr_film_clear", ctypes.c_int, [_P]),
+    ("cr_film_read", ctypes.c_int, [_P, _P, _P]),
+    ("cr_film_resolve", ctypes.c_int, [_P, _P]),
+    ("cr_render", ctypes.c_int, [_P, ctypes.POINTER(CrIntegratorConfig), _U32, _U32, _P]),
+    ("cr_render_ray_count", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint64)]),
+    ("cr_trace_closest", ctypes.c_int, [_P, _P, _U64, _P]),
+    ("cr_trace_closest_device", ctypes.c_int, [_P, _P, _U64, _P, _P]),
+    ("cr_trace_occluded", ctypes.c_int, [_P, _P, _U64, _P]),
+    ("cr_trace_occluded_device", ctypes.c_int, [_P, _P, _U64, _P, _P]),
+    ("cr_camera_generate_rays", ctypes.c_int, [ctypes.POINTER(CrCamera), _P, _U64, _P]),
+    ("cr_bsdf_evaluate", ctypes.c_int, [_P, _P, _P, _P, _U64, _P, _P]),
+    ("cr_bsdf_sample", ctypes.c_int, [_P, _P, _P, _P, _U64, _P, _P, _P]),
+    ("cr_kernel_launch_count", ctypes.c_uint64, []),
+]
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Loads the shared library (once) and declares every entry point."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError(f"{path} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'` "
+                          "(craystal_gb300 has no CPU fallback)")
+    lib = ctypes.CDLL(path)
+    for name, res, args in SIGNATURES:
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(code: int):
+    if code != CR_OK:
+        raise CrayError(code, load().cr_last_error().decode())
+
+
+def ptr(a) -> int:
+    """Address of a numpy array (or None -> NULL)."""
+    if a is None:
+        return None
+    return a.ctypes.data

@@ -1,0 +1,314 @@
+"""Host-side mirror of the reference's hot-path API (Source/CRaystal):
+Scene / SceneData / MeshData / MaterialData (Scene/Scene.h:40-58,
+Scene/Triangle.h:36-42, Core/Material.h:34-66), Camera (Core/Camera.h),
+Sensor (Core/Sensor.h) and PathTraceIntegrator (Core/Integrator.h).
+
+Everything runs through the C ABI of libcraystal_gb300.so; there is no CPU
+path.  Errors raise CrayError (the reference raises RuntimeError).
+"""
+import ctypes
+import enum
+from dataclasses import dataclass, field
+from typing import List, Optional
+
+import numpy as np
+
+from . import _lib
+from ._lib import (BVH_NODE_DTYPE, HIT_DTYPE, MATERIAL_DTYPE, MESH_DTYPE, RAY_DTYPE, CrBvhStats, CrCamera,
+                   CrIntegratorConfig, check, load, ptr)
+
+
+class MaterialType(enum.IntEnum):
+    """Core/Material.h:12-16."""
+    FullDiffuse = 0
+    Principled = 1
+    Phong = 2
+
+
+class MaterialFlags(enum.IntFlag):
+    """Core/Material.h:26-30."""
+    IsEmissive = 1
+    IsDiffuse = 2
+
+
+@dataclass
+class MaterialData:
+    """Core/Material.h:34-66 (the fields the path reads)."""
+    diffuseRefl: tuple = (0.0, 0.0, 0.0)
+    specularRefl: tuple = (0.0, 0.0, 0.0)
+    emission: tuple = (0.0, 0.0, 0.0)
+    shininess: float = 0.0
+    type: MaterialType = MaterialType.FullDiffuse
+    flags: int = 0
+
+    def finalize(self):
+        """MaterialData::finalize, Core/Material.h:57-65."""
+        if max(self.emission) != 0.0:
+            self.flags |= int(MaterialFlags.IsEmissive)
+        if max(self.specularRefl) == 0.0:
+            self.flags |= int(MaterialFlags.IsDiffuse)
+
+    def isEmissive(self) -> bool:
+        return bool(self.flags & MaterialFlags.IsEmissive)
+
+
+@dataclass
+class MeshData:
+    """Scene/Triangle.h:36-42: per-mesh vertex arrays and local indices."""
+    position: np.ndarray
+    index: np.ndarray
+    materialID: int = 0
+    normal: Optional[np.ndarray] = None
+    texCrd: Optional[np.ndarray] = None
+
+
+@dataclass
+class SceneData:
+    """Scene/Scene.h:40-47 (spheres and textures are not part of this path)."""
+    meshes: List[MeshData] = field(default_factory=list)
+    materials: List[MaterialData] = field(default_factory=list)
+    emissiveIndex: List[int] = field(default_factory=list)
+
+
+def flatten_scene(data: SceneData):
+    """TriangleMeshManager's concatenation (Scene/Triangle.cu:98-131): global
+    vertex arrays, indices rebased by each mesh's vertex offset, MeshDesc."""
+    pos, nrm, uv, idx = [], [], [], []
+    descs = np.zeros(len(data.meshes), MESH_DTYPE)
+    nv = ni = 0
+    for m, mesh in enumerate(data.meshes):
+        p = np.ascontiguousarray(mesh.position, np.float32).reshape(-1, 3)
+        n = (np.zeros_like(p) if mesh.normal is None else np.ascontiguousarray(mesh.normal, np.float32).reshape(-1, 3))
+        t = (np.zeros((len(p), 2), np.float32) if mesh.texCrd is None
+             else np.ascontiguousarray(mesh.texCrd, np.float32).reshape(-1, 2))
+        i = np.ascontiguousarray(mesh.index, np.uint32).reshape(-1)
+        descs[m] = (ni, len(i), nv, mesh.materialID)
+        pos.append(p)
+        nrm.append(n)
+        uv.append(t)
+        idx.append(i + np.uint32(nv))
+        nv += len(p)
+        ni += len(i)
+    cat = lambda xs, shape, dt: np.concatenate(xs) if xs else np.zeros(shape, dt)
+    mats = np.zeros(len(data.materials), MATERIAL_DTYPE)
+    for k, md in enumerate(data.materials):
+        mats[k] = (md.diffuseRefl, md.specularRefl, md.emission, md.shininess, int(md.type), md.flags)
+    return dict(pos=cat(pos, (0, 3), np.float32), nrm=cat(nrm, (0, 3), np.float32), uv=cat(uv, (0, 2), np.float32),
+                idx=cat(idx, (0,), np.uint32), meshes=descs, mats=mats,
+                emissive=np.asarray(data.emissiveIndex, np.uint32))
+
+
+class Sensor:
+    """Core/Sensor.h:35-61: film size, spp and the host copy of the film."""
+
+    def __init__(self, size=(512, 512), spp: int = 1):
+        self.size = (int(size[0]), int(size[1]))
+        self.spp = int(spp)
+        self.data = np.zeros((self.size[1], self.size[0], 3), np.float32)
+        self.weight = np.zeros((self.size[1], self.size[0]), np.float32)
+
+    def setSPP(self, value: int):
+        self.spp = int(value)
+
+    def getSPP(self) -> int:
+        return self.spp
+
+    def getSize(self):
+        return self.size
+
+    def createImage(self) -> np.ndarray:
+        """Sensor::createImage (Core/Sensor.cu:93-112): sum / weight, HxWx3."""
+        with np.errstate(divide="ignore", invalid="ignore"):
+            return self.data / self.weight[..., None]
+
+
+class Camera:
+    """Core/Camera.h:18-46 with the defaults of CameraProxy (Core/CameraProxy.h:12-23)."""
+
+    def __init__(self):
+        self.posW = (0.0, 0.0, 0.0)
+        self.fovY = 60.0
+        self.target = (0.0, 0.0, -1.0)
+        self.up = (0.0, 1.0, 0.0)
+        self.sensor: Optional[Sensor] = None
+
+    def setFovY(self, v):
+        self.fovY = float(v)
+
+    def setWorldPosition(self, p):
+        self.posW = tuple(float(x) for x in p)
+
+    def setTarget(self, t):
+        self.target = tuple(float(x) for x in t)
+
+    def setUp(self, u):
+        self.up = tuple(float(x) for x in u)
+
+    def setSensor(self, s: Sensor):
+        self.sensor = s
+
+    def getSensor(self) -> Optional[Sensor]:
+        return self.sensor
+
+    def calculateCameraData(self):
+        """The basis is computed in the library when the camera is set on a scene."""
+
+    def _c(self) -> CrCamera:
+        c = CrCamera()
+        c.pos[:] = self.posW
+        c.target[:] = self.target
+        c.up[:] = self.up
+        c.fov_y = self.fovY
+        w, h = self.sensor.size if self.sensor else (512, 512)
+        c.width, c.height = w, h
+        return c
+
+
+class Scene:
+    """Scene/Scene.h:50-82.  Construction uploads the geometry and builds the
+    BVH on the GPU."""
+
+    def __init__(self, data: SceneData):
+        lib = load()
+        f = flatten_scene(data)
+        self._flat = f
+        self.n_tris = len(f["idx"]) // 3
+        h = ctypes.c_void_p()
+        check(lib.cr_scene_create(ptr(f["pos"]), ptr(f["nrm"]), ptr(f["uv"]), len(f["pos"]), ptr(f["idx"]),
+                                  self.n_tris, ptr(f["meshes"]), len(f["meshes"]), ptr(f["mats"]), len(f["mats"]),
+                                  ptr(f["emissive"]), len(f["emissive"]), ctypes.byref(h)))
+        self._h = h
+        self._camera: Optional[Camera] = None
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            load().cr_scene_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def setCamera(self, cam: Camera):
+        self._camera = cam
+        check(load().cr_scene_set_camera(self._h, ctypes.byref(cam._c())))
+
+    def getCamera(self) -> Optional[Camera]:
+        return self._camera
+
+    # --- BVH introspection (Core/BVH.cu:111-115 logs the same figures) ---
+    def bvh_stats(self) -> dict:
+        st = CrBvhStats()
+        check(load().cr_scene_bvh_stats(self._h, ctypes.byref(st)))
+        return {k: (list(getattr(st, k)) if k in ("root_min", "root_max") else getattr(st, k))
+                for k, _ in CrBvhStats._fields_}
+
+    def bvh_export(self):
+        """Nodes in the reference layout (post-order, root last) and the
+        leaf-slot -> primitive map."""
+        st = self.bvh_stats()
+        nodes = np.zeros(st["node_count"], BVH_NODE_DTYPE)
+        pmap = np.zeros(self.n_tris, np.uint32)
+        check(load().cr_scene_bvh_export(self._h, ptr(nodes), ptr(pmap)))
+        return nodes, pmap
+
+    # --- ray queries (SceneView::intersect / intersectOcclusion) ---
+    def trace_closest(self, rays: np.ndarray) -> np.ndarray:
+        rays = np.ascontiguousarray(rays, RAY_DTYPE)
+        hits = np.empty(len(rays), HIT_DTYPE)
+        check(load().cr_trace_closest(self._h, ptr(rays), len(rays), ptr(hits)))
+        return hits
+
+    def trace_occluded(self, rays: np.ndarray) -> np.ndarray:
+        rays = np.ascontiguousarray(rays, RAY_DTYPE)
+        occ = np.empty(len(rays), np.uint8)
+        check(load().cr_trace_occluded(self._h, ptr(rays), len(rays), ptr(occ)))
+        return occ
+
+    def trace_closest_device(self, rays_ptr: int, n: int, hits_ptr: int, stream: int = 0):
+        check(load().cr_trace_closest_device(self._h, rays_ptr, n, hits_ptr, stream or None))
+
+    def trace_occluded_device(self, rays_ptr: int, n: int, occ_ptr: int, stream: int = 0):
+        check(load().cr_trace_occluded_device(self._h, rays_ptr, n, occ_ptr, stream or None))
+
+    # --- film ---
+    def film_clear(self):
+        check(load().cr_film_clear(self._h))
+
+    def film_read(self):
+        w, h = self._camera.sensor.size
+        rgb = np.zeros((h, w, 3), np.float32)
+        wt = np.zeros((h, w), np.float32)
+        check(load().cr_film_read(self._h, ptr(rgb), ptr(wt)))
+        return rgb, wt
+
+    def film_resolve(self) -> np.ndarray:
+        w, h = self._camera.sensor.size
+        out = np.zeros((h, w, 3), np.float32)
+        check(load().cr_film_resolve(self._h, ptr(out)))
+        return out
+
+    def render_ray_count(self) -> int:
+        v = ctypes.c_uint64()
+        check(load().cr_render_ray_count(self._h, ctypes.byref(v)))
+        return v.value
+
+
+class PathTraceIntegrator:
+    """Core/Integrator.h:10-38.
+
+    The reference never copies Configs into its device view, so its kernel
+    always runs with maxDepth 10 and rrThreshold 0.05 and only useMIS takes
+    effect (Core/Integrator.cu:8-11, 234, 247).  compat=True (default)
+    reproduces that; compat=False hands Configs to the kernel.
+    """
+
+    class Configs:
+        def __init__(self, maxDepth: int = 10, rrThreshold: float = 0.15, useMIS: bool = True):
+            self.maxDepth = maxDepth
+            self.rrThreshold = rrThreshold
+            self.useMIS = useMIS
+
+    def __init__(self, configs: "PathTraceIntegrator.Configs" = None, compat: bool = True):
+        self.configs = configs or PathTraceIntegrator.Configs()
+        self.compat = compat
+
+    def device_config(self) -> CrIntegratorConfig:
+        c = CrIntegratorConfig()
+        if self.compat:
+            c.max_depth, c.rr_threshold = 10, 0.05
+        else:
+            c.max_depth, c.rr_threshold = self.configs.maxDepth, self.configs.rrThreshold
+        c.use_mis = 1 if self.configs.useMIS else 0
+        c.flags = 0
+        return c
+
+    def dispatch(self, scene: Scene, spp: int, first_sample: int = 0, stream: int = 0, readback: bool = True):
+        """PathTraceIntegrator::dispatch (Core/Integrator.cu:233-262): spp
+        samples per pixel with sample indices first_sample.. (the reference
+        always starts at 0), then the film is read back into the sensor."""
+        cam = scene.getCamera()
+        if cam is None or cam.sensor is None:
+            raise _lib.CrayError(_lib.CR_ERR_INVALID_ARGUMENT, "scene has no camera with a sensor")
+        cam.sensor.setSPP(spp)
+        scene.setCamera(cam)
+        cfg = self.device_config()
+        check(load().cr_render(scene.handle, ctypes.byref(cfg), int(spp), int(first_sample), stream or None))
+        if readback:
+            rgb, wt = scene.film_read()
+            cam.sensor.data[...] = rgb
+            cam.sensor.weight[...] = wt
+
+
+def kernel_launch_count() -> int:
+    return int(load().cr_kernel_launch_count())
+
+
+def version() -> str:
+    return load().cr_version().decode()

@@ -1,0 +1,319 @@
+// cr_core.cu -- C ABI plumbing: errors, scene lifetime, camera, film.
+
+#include <cstdarg>
+#include <cstring>
+
+#include "cr_internal.cuh"
+#include "cr_math.cuh"
+#include "cr_traverse.cuh"
+
+namespace cr {
+namespace {
+thread_local std::string gError;
+std::atomic<uint64_t> gLaunches{0};
+}  // namespace
+
+void setError(const char* fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    gError = buf;
+}
+
+void clearError() { gError.clear(); }
+
+int fail(int code, const char* fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    gError = buf;
+    return code;
+}
+
+void countLaunch(uint64_t n) { gLaunches.fetch_add(n, std::memory_order_relaxed); }
+
+namespace {
+
+// MaterialData::finalize (Core/Material.h:57-65) and the per-material part
+// of the BSDF constructors (Material/PhongBRDF.cu:10-18,
+// Material/PrincipledBRDF.cu:35-55).
+MaterialGpu deriveMaterial(const cr_material& m) {
+    MaterialGpu g;
+    std::memset(&g, 0, sizeof(g));
+    for (int k = 0; k < 3; k++) {
+        g.kd[k] = m.diffuse[k];
+        g.ks[k] = m.specular[k];
+        g.em[k] = m.emission[k];
+    }
+    g.shininess = m.shininess;
+    g.type = m.type;
+    g.flags = m.flags;
+    const Spec kd = sp(m.diffuse[0], m.diffuse[1], m.diffuse[2]);
+    const Spec ks = sp(m.specular[0], m.specular[1], m.specular[2]);
+    const Spec em = sp(m.emission[0], m.emission[1], m.emission[2]);
+    if (maxValue(em) != 0.0f) g.flags |= CR_MATERIAL_EMISSIVE;
+    if (maxValue(ks) == 0.0f) g.flags |= CR_MATERIAL_DIFFUSE_ONLY;
+    if (m.type == CR_MATERIAL_PHONG) {
+        float d = smax(averageValue(kd), 0.0f);
+        float s = smax(averageValue(ks), 0.0f);
+        float sum = gmax(d + s, kEps);
+        g.dProb = d / sum;
+        g.sProb = s / sum;
+    } else if (m.type == CR_MATERIAL_PRINCIPLED) {
+        float r = sqrtf(2.0f / (m.shininess + 1.0f));
+        float met = averageValue(ks);
+        g.rough = r < 0.0f ? 0.0f : (1.0f < r ? 1.0f : r);
+        g.metal = met < 0.0f ? 0.0f : (1.0f < met ? 1.0f : met);
+        float spr = 0.1f * (1.0f - g.metal) + 1.0f * g.metal;
+        float d = 1.0f, s = spr;
+        d /= (d + s);
+        s /= (d + s);  // uses the updated d, as PrincipledBRDF.cu:47-48 does
+        g.dProb = d;
+        g.sProb = s;
+    } else {
+        g.dProb = 1.0f;
+        g.sProb = 0.0f;
+    }
+    return g;
+}
+
+template <class T>
+int upload(T** dst, const T* src, size_t n) {
+    CR_CUDA(cudaMalloc(dst, std::max<size_t>(n, 1) * sizeof(T)));
+    if (n) CR_CUDA(cudaMemcpy(*dst, src, n * sizeof(T), cudaMemcpyHostToDevice));
+    return CR_OK;
+}
+
+void freeScene(cr_scene* s) {
+    if (!s) return;
+    cudaSetDevice(s->device);
+    void* ptrs[] = {s->pos,  s->nrm,      s->uv,         s->idx,        s->primToMesh, s->meshes,
+                    s->mats, s->emissive, s->pairs,      s->leaves,     s->tris,       s->slotToPrim,
+                    s->buildNodes, s->errFlags, s->filmRgb, s->filmW, s->rayCounter};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    for (int k = 0; k < 2; k++) {
+        if (s->stageRays[k]) cudaFree(s->stageRays[k]);
+        if (s->stageHits[k]) cudaFree(s->stageHits[k]);
+        if (s->stageOcc[k]) cudaFree(s->stageOcc[k]);
+        if (s->streams[k]) cudaStreamDestroy(s->streams[k]);
+    }
+    delete s;
+}
+
+int createScene(const float* pos, const float* nrm, const float* uv, uint64_t nv, const uint32_t* idx, uint64_t nt,
+                const cr_mesh_desc* meshes, uint32_t nMeshes, const cr_material* mats, uint32_t nMats,
+                const uint32_t* emissive, uint32_t nEmissive, cr_scene* s) {
+    if (nv && !pos) return fail(CR_ERR_INVALID_ARGUMENT, "positions are NULL");
+    if (nt && !idx) return fail(CR_ERR_INVALID_ARGUMENT, "indices are NULL");
+    if (nt && (!meshes || nMeshes == 0)) return fail(CR_ERR_INVALID_ARGUMENT, "triangles need at least one mesh");
+    if (nMeshes && (!mats || nMats == 0)) return fail(CR_ERR_INVALID_ARGUMENT, "meshes need materials");
+    if (nEmissive && !emissive) return fail(CR_ERR_INVALID_ARGUMENT, "emissive list is NULL");
+    if (nv >= 0xffffffffull) return fail(CR_ERR_UNSUPPORTED, "too many vertices (%llu)", (unsigned long long)nv);
+    for (uint64_t i = 0; i < 3 * nv; i++)
+        if (!std::isfinite(pos[i])) return fail(CR_ERR_INVALID_ARGUMENT, "vertex position %llu is not finite",
+                                                (unsigned long long)(i / 3));
+    for (uint64_t i = 0; i < 3 * nt; i++)
+        if (idx[i] >= nv) return fail(CR_ERR_INVALID_ARGUMENT, "index %llu = %u is out of range (%llu vertices)",
+                                      (unsigned long long)i, idx[i], (unsigned long long)nv);
+    // primitive -> mesh, Scene/Triangle.cu:121-131
+    std::vector<uint32_t> primToMesh(nt, 0);
+    for (uint32_t m = 0; m < nMeshes; m++) {
+        if (meshes[m].material_id >= nMats)
+            return fail(CR_ERR_INVALID_ARGUMENT, "mesh %u uses material %u of %u", m, meshes[m].material_id, nMats);
+        if (meshes[m].index_offset % 3 || meshes[m].index_count % 3 ||
+            (uint64_t)meshes[m].index_offset + meshes[m].index_count > 3 * nt)
+            return fail(CR_ERR_INVALID_ARGUMENT, "mesh %u index range is invalid", m);
+        const uint32_t start = meshes[m].index_offset / 3u, count = meshes[m].index_count / 3u;
+        for (uint32_t k = 0; k < count; k++) primToMesh[start + k] = m;
+    }
+    for (uint32_t e = 0; e < nEmissive; e++)
+        if (emissive[e] >= nt) return fail(CR_ERR_INVALID_ARGUMENT, "emitter %u = %u is not a triangle", e, emissive[e]);
+    std::vector<MaterialGpu> gm(nMats);
+    for (uint32_t m = 0; m < nMats; m++) {
+        if (mats[m].type > CR_MATERIAL_PHONG) return fail(CR_ERR_INVALID_ARGUMENT, "material %u type %u", m, mats[m].type);
+        gm[m] = deriveMaterial(mats[m]);
+    }
+    std::vector<float> zeros;
+    s->nv = nv;
+    s->nt = nt;
+    s->nMeshes = nMeshes;
+    s->nMats = nMats;
+    s->nEmissive = nEmissive;
+    int rc;
+    if ((rc = upload(&s->pos, reinterpret_cast<const float3*>(pos), nv))) return rc;
+    if (!nrm || !uv) zeros.assign(3 * std::max<uint64_t>(nv, 1), 0.0f);
+    if ((rc = upload(&s->nrm, reinterpret_cast<const float3*>(nrm ? nrm : zeros.data()), nv))) return rc;
+    if ((rc = upload(&s->uv, reinterpret_cast<const float2*>(uv ? uv : zeros.data()), nv))) return rc;
+    if ((rc = upload(&s->idx, idx, 3 * nt))) return rc;
+    if ((rc = upload(&s->primToMesh, primToMesh.data(), nt))) return rc;
+    if ((rc = upload(&s->meshes, meshes, nMeshes))) return rc;
+    if ((rc = upload(&s->mats, gm.data(), nMats))) return rc;
+    if ((rc = upload(&s->emissive, emissive, nEmissive))) return rc;
+    CR_CUDA(cudaMalloc(&s->errFlags, 4));
+    CR_CUDA(cudaMemset(s->errFlags, 0, 4));
+    CR_CUDA(cudaMalloc(&s->rayCounter, sizeof(unsigned long long)));
+    CR_CUDA(cudaMemset(s->rayCounter, 0, sizeof(unsigned long long)));
+    return buildBvh(s);
+}
+
+}  // namespace
+
+MaterialGpu deriveMaterialPublic(const cr_material& m) { return deriveMaterial(m); }
+
+}  // namespace cr
+
+using namespace cr;
+
+extern "C" {
+
+const char* cr_last_error(void) { return gError.c_str(); }
+
+const char* cr_version(void) { return "craystal_gb300 0.1 (sm_103a)"; }
+
+uint64_t cr_kernel_launch_count(void) { return gLaunches.load(); }
+
+int cr_set_device(int device) {
+    clearError();
+    CR_CUDA(cudaSetDevice(device));
+    return CR_OK;
+}
+
+int cr_scene_create(const float* pos, const float* nrm, const float* uv, uint64_t n_vertices, const uint32_t* idx,
+                    uint64_t n_tris, const cr_mesh_desc* meshes, uint32_t n_meshes, const cr_material* mats,
+                    uint32_t n_mats, const uint32_t* emissive, uint32_t n_emissive, cr_scene** out) {
+    clearError();
+    if (!out) return fail(CR_ERR_INVALID_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    cr_scene* s = new cr_scene();
+    CR_CUDA(cudaGetDevice(&s->device));
+    int rc = createScene(pos, nrm, uv, n_vertices, idx, n_tris, meshes, n_meshes, mats, n_mats, emissive, n_emissive, s);
+    if (rc) {
+        std::string msg = gError;
+        freeScene(s);
+        gError = msg;
+        return rc;
+    }
+    *out = s;
+    return CR_OK;
+}
+
+int cr_scene_destroy(cr_scene* scene) {
+    clearError();
+    freeScene(scene);
+    return CR_OK;
+}
+
+int cr_scene_bvh_stats(const cr_scene* scene, cr_bvh_stats* out) {
+    clearError();
+    if (!scene || !out) return fail(CR_ERR_INVALID_ARGUMENT, "NULL argument");
+    *out = scene->stats;
+    return CR_OK;
+}
+
+int cr_scene_bvh_export(const cr_scene* scene, cr_bvh_node* nodes, uint32_t* prim_map) {
+    clearError();
+    if (!scene) return fail(CR_ERR_INVALID_ARGUMENT, "scene is NULL");
+    CR_CUDA(cudaSetDevice(scene->device));
+    return exportBvh(scene, nodes, prim_map);
+}
+
+int cr_scene_set_camera(cr_scene* scene, const cr_camera* cam) {
+    clearError();
+    if (!scene || !cam) return fail(CR_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (cam->width == 0 || cam->height == 0 || cam->width > 65536 || cam->height > 65536)
+        return fail(CR_ERR_INVALID_ARGUMENT, "sensor size %ux%u", cam->width, cam->height);
+    CR_CUDA(cudaSetDevice(scene->device));
+    // Camera::calculateCameraData, Core/Camera.cu:35-39
+    const float3 pos = mk3(cam->pos[0], cam->pos[1], cam->pos[2]);
+    const float3 tgt = mk3(cam->target[0], cam->target[1], cam->target[2]);
+    const float3 up = mk3(cam->up[0], cam->up[1], cam->up[2]);
+    CameraGpu c;
+    c.pos = pos;
+    c.W = normalize(sub(tgt, pos));
+    c.U = normalize(cross(c.W, up));
+    c.V = normalize(cross(c.U, c.W));
+    // CameraProxy::generateRay, Core/CameraProxy.h:32-35: the tangent is
+    // evaluated in double (fovY * 0.5 promotes) and stored as float
+    c.halfH = (float)std::tan(((double)cam->fov_y * 0.5) * 0.01745329251994329576923690768489);
+    const float aspect = (float)cam->width / (float)cam->height;
+    c.halfW = aspect * c.halfH;
+    c.width = cam->width;
+    c.height = cam->height;
+    const bool resize = !scene->hasCamera || scene->cam.width != c.width || scene->cam.height != c.height;
+    if (resize) {
+        if (scene->filmRgb) cudaFree(scene->filmRgb);
+        if (scene->filmW) cudaFree(scene->filmW);
+        scene->filmRgb = nullptr;
+        scene->filmW = nullptr;
+        const size_t px = (size_t)c.width * c.height;
+        CR_CUDA(cudaMalloc(&scene->filmRgb, px * 3 * sizeof(float)));
+        CR_CUDA(cudaMalloc(&scene->filmW, px * sizeof(float)));
+        CR_CUDA(cudaMemset(scene->filmRgb, 0, px * 3 * sizeof(float)));
+        CR_CUDA(cudaMemset(scene->filmW, 0, px * sizeof(float)));
+        CR_CUDA(cudaMemset(scene->rayCounter, 0, sizeof(unsigned long long)));
+    }
+    scene->cam = c;
+    scene->hasCamera = true;
+    return CR_OK;
+}
+
+int cr_film_clear(cr_scene* scene) {
+    clearError();
+    if (!scene || !scene->hasCamera) return fail(CR_ERR_INVALID_ARGUMENT, "scene has no camera / film");
+    CR_CUDA(cudaSetDevice(scene->device));
+    CR_CUDA(cudaDeviceSynchronize());
+    const size_t px = (size_t)scene->cam.width * scene->cam.height;
+    CR_CUDA(cudaMemset(scene->filmRgb, 0, px * 3 * sizeof(float)));
+    CR_CUDA(cudaMemset(scene->filmW, 0, px * sizeof(float)));
+    CR_CUDA(cudaMemset(scene->rayCounter, 0, sizeof(unsigned long long)));
+    CR_CUDA(cudaDeviceSynchronize());
+    return CR_OK;
+}
+
+int cr_film_read(cr_scene* scene, float* rgb, float* weight) {
+    clearError();
+    if (!scene || !scene->hasCamera) return fail(CR_ERR_INVALID_ARGUMENT, "scene has no camera / film");
+    CR_CUDA(cudaSetDevice(scene->device));
+    CR_CUDA(cudaDeviceSynchronize());
+    const size_t px = (size_t)scene->cam.width * scene->cam.height;
+    if (rgb) CR_CUDA(cudaMemcpy(rgb, scene->filmRgb, px * 3 * sizeof(float), cudaMemcpyDeviceToHost));
+    if (weight) CR_CUDA(cudaMemcpy(weight, scene->filmW, px * sizeof(float), cudaMemcpyDeviceToHost));
+    uint32_t err = 0;
+    CR_CUDA(cudaMemcpy(&err, scene->errFlags, 4, cudaMemcpyDeviceToHost));
+    if (err) return fail(CR_ERR_DEVICE, "render reported device error flags 0x%x", err);
+    return CR_OK;
+}
+
+int cr_film_resolve(cr_scene* scene, float* rgb) {
+    clearError();
+    if (!scene || !scene->hasCamera || !rgb) return fail(CR_ERR_INVALID_ARGUMENT, "scene has no film / rgb is NULL");
+    CR_CUDA(cudaSetDevice(scene->device));
+    return resolveFilm(scene, rgb);
+}
+
+int cr_render(cr_scene* scene, const cr_integrator_config* cfg, uint32_t spp, uint32_t first_sample, void* stream) {
+    clearError();
+    if (!scene || !cfg) return fail(CR_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (!scene->hasCamera) return fail(CR_ERR_INVALID_ARGUMENT, "scene has no camera; call cr_scene_set_camera");
+    if (cfg->max_depth > 1024) return fail(CR_ERR_INVALID_ARGUMENT, "max_depth %u", cfg->max_depth);
+    CR_CUDA(cudaSetDevice(scene->device));
+    return renderDevice(scene, cfg, spp, first_sample, static_cast<cudaStream_t>(stream));
+}
+
+int cr_render_ray_count(cr_scene* scene, uint64_t* rays) {
+    clearError();
+    if (!scene || !rays) return fail(CR_ERR_INVALID_ARGUMENT, "NULL argument");
+    CR_CUDA(cudaSetDevice(scene->device));
+    CR_CUDA(cudaDeviceSynchronize());
+    unsigned long long v = 0;
+    CR_CUDA(cudaMemcpy(&v, scene->rayCounter, sizeof(v), cudaMemcpyDeviceToHost));
+    *rays = v;
+    return CR_OK;
+}
+
+}  // extern "C"

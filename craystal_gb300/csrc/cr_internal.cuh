@@ -1,0 +1,217 @@
+// cr_internal.cuh -- types and device helpers shared by the craystal_gb300
+// translation units.
+//
+// Every translation unit is compiled with -fmad=false (device) and
+// -ffp-contract=off (host): each float multiply and add is rounded on its
+// own, in the order written, which is the order of the reference source
+// (glm 1.0.1 for dot / cross / normalize / reflect / mat3 * vec3).  Division
+// and square root are IEEE round-to-nearest (-prec-div / -prec-sqrt on).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "craystal_c.h"
+
+namespace cr {
+
+// ---------------------------------------------------------------------------
+// error plumbing
+// ---------------------------------------------------------------------------
+void setError(const char* fmt, ...);
+void clearError();
+int fail(int code, const char* fmt, ...);
+void countLaunch(uint64_t n = 1);
+
+#define CR_CUDA(call)                                                              \
+    do {                                                                           \
+        cudaError_t _e = (call);                                                   \
+        if (_e != cudaSuccess) {                                                   \
+            return ::cr::fail(_e == cudaErrorMemoryAllocation ? CR_ERR_OUT_OF_MEMORY \
+                                                             : CR_ERR_CUDA,        \
+                              "%s failed: %s (%s:%d)", #call,                      \
+                              cudaGetErrorString(_e), __FILE__, __LINE__);         \
+        }                                                                          \
+    } while (0)
+
+#define CR_LAUNCH_CHECK()                                                          \
+    do {                                                                           \
+        ::cr::countLaunch();                                                       \
+        cudaError_t _e = cudaGetLastError();                                       \
+        if (_e != cudaSuccess)                                                     \
+            return ::cr::fail(CR_ERR_CUDA, "kernel launch failed: %s (%s:%d)",      \
+                              cudaGetErrorString(_e), __FILE__, __LINE__);         \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// constants, Math/MathDefs.h:12-20
+// ---------------------------------------------------------------------------
+constexpr float kEps = 1e-6f;
+constexpr float kPi = 3.14159265358979323846f;
+constexpr float k2Pi = 2.f * kPi;
+constexpr float kInvPi = 1.f / kPi;
+constexpr float kInv2Pi = 0.5f / kPi;
+constexpr float kFltEps = 1.19209290e-07f;  // std::numeric_limits<float>::epsilon()
+
+// Device error flags (bits of Scene::errFlags).
+constexpr uint32_t kErrStackOverflow = 1u;
+
+// ---------------------------------------------------------------------------
+// GPU-resident scene layout
+// ---------------------------------------------------------------------------
+
+// One interior node of the binary BVH with both children's boxes in one
+// 64-byte record, so a visit is four coalesced 16-byte loads.
+//   p0 = (L.min.x, L.min.y, L.min.z, L.max.x)
+//   p1 = (L.max.y, L.max.z, R.min.x, R.min.y)
+//   p2 = (R.min.z, R.max.x, R.max.y, R.max.z)
+//   ref = (L.ref, R.ref, flags, 0).  A child ref with bit 31 clear is the
+//         pair index of an interior child; with bit 31 set, bits 0-30 index
+//         the leaf table (first leaf slot, triangle count).  flags bits 0-2
+//         (left) and 3-5 (right) mark box axes thinner than FLT_EPSILON,
+//         which take the degenerate-slab branch of Math/AABB.cu:10-19.
+struct __align__(64) NodePair {
+    float4 p0, p1, p2;
+    uint4 ref;
+};
+
+// Triangle block per leaf slot (48 B): v0 with the primitive id in .w,
+// e1 = v1 - v0 and e2 = v2 - v0 exactly as Moller-Trumbore forms them.
+struct __align__(16) TriBlock {
+    float4 v0;
+    float4 e1;
+    float4 e2;
+};
+
+// Node produced by the GPU builder (breadth-first numbering).
+struct __align__(16) BuildNode {
+    float4 lo;   // min.xyz
+    float4 hi;   // max.xyz
+    uint4 info;  // (a, b, isLeaf, depth): leaf (start, count), interior (left, right)
+};
+
+struct MaterialGpu {
+    float kd[3];
+    float ks[3];
+    float em[3];
+    float shininess;
+    uint32_t type;
+    uint32_t flags;
+    // derived once per material, as the BSDF constructors compute them
+    float dProb, sProb;       // lobe selection (Phong, Principled)
+    float rough, metal;       // Principled
+};
+
+struct CameraGpu {
+    float3 pos, U, V, W;
+    float halfH, halfW;
+    uint32_t width, height;
+};
+
+// Everything a traversal or render kernel reads, passed by value.
+constexpr uint32_t kLeafBit = 0x80000000u;
+
+struct SceneView {
+    const NodePair* pairs;
+    const uint2* leaves;
+    const TriBlock* tris;
+    const float3* pos;
+    const float3* nrm;
+    const float2* uv;
+    const uint32_t* idx;
+    const uint32_t* primToMesh;
+    const cr_mesh_desc* meshes;
+    const MaterialGpu* mats;
+    const uint32_t* emissive;
+    uint32_t nEmissive;
+    uint32_t rootRef;              // same encoding as a child ref
+    uint32_t rootFlags;            // degenerate axes of the root box
+    float3 rootMin, rootMax;
+    uint32_t hasRoot;
+    uint32_t* errFlags;
+};
+
+}  // namespace cr
+
+struct cr_scene {
+    int device = 0;
+    uint64_t nv = 0, nt = 0;
+    uint32_t nMeshes = 0, nMats = 0, nEmissive = 0;
+    float3* pos = nullptr;
+    float3* nrm = nullptr;
+    float2* uv = nullptr;
+    uint32_t* idx = nullptr;
+    uint32_t* primToMesh = nullptr;
+    cr_mesh_desc* meshes = nullptr;
+    cr::MaterialGpu* mats = nullptr;
+    uint32_t* emissive = nullptr;
+    // BVH
+    cr::NodePair* pairs = nullptr;
+    uint32_t nPairs = 0;
+    uint2* leaves = nullptr;
+    uint32_t nLeaves = 0;
+    cr::TriBlock* tris = nullptr;
+    uint32_t* slotToPrim = nullptr;
+    cr::BuildNode* buildNodes = nullptr;
+    uint32_t nBuildNodes = 0;
+    uint32_t rootRef = 0, rootFlags = 0, hasRoot = 0;
+    float3 rootMin{0, 0, 0}, rootMax{0, 0, 0};
+    cr_bvh_stats stats{};
+    uint32_t* errFlags = nullptr;
+    // camera + film
+    bool hasCamera = false;
+    cr::CameraGpu cam{};
+    float* filmRgb = nullptr;
+    float* filmW = nullptr;
+    unsigned long long* rayCounter = nullptr;
+    // host trace staging
+    cudaStream_t streams[2] = {nullptr, nullptr};
+    cr_ray* stageRays[2] = {nullptr, nullptr};
+    cr_hit* stageHits[2] = {nullptr, nullptr};
+    uint8_t* stageOcc[2] = {nullptr, nullptr};
+    uint64_t stageCap = 0;
+
+    cr::SceneView view() const {
+        cr::SceneView v;
+        v.pairs = pairs;
+        v.leaves = leaves;
+        v.tris = tris;
+        v.pos = pos;
+        v.nrm = nrm;
+        v.uv = uv;
+        v.idx = idx;
+        v.primToMesh = primToMesh;
+        v.meshes = meshes;
+        v.mats = mats;
+        v.emissive = emissive;
+        v.nEmissive = nEmissive;
+        v.rootRef = rootRef;
+        v.rootFlags = rootFlags;
+        v.rootMin = rootMin;
+        v.rootMax = rootMax;
+        v.hasRoot = hasRoot;
+        v.errFlags = errFlags;
+        return v;
+    }
+};
+
+namespace cr {
+
+// implemented in cr_bvh.cu
+int buildBvh(cr_scene* s);
+int exportBvh(const cr_scene* s, cr_bvh_node* nodes, uint32_t* primMap);
+// implemented in cr_trace.cu
+int traceClosestDevice(cr_scene* s, const cr_ray* rays, uint64_t n, cr_hit* hits, cudaStream_t st);
+int traceOccludedDevice(cr_scene* s, const cr_ray* rays, uint64_t n, uint8_t* occ, cudaStream_t st);
+// implemented in cr_render.cu
+int renderDevice(cr_scene* s, const cr_integrator_config* cfg, uint32_t spp, uint32_t first,
+                 cudaStream_t st);
+int resolveFilm(cr_scene* s, float* rgbHost);
+
+}  // namespace cr

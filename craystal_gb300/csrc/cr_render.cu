@@ -1,0 +1,455 @@
+// cr_render.cu -- the path-tracing megakernel (pathTraceKernel<useMIS>,
+// Core/Integrator.cu:142-227, with sampleLight :21-72 and evalMIS :74-140)
+// and the film (SensorData::addSample, Core/Sensor.cu:19-43; resolve
+// Sensor::createImage, :93-112).
+//
+// One thread owns one pixel and loops over a run of sample indices; the
+// launch covers (16 x 16 pixel tiles) x (runs of samples), so that small
+// images still fill the GPU.  Film splats go to an 18 x 18 tile in shared
+// memory (the 16 x 16 pixels plus the one-pixel apron the triangle filter
+// of radius 1 reaches) and are added to the global film once per block,
+// instead of 16 global atomics per sample in the reference.
+
+#include "cr_internal.cuh"
+#include "cr_math.cuh"
+#include "cr_shading.cuh"
+#include "cr_traverse.cuh"
+
+namespace cr {
+namespace {
+
+constexpr int kTileW = 16;
+constexpr int kApron = 18;
+
+struct Params {
+    uint32_t maxDepth;
+    float rrThreshold;
+    uint32_t useMIS;
+    uint32_t spp;
+    uint32_t first;
+    uint32_t sppPerBlock;
+};
+
+struct PathCtx {
+    const SceneView& sc;
+    uint32_t rays;
+};
+
+__device__ __forceinline__ bool closest(PathCtx& c, float3 o, float3 d, THit& h) {
+    c.rays++;
+    h.t = INFINITY;
+    h.prim = CR_MISS;
+    h.u = h.v = 0.0f;
+    return traverse<false>(c.sc, makeTRay(o, 0.0f, d, INFINITY), h);
+}
+
+__device__ __forceinline__ bool occluded(PathCtx& c, float3 o, float3 d, float tMax) {
+    c.rays++;
+    THit h;
+    h.t = INFINITY;
+    return traverse<true>(c.sc, makeTRay(o, 0.0f, d, tMax), h);
+}
+
+struct LightSample {
+    Spec weight;
+    float3 dirW;
+    float pdf;
+    uint32_t id;
+    float selectPdf;
+};
+
+// sampleLight, Core/Integrator.cu:21-72
+__device__ LightSample sampleLight(PathCtx& c, const Isect& it, const Bsdf& bsdf, Sampler& smp) {
+    const SceneView& sc = c.sc;
+    LightSample ls;
+    ls.weight = sp(0.0f);
+    ls.dirW = mk3(0.0f, 0.0f, 0.0f);
+    ls.pdf = 0.0f;
+    ls.id = 0;
+    ls.selectPdf = 0.0f;
+    const int cnt = (int)sc.nEmissive;
+    if (cnt == 0) return ls;
+    const int pick = min(f2iX86((float)cnt * smp.next1D()), cnt - 1);
+    const uint32_t id = sc.emissive[pick];
+    const TriVerts tri = loadTriangle(sc, id);
+    const float2 b = sampleBarycentric(smp.next2D());
+    const float3 w = mk3((1.f - b.x) - b.y, b.x, b.y);
+    const float3 vp = interp(tri.p, w);
+    const float3 vn = interp(tri.n, w);
+    const float3 target = offsetRayOrigin(vp, faceNormal(tri));
+    const float3 toLight = sub(target, it.posW);
+    const float distSqr = dot(toLight, toLight);
+    const float dist = sqrtf(distSqr);
+    const float3 dir = divs(toLight, dist);
+    const float3 ofn = it.orientedFaceNormal();
+    if (dot(ofn, dir) < 0.0f || dot(vn, dir) > 0.0f || dist < kEps) return ls;
+    const float3 so = offsetRayOrigin(it.posW, ofn);
+    const float tMax = length(sub(so, target)) - kEps;
+    if (occluded(c, so, dir, tMax)) return ls;
+    const MaterialGpu& m = materialOf(sc, id);
+    ls.weight = mul(bsdf.evaluate(it.viewW, dir), sp(m.em[0], m.em[1], m.em[2]));
+    ls.dirW = dir;
+    ls.pdf = distSqr / (triArea(tri) * absDot(dir, vn));
+    ls.id = id;
+    ls.selectPdf = (float)(1.0 / (double)cnt);
+    return ls;
+}
+
+// evalMIS, Core/Integrator.cu:74-140
+__device__ Spec evalMIS(PathCtx& c, const Isect& it, const Bsdf& bsdf, Sampler& smp) {
+    const SceneView& sc = c.sc;
+    Spec value = sp(0.0f);
+    const LightSample ls = sampleLight(c, it, bsdf, smp);
+    if (ls.pdf <= 0.0f) return value;
+    {
+        const float lightPdf = ls.pdf;
+        if (lightPdf > 0.0f) {
+            const float bsdfPdf = bsdf.evaluatePdf(it.viewW, ls.dirW);
+            if (bsdfPdf > 0.0f) value = add(value, divs(mul(powerHeuristic(lightPdf, bsdfPdf), ls.weight), lightPdf));
+        }
+    }
+    {
+        float3 dir;
+        float bsdfPdf = 0.0f;
+        const Spec w = bsdf.sampleEvaluate(smp.next2D(), it.viewW, dir, bsdfPdf);
+        if (maxValue(w) > 0.0f && bsdfPdf > 0.0f) {
+            const float3 o = offsetRayOrigin(it.posW, it.orientedFaceNormal());
+            THit h;
+            if (closest(c, o, dir, h) && h.prim == ls.id) {
+                // createIntersection of the light hit: only its position and
+                // face normal are read
+                const TriVerts tri = loadTriangle(sc, h.prim);
+                const float3 lpos = add(o, mul(h.t, dir));
+                const float3 lfn = faceNormal(tri);
+                const MaterialGpu& m = materialOf(sc, h.prim);
+                if (m.flags & CR_MATERIAL_EMISSIVE) {
+                    const Spec em = sp(m.em[0], m.em[1], m.em[2]);
+                    const float3 toLight = sub(lpos, it.posW);
+                    const float distSqr = dot(toLight, toLight);
+                    const float3 lv = divs(toLight, sqrtf(distSqr));
+                    const float cosL = absDot(lv, lfn);
+                    if (cosL != 0.0f) {
+                        const float area = triArea(tri);
+                        const float lightPdf = distSqr / (area * cosL);
+                        value = add(value, divs(mul(mul(powerHeuristic(bsdfPdf, lightPdf), em), w), bsdfPdf));
+                    }
+                }
+            }
+        }
+    }
+    return divs(value, ls.selectPdf);
+}
+
+// CameraProxy::generateRay, Core/CameraProxy.h:25-40
+__device__ __forceinline__ float3 cameraDir(const CameraGpu& cam, float2 s) {
+    const float u = 2.0f * (s.x / (float)cam.width) - 1.0f;
+    const float v = 1.0f - 2.0f * (s.y / (float)cam.height);
+    return normalize(add(add(mul(cam.U, u * cam.halfW), mul(cam.V, v * cam.halfH)), cam.W));
+}
+
+// pathTraceKernel body for one (pixel, sample index).
+__device__ Spec tracePath(PathCtx& c, const CameraGpu& cam, const Params& p, uint32_t x, uint32_t y, uint32_t si,
+                          float2& pixel) {
+    const SceneView& sc = c.sc;
+    Sampler smp(x, y, si);
+    const float2 j = smp.next2D();
+    pixel = make_float2((float)x + j.x, (float)y + j.y);
+    float3 ro = cam.pos;
+    float3 rd = cameraDir(cam, pixel);
+    Spec radiance = sp(0.0f), beta = sp(1.0f);
+    for (uint32_t depth = 0; depth < p.maxDepth; depth++) {
+        bool terminate = false;
+        THit h;
+        if (closest(c, ro, rd, h)) {
+            const Isect it = makeIsect(sc, ro, rd, h.t, h.u, h.v, h.prim);
+            const MaterialGpu& m = materialOf(sc, h.prim);
+            if (m.flags & CR_MATERIAL_EMISSIVE) {
+                radiance = add(radiance, mul(sp(m.em[0], m.em[1], m.em[2]), beta));
+                break;
+            }
+            Bsdf bsdf;
+            bsdf.init(m, it.frame);
+            if (p.useMIS) {
+                radiance = add(radiance, mul(evalMIS(c, it, bsdf, smp), beta));
+            } else {
+                const LightSample ls = sampleLight(c, it, bsdf, smp);
+                if (ls.pdf > 0.0f) radiance = add(radiance, divs(divs(mul(ls.weight, beta), ls.pdf), ls.selectPdf));
+            }
+            float3 wi;
+            float pdf = 0.0f;
+            const Spec f = bsdf.sampleEvaluate(smp.next2D(), it.viewW, wi, pdf);
+            if (pdf <= 0.0f) break;
+            beta = mul(beta, divs(f, pdf));
+            ro = offsetRayOrigin(it.posW, it.orientedFaceNormal());
+            rd = wi;
+        } else {
+            terminate = true;
+        }
+        if (smp.next1D() < p.rrThreshold) terminate = true;
+        if (terminate) break;
+        if (depth > 5) {
+            float q = smax(p.rrThreshold, 1.0f - maxValue(beta));
+            q = q < 0.0f ? 0.0f : (1.0f < q ? 1.0f : q);
+            if (smp.next1D() < q) break;
+            beta = divs(beta, 1.0f - q);
+        }
+    }
+    return radiance;
+}
+
+__global__ void __launch_bounds__(kTileW* kTileW) kRender(const SceneView sc, const CameraGpu cam, const Params p,
+                                                          float* __restrict__ filmRgb, float* __restrict__ filmW,
+                                                          unsigned long long* __restrict__ rayCounter) {
+    __shared__ float tile[kApron * kApron * 4];
+    __shared__ uint32_t warpRays[kTileW * kTileW / 32];
+    const int tid = threadIdx.y * kTileW + threadIdx.x;
+    for (int i = tid; i < kApron * kApron * 4; i += kTileW * kTileW) tile[i] = 0.0f;
+    __syncthreads();
+    const int tx0 = blockIdx.x * kTileW, ty0 = blockIdx.y * kTileW;
+    const uint32_t x = tx0 + threadIdx.x, y = ty0 + threadIdx.y;
+    PathCtx c{sc, 0u};
+    if (x < cam.width && y < cam.height) {
+        const uint32_t s0 = blockIdx.z * p.sppPerBlock;
+        const uint32_t s1 = min(p.spp, s0 + p.sppPerBlock);
+        for (uint32_t s = s0; s < s1; s++) {
+            float2 pix;
+            const Spec L = tracePath(c, cam, p, x, y, p.first + s, pix);
+            // SensorData::addSample, Core/Sensor.cu:19-43
+            if (isnan(L.r) || isnan(L.g) || isnan(L.b) || isinf(L.r) || isinf(L.g) || isinf(L.b)) continue;
+            int xa = (int)floorf(pix.x - 1.0f), ya = (int)floorf(pix.y - 1.0f);
+            int xb = (int)ceilf(pix.x + 1.0f), yb = (int)ceilf(pix.y + 1.0f);
+            xa = max(xa, 0);
+            ya = max(ya, 0);
+            xb = min(xb, (int)cam.width - 1);
+            yb = min(yb, (int)cam.height - 1);
+            for (int yy = ya; yy <= yb; yy++) {
+                for (int xx = xa; xx <= xb; xx++) {
+                    const float dx = pix.x - ((float)xx + 0.5f), dy = pix.y - ((float)yy + 0.5f);
+                    const float w = smax(0.0f, 1.0f - fabsf(dx)) * smax(0.0f, 1.0f - fabsf(dy));
+                    if (w == 0.0f) continue;  // adding +0 leaves the film unchanged
+                    const int lx = xx - tx0 + 1, ly = yy - ty0 + 1;
+                    if (lx >= 0 && lx < kApron && ly >= 0 && ly < kApron) {
+                        float* cell = tile + (ly * kApron + lx) * 4;
+                        atomicAdd(cell + 0, L.r * w);
+                        atomicAdd(cell + 1, L.g * w);
+                        atomicAdd(cell + 2, L.b * w);
+                        atomicAdd(cell + 3, w);
+                    } else {
+                        const size_t pi = (size_t)yy * cam.width + xx;
+                        atomicAdd(filmRgb + 3 * pi + 0, L.r * w);
+                        atomicAdd(filmRgb + 3 * pi + 1, L.g * w);
+                        atomicAdd(filmRgb + 3 * pi + 2, L.b * w);
+                        atomicAdd(filmW + pi, w);
+                    }
+                }
+            }
+        }
+    }
+    uint32_t r = c.rays;
+    for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+    if ((tid & 31) == 0) warpRays[tid >> 5] = r;
+    __syncthreads();
+    if (tid == 0) {
+        unsigned long long s = 0;
+        for (int k = 0; k < kTileW * kTileW / 32; k++) s += warpRays[k];
+        atomicAdd(rayCounter, s);
+    }
+    for (int i = tid; i < kApron * kApron; i += kTileW * kTileW) {
+        const float* cell = tile + i * 4;
+        if (cell[3] == 0.0f && cell[0] == 0.0f && cell[1] == 0.0f && cell[2] == 0.0f) continue;
+        const int gx = tx0 - 1 + i % kApron, gy = ty0 - 1 + i / kApron;
+        if (gx < 0 || gy < 0 || gx >= (int)cam.width || gy >= (int)cam.height) continue;
+        const size_t pi = (size_t)gy * cam.width + gx;
+        atomicAdd(filmRgb + 3 * pi + 0, cell[0]);
+        atomicAdd(filmRgb + 3 * pi + 1, cell[1]);
+        atomicAdd(filmRgb + 3 * pi + 2, cell[2]);
+        atomicAdd(filmW + pi, cell[3]);
+    }
+}
+
+__global__ void kResolve(const float* __restrict__ rgb, const float* __restrict__ w, size_t n, float* __restrict__ out) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float ws = w[i];
+    out[3 * i + 0] = rgb[3 * i + 0] / ws;
+    out[3 * i + 1] = rgb[3 * i + 1] / ws;
+    out[3 * i + 2] = rgb[3 * i + 2] / ws;
+}
+
+}  // namespace
+
+int renderDevice(cr_scene* s, const cr_integrator_config* cfg, uint32_t spp, uint32_t first, cudaStream_t st) {
+    if (spp == 0) return CR_OK;
+    Params p;
+    p.maxDepth = cfg->max_depth;
+    p.rrThreshold = cfg->rr_threshold;
+    p.useMIS = cfg->use_mis ? 1u : 0u;
+    p.spp = spp;
+    p.first = first;
+    const uint32_t tilesX = (s->cam.width + kTileW - 1) / kTileW, tilesY = (s->cam.height + kTileW - 1) / kTileW;
+    // enough blocks to fill every SM several times over, at most 8 samples
+    // per thread per launch run
+    int dev = 0, sms = 0;
+    CR_CUDA(cudaGetDevice(&dev));
+    CR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const uint64_t tiles = (uint64_t)tilesX * tilesY;
+    const uint64_t wantBlocks = (uint64_t)sms * 32;
+    uint32_t runs = (uint32_t)std::min<uint64_t>(spp, std::max<uint64_t>(1, (wantBlocks + tiles - 1) / tiles));
+    runs = std::max(runs, (spp + 7) / 8);
+    runs = std::min(runs, 65535u);
+    p.sppPerBlock = (spp + runs - 1) / runs;
+    runs = (spp + p.sppPerBlock - 1) / p.sppPerBlock;
+    dim3 grid(tilesX, tilesY, runs), block(kTileW, kTileW, 1);
+    kRender<<<grid, block, 0, st>>>(s->view(), s->cam, p, s->filmRgb, s->filmW, s->rayCounter);
+    CR_LAUNCH_CHECK();
+    return CR_OK;
+}
+
+int resolveFilm(cr_scene* s, float* rgbHost) {
+    const size_t n = (size_t)s->cam.width * s->cam.height;
+    float* d = nullptr;
+    CR_CUDA(cudaDeviceSynchronize());
+    CR_CUDA(cudaMalloc(&d, n * 3 * sizeof(float)));
+    kResolve<<<(unsigned)((n + 255) / 256), 256>>>(s->filmRgb, s->filmW, n, d);
+    cudaError_t e = cudaGetLastError();
+    countLaunch();
+    if (e == cudaSuccess) e = cudaMemcpy(rgbHost, d, n * 3 * sizeof(float), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return fail(CR_ERR_CUDA, "film resolve failed: %s", cudaGetErrorString(e));
+    return CR_OK;
+}
+
+}  // namespace cr
+
+// ---------------------------------------------------------------------------
+// batch entry points for single stages: camera rays and BSDF queries
+// ---------------------------------------------------------------------------
+namespace cr {
+namespace {
+
+__global__ void kCameraRays(const CameraGpu cam, const float2* __restrict__ sp, uint64_t n, cr_ray* __restrict__ out) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float3 d = cameraDir(cam, sp[i]);
+    cr_ray r;
+    r.o[0] = cam.pos.x;
+    r.o[1] = cam.pos.y;
+    r.o[2] = cam.pos.z;
+    r.tmin = 0.0f;
+    r.d[0] = d.x;
+    r.d[1] = d.y;
+    r.d[2] = d.z;
+    r.tmax = INFINITY;
+    out[i] = r;
+}
+
+__global__ void kBsdf(const MaterialGpu m, const float3* __restrict__ nrm, const float3* __restrict__ wo,
+                      const float3* __restrict__ wi, const float2* __restrict__ u, uint64_t n, float3* __restrict__ wiOut,
+                      float3* __restrict__ f, float* __restrict__ pdf) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Frame fr;
+    fr.build(nrm[i]);
+    Bsdf b;
+    b.init(m, fr);
+    Spec v;
+    float p;
+    if (u) {
+        float3 w;
+        p = 0.0f;
+        v = b.sampleEvaluate(u[i], wo[i], w, p);
+        wiOut[i] = w;
+    } else {
+        v = b.evaluate(wo[i], wi[i]);
+        p = b.evaluatePdf(wo[i], wi[i]);
+    }
+    f[i] = mk3(v.r, v.g, v.b);
+    pdf[i] = p;
+}
+
+template <class T>
+struct Dev {
+    T* p = nullptr;
+    ~Dev() {
+        if (p) cudaFree(p);
+    }
+};
+
+}  // namespace
+
+MaterialGpu deriveMaterialPublic(const cr_material& m);
+
+}  // namespace cr
+
+using namespace cr;
+
+extern "C" int cr_camera_generate_rays(const cr_camera* cam, const float* sensor_pos, uint64_t n, cr_ray* rays) {
+    clearError();
+    if (!cam || (n && (!sensor_pos || !rays))) return fail(CR_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (cam->width == 0 || cam->height == 0) return fail(CR_ERR_INVALID_ARGUMENT, "sensor size is zero");
+    if (n == 0) return CR_OK;
+    CameraGpu c;
+    const float3 pos = mk3(cam->pos[0], cam->pos[1], cam->pos[2]);
+    c.pos = pos;
+    c.W = normalize(sub(mk3(cam->target[0], cam->target[1], cam->target[2]), pos));
+    c.U = normalize(cross(c.W, mk3(cam->up[0], cam->up[1], cam->up[2])));
+    c.V = normalize(cross(c.U, c.W));
+    c.halfH = (float)std::tan(((double)cam->fov_y * 0.5) * 0.01745329251994329576923690768489);
+    c.halfW = ((float)cam->width / (float)cam->height) * c.halfH;
+    c.width = cam->width;
+    c.height = cam->height;
+    Dev<float2> dsp;
+    Dev<cr_ray> dr;
+    CR_CUDA(cudaMalloc(&dsp.p, n * sizeof(float2)));
+    CR_CUDA(cudaMalloc(&dr.p, n * sizeof(cr_ray)));
+    CR_CUDA(cudaMemcpy(dsp.p, sensor_pos, n * sizeof(float2), cudaMemcpyHostToDevice));
+    kCameraRays<<<(unsigned)((n + 127) / 128), 128>>>(c, dsp.p, n, dr.p);
+    CR_LAUNCH_CHECK();
+    CR_CUDA(cudaMemcpy(rays, dr.p, n * sizeof(cr_ray), cudaMemcpyDeviceToHost));
+    return CR_OK;
+}
+
+static int bsdfBatch(const cr_material* mat, const float* n, const float* wo, const float* wi, const float* u,
+                     uint64_t count, float* wiOut, float* f, float* pdf) {
+    if (!mat || (count && (!n || !wo || !f || !pdf || (!wi && !u) || (u && !wiOut))))
+        return fail(CR_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (mat->type > CR_MATERIAL_PHONG) return fail(CR_ERR_INVALID_ARGUMENT, "material type %u", mat->type);
+    if (count == 0) return CR_OK;
+    const MaterialGpu m = deriveMaterialPublic(*mat);
+    Dev<float3> dn, dwo, dwi, dwio, df;
+    Dev<float2> du;
+    Dev<float> dp;
+    const size_t v3 = count * sizeof(float3);
+    CR_CUDA(cudaMalloc(&dn.p, v3));
+    CR_CUDA(cudaMalloc(&dwo.p, v3));
+    CR_CUDA(cudaMalloc(&df.p, v3));
+    CR_CUDA(cudaMalloc(&dp.p, count * sizeof(float)));
+    CR_CUDA(cudaMemcpy(dn.p, n, v3, cudaMemcpyHostToDevice));
+    CR_CUDA(cudaMemcpy(dwo.p, wo, v3, cudaMemcpyHostToDevice));
+    if (u) {
+        CR_CUDA(cudaMalloc(&du.p, count * sizeof(float2)));
+        CR_CUDA(cudaMalloc(&dwio.p, v3));
+        CR_CUDA(cudaMemcpy(du.p, u, count * sizeof(float2), cudaMemcpyHostToDevice));
+    } else {
+        CR_CUDA(cudaMalloc(&dwi.p, v3));
+        CR_CUDA(cudaMemcpy(dwi.p, wi, v3, cudaMemcpyHostToDevice));
+    }
+    kBsdf<<<(unsigned)((count + 127) / 128), 128>>>(m, dn.p, dwo.p, dwi.p, du.p, count, dwio.p, df.p, dp.p);
+    CR_LAUNCH_CHECK();
+    CR_CUDA(cudaMemcpy(f, df.p, v3, cudaMemcpyDeviceToHost));
+    CR_CUDA(cudaMemcpy(pdf, dp.p, count * sizeof(float), cudaMemcpyDeviceToHost));
+    if (u) CR_CUDA(cudaMemcpy(wiOut, dwio.p, v3, cudaMemcpyDeviceToHost));
+    return CR_OK;
+}
+
+extern "C" int cr_bsdf_evaluate(const cr_material* mat, const float* n, const float* wo, const float* wi,
+                                uint64_t count, float* f, float* pdf) {
+    clearError();
+    return bsdfBatch(mat, n, wo, wi, nullptr, count, nullptr, f, pdf);
+}
+
+extern "C" int cr_bsdf_sample(const cr_material* mat, const float* n, const float* wo, const float* u,
+                              uint64_t count, float* wi, float* f, float* pdf) {
+    clearError();
+    return bsdfBatch(mat, n, wo, nullptr, u, count, wi, f, pdf);
+}

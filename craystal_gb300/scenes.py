@@ -1,0 +1,160 @@
+"""Seeded synthetic workloads (the reference ships no scene assets).
+
+cornell_box  -- procedural Cornell box: 5 wall quads in [-1,1]^3 open towards
+                +z, two boxes (half heights 0.6 and 0.3) rotated about y by
+                U(0, 45 deg), a 0.25 x 0.25 ceiling light of emission 15;
+                34 + 2 triangles; grey albedos U(0.2, 0.8) per object,
+                Lambertian walls, Phong boxes (exponent 32); fov 40 deg.
+random_triangles -- N triangles, centroids U[0,1]^3, vertices c + e_k with
+                e_k ~ N(0, 0.01^2) per component.
+random_rays  -- origins on the sphere of radius 2 about the origin,
+                directions towards U[0,1]^3, tmin 1e-4, tmax +inf.
+"""
+import math
+
+import numpy as np
+
+from ._lib import RAY_DTYPE
+from .api import Camera, MaterialData, MaterialType, MeshData, SceneData, Sensor
+
+
+def _quad(p0, p1, p2, p3, normal):
+    pos = np.array([p0, p1, p2, p3], np.float32)
+    idx = np.array([0, 1, 2, 0, 2, 3], np.uint32)
+    nrm = np.repeat(np.asarray(normal, np.float32)[None], 4, 0)
+    return pos, nrm, idx
+
+
+def _oriented(pos, idx, inward_point):
+    """Flips triangles whose geometric normal points away from inward_point,
+    and returns per-vertex face normals (flat shading)."""
+    idx = idx.copy().reshape(-1, 3)
+    out_pos, out_nrm, out_idx = [], [], []
+    for t in idx:
+        v = pos[t]
+        n = np.cross(v[1] - v[0], v[2] - v[0])
+        c = v.mean(0)
+        if np.dot(n, np.asarray(inward_point) - c) < 0:
+            t = t[[0, 2, 1]]
+            v = pos[t]
+            n = -n
+        n = n / np.linalg.norm(n)
+        base = len(out_pos) * 3
+        out_pos.append(v)
+        out_nrm.append(np.repeat(n[None], 3, 0))
+        out_idx.append(np.arange(base, base + 3))
+    return (np.concatenate(out_pos).astype(np.float32), np.concatenate(out_nrm).astype(np.float32),
+            np.concatenate(out_idx).astype(np.uint32))
+
+
+def _box(center, half, angle):
+    cx, cy, cz = center
+    hx, hy, hz = half
+    corners = []
+    for sx in (-1, 1):
+        for sy in (-1, 1):
+            for sz in (-1, 1):
+                x, z = sx * hx, sz * hz
+                ca, sa = math.cos(angle), math.sin(angle)
+                corners.append((cx + ca * x + sa * z, cy + sy * hy, cz - sa * x + ca * z))
+    c = np.array(corners, np.float64)
+    faces = [(0, 1, 3, 2), (4, 6, 7, 5), (0, 4, 5, 1), (2, 3, 7, 6), (0, 2, 6, 4), (1, 5, 7, 3)]
+    tris = []
+    for a, b, cc, d in faces:
+        tris += [(a, b, cc), (a, cc, d)]
+    idx = np.array(tris, np.uint32).reshape(-1)
+    # orient outward: flip so that normals point away from the center
+    idx3 = idx.reshape(-1, 3).copy()
+    pos, nrm, out = [], [], []
+    for t in idx3:
+        v = c[t]
+        n = np.cross(v[1] - v[0], v[2] - v[0])
+        if np.dot(n, v.mean(0) - np.array(center)) < 0:
+            t = t[[0, 2, 1]]
+            v = c[t]
+            n = -n
+        n /= np.linalg.norm(n)
+        base = len(pos) * 3
+        pos.append(v)
+        nrm.append(np.repeat(n[None], 3, 0))
+        out.append(np.arange(base, base + 3))
+    return (np.concatenate(pos).astype(np.float32), np.concatenate(nrm).astype(np.float32),
+            np.concatenate(out).astype(np.uint32))
+
+
+def cornell_box(seed: int = 0, width: int = 256, height: int = 256):
+    """Returns (SceneData, Camera) of the procedural Cornell box."""
+    rng = np.random.default_rng(seed)
+    meshes, mats = [], []
+    walls = [
+        ((-1, -1, -1), (1, -1, -1), (1, -1, 1), (-1, -1, 1)),   # floor
+        ((-1, 1, -1), (-1, 1, 1), (1, 1, 1), (1, 1, -1)),       # ceiling
+        ((-1, -1, -1), (-1, 1, -1), (1, 1, -1), (1, -1, -1)),   # back
+        ((-1, -1, -1), (-1, -1, 1), (-1, 1, 1), (-1, 1, -1)),   # left
+        ((1, -1, -1), (1, 1, -1), (1, 1, 1), (1, -1, 1)),       # right
+    ]
+    for quad in walls:
+        pos = np.array(quad, np.float32)
+        p, n, i = _oriented(pos, np.array([0, 1, 2, 0, 2, 3], np.uint32), (0.0, 0.0, 0.0))
+        a = float(rng.uniform(0.2, 0.8))
+        mats.append(MaterialData(diffuseRefl=(a, a, a), type=MaterialType.FullDiffuse))
+        meshes.append(MeshData(position=p, normal=n, index=i, materialID=len(mats) - 1))
+    for center, half in (((-0.35, -1.0 + 0.6 + 1e-4, -0.3), (0.3, 0.6, 0.3)),
+                         ((0.4, -1.0 + 0.3 + 1e-4, 0.3), (0.3, 0.3, 0.3))):
+        ang = float(rng.uniform(0.0, math.pi / 4))
+        p, n, i = _box(center, half, ang)
+        a = float(rng.uniform(0.2, 0.8))
+        mats.append(MaterialData(diffuseRefl=(a, a, a), specularRefl=(0.1, 0.1, 0.1), shininess=32.0,
+                                 type=MaterialType.Phong))
+        meshes.append(MeshData(position=p, normal=n, index=i, materialID=len(mats) - 1))
+    y = 1.0 - 1e-3
+    lp = np.array([(-0.125, y, -0.125), (0.125, y, -0.125), (0.125, y, 0.125), (-0.125, y, 0.125)], np.float32)
+    p, n, i = _oriented(lp, np.array([0, 1, 2, 0, 2, 3], np.uint32), (0.0, -1.0, 0.0))
+    mats.append(MaterialData(emission=(15.0, 15.0, 15.0), type=MaterialType.FullDiffuse))
+    meshes.append(MeshData(position=p, normal=n, index=i, materialID=len(mats) - 1))
+    for m in mats:
+        m.finalize()
+    n_tris = sum(len(m.index) // 3 for m in meshes)
+    data = SceneData(meshes=meshes, materials=mats, emissiveIndex=[n_tris - 2, n_tris - 1])
+    cam = Camera()
+    cam.setWorldPosition((0.0, 0.0, 3.9))
+    cam.setTarget((0.0, 0.0, 0.0))
+    cam.setUp((0.0, 1.0, 0.0))
+    cam.setFovY(40.0)
+    cam.setSensor(Sensor((width, height)))
+    return data, cam
+
+
+def random_triangles(n: int, seed: int = 0):
+    """Positions (3n x 3 float32) and indices (3n uint32) of n random triangles."""
+    rng = np.random.default_rng(seed)
+    c = rng.random((n, 1, 3), dtype=np.float64)
+    e = rng.normal(0.0, 0.01, size=(n, 3, 3))
+    pos = (c + e).astype(np.float32).reshape(-1, 3)
+    idx = np.arange(3 * n, dtype=np.uint32)
+    return pos, idx
+
+
+def random_triangle_scene(n: int, seed: int = 0) -> SceneData:
+    pos, idx = random_triangles(n, seed)
+    mat = MaterialData(diffuseRefl=(0.5, 0.5, 0.5), type=MaterialType.FullDiffuse)
+    mat.finalize()
+    return SceneData(meshes=[MeshData(position=pos, index=idx, materialID=0)], materials=[mat], emissiveIndex=[])
+
+
+def random_rays(n: int, seed: int = 1, tmin: float = 1e-4) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    rays = np.empty(n, RAY_DTYPE)
+    chunk = 1 << 22
+    for s in range(0, n, chunk):
+        m = min(chunk, n - s)
+        o = rng.normal(size=(m, 3))
+        o *= 2.0 / np.linalg.norm(o, axis=1, keepdims=True)
+        p = rng.random((m, 3))
+        d = p - o
+        d /= np.linalg.norm(d, axis=1, keepdims=True)
+        rays["o"][s:s + m] = o.astype(np.float32)
+        rays["d"][s:s + m] = d.astype(np.float32)
+    rays["tmin"] = np.float32(tmin)
+    rays["tmax"] = np.float32(np.inf)
+    return rays

@@ -1,0 +1,237 @@
+/*
+ * craystal_c.h -- C ABI of craystal_gb300, a GB300-native (sm_103a)
+ * implementation of the CRaystal path-tracing hot path.
+ *
+ * The entry points replace the C++ classes of the reference library
+ * (Hyiker/CRaystal, Source/CRaystal) one for one; each declaration cites
+ * the reference interface it stands for.  Conventions:
+ *   - every function returns CR_OK (0) or an error code; cr_last_error()
+ *     returns a message for the calling thread's last failure (no exceptions
+ *     cross the ABI, where the reference throws RuntimeError,
+ *     Core/Error.h:113-124 and Utils/CudaUtils.h:3-12);
+ *   - host arrays passed to cr_scene_create are copied; the caller keeps them;
+ *   - "_device" entry points take device pointers and a cudaStream_t (passed
+ *     as void*, NULL = legacy default stream) and return without waiting;
+ *     the others take host pointers and return when the results are in them;
+ *   - a scene handle is not thread-safe; distinct handles are independent.
+ */
+#ifndef CRAYSTAL_C_H
+#define CRAYSTAL_C_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CR_OK 0
+#define CR_ERR_INVALID_ARGUMENT 1
+#define CR_ERR_CUDA 2
+#define CR_ERR_OUT_OF_MEMORY 3
+#define CR_ERR_DEVICE 4       /* a kernel reported an error (stack overflow, timeout) */
+#define CR_ERR_UNSUPPORTED 5
+
+#define CR_MISS 0xFFFFFFFFu
+
+/* Material types, Core/Material.h:12-16. */
+#define CR_MATERIAL_DIFFUSE 0u
+#define CR_MATERIAL_PRINCIPLED 1u
+#define CR_MATERIAL_PHONG 2u
+/* Material flags, Core/Material.h:26-30 (set by MaterialData::finalize). */
+#define CR_MATERIAL_EMISSIVE 1u
+#define CR_MATERIAL_DIFFUSE_ONLY 2u
+
+/* Ray, Math/Ray.h:8-13: origin, tMin, direction, tMax (32 bytes). */
+typedef struct {
+    float o[3];
+    float tmin;
+    float d[3];
+    float tmax;
+} cr_ray;
+
+/* Closest hit: primitive index (CR_MISS when nothing is hit), t and the
+ * barycentrics (u, v) of Scene/Triangle.cu:68-69; RayHit, Core/Hit.h:26-30. */
+typedef struct {
+    uint32_t prim;
+    float t;
+    float u;
+    float v;
+} cr_hit;
+
+/* MaterialData, Core/Material.h:34-66, the fields the path reads. */
+typedef struct {
+    float diffuse[3];   /* Kd */
+    float specular[3];  /* Ks */
+    float emission[3];
+    float shininess;    /* Phong exponent; Principled roughness = sqrt(2/(s+1)) */
+    uint32_t type;      /* CR_MATERIAL_* */
+    uint32_t flags;     /* CR_MATERIAL_EMISSIVE | CR_MATERIAL_DIFFUSE_ONLY; 0 = derive */
+} cr_material;
+
+/* MeshDesc, Scene/Triangle.h:27-32 (indices already rebased to the global
+ * vertex array, as TriangleMeshManager does at Scene/Triangle.cu:98-120). */
+typedef struct {
+    uint32_t index_offset;
+    uint32_t index_count;
+    uint32_t vertex_offset;
+    uint32_t material_id;
+} cr_mesh_desc;
+
+/* Camera + sensor size: Camera::setWorldPosition/setTarget/setUp/setFovY
+ * (Core/Camera.h:24-31) and Sensor(UInt2 size) (Core/Sensor.h:35). */
+typedef struct {
+    float pos[3];
+    float target[3];
+    float up[3];
+    float fov_y;        /* degrees */
+    uint32_t width;
+    uint32_t height;
+} cr_camera;
+
+/* PathTraceIntegrator::Configs / DeviceView, Core/Integrator.h:14-23.
+ * The reference never copies Configs into the device view, so its kernels
+ * always run with max_depth 10 and rr_threshold 0.05; pass those for the
+ * reference's effective behaviour. */
+typedef struct {
+    uint32_t max_depth;
+    float rr_threshold;
+    uint32_t use_mis;
+    uint32_t flags;     /* reserved, 0 */
+} cr_integrator_config;
+
+/* Binary BVH node in the reference's layout (Core/BVH.h:17-30): nodes in
+ * post-order with the root last; leaf: (a, b) = (first leaf slot, count),
+ * interior: (a, b) = (left child, right child). */
+typedef struct {
+    float bmin[3];
+    float bmax[3];
+    uint32_t is_leaf;
+    uint32_t a;
+    uint32_t b;
+} cr_bvh_node;
+
+typedef struct {
+    uint32_t node_count;
+    uint32_t leaf_count;
+    uint32_t max_depth;        /* deepest interior node */
+    uint32_t max_leaf_size;
+    uint32_t max_leaf_depth;
+    uint32_t levels;           /* breadth-first build levels executed */
+    float root_min[3];
+    float root_max[3];
+    double build_ms;           /* device time of the GPU build */
+    uint64_t device_bytes;     /* BVH + triangle blocks resident in HBM */
+} cr_bvh_stats;
+
+typedef struct cr_scene cr_scene;
+
+/* Thread-local message of the last failed call ("" after success). */
+const char* cr_last_error(void);
+
+/* Library version string. */
+const char* cr_version(void);
+
+/* Selects the CUDA device used by subsequent calls of this thread. */
+int cr_set_device(int device);
+
+/* Scene(SceneData&&), Scene/Scene.cu:61-78: uploads the global vertex and
+ * index arrays (TriangleMeshManager, Scene/Triangle.cu:98-165), the
+ * materials and emitter list (MaterialManager, Core/Material.cu:15-31) and
+ * builds the BVH on the GPU (replacing the host build of Core/BVH.cu:88-116;
+ * same binned-SAH decisions, see cr_scene_bvh_export).  nrm and uv may be
+ * NULL (zeros).  Material flags of 0 are derived as MaterialData::finalize
+ * does (Core/Material.h:57-65). */
+int cr_scene_create(const float* pos, const float* nrm, const float* uv,
+                    uint64_t n_vertices, const uint32_t* idx, uint64_t n_tris,
+                    const cr_mesh_desc* meshes, uint32_t n_meshes,
+                    const cr_material* mats, uint32_t n_mats,
+                    const uint32_t* emissive, uint32_t n_emissive,
+                    cr_scene** out);
+
+int cr_scene_destroy(cr_scene* scene);
+
+/* BVH statistics, the figures BVH::build logs (Core/BVH.cu:111-115). */
+int cr_scene_bvh_stats(const cr_scene* scene, cr_bvh_stats* out);
+
+/* Copies the BVH out in the reference's node layout: nodes (node_count
+ * entries, post-order, root last, as BVH::buildRecursive numbers them,
+ * Core/BVH.cu:150-212) and prim_map (n_tris entries: leaf slot -> primitive,
+ * bvhToMeshPrimitiveIndex of Core/BVH.cu:322-338).  Either may be NULL. */
+int cr_scene_bvh_export(const cr_scene* scene, cr_bvh_node* nodes,
+                        uint32_t* prim_map);
+
+/* Scene::setCamera + Camera::calculateCameraData + Sensor(size)
+ * (Scene/Scene.h:56-58, Core/Camera.cu:35-39, Core/Sensor.cu:46-60).  A
+ * sensor of a new size gets a new film, cleared to zero. */
+int cr_scene_set_camera(cr_scene* scene, const cr_camera* cam);
+
+/* Zeroes the film (the reference never clears its film, Core/Sensor.cu:55-59). */
+int cr_film_clear(cr_scene* scene);
+
+/* Sensor::readbackDeviceData (Core/Sensor.cu:82-86): rgb = width*height*3
+ * floats (sum of weighted radiance), weight = width*height floats.  Either
+ * may be NULL.  Waits for all work on the scene's film. */
+int cr_film_read(cr_scene* scene, float* rgb, float* weight);
+
+/* Sensor::createImage (Core/Sensor.cu:93-112): rgb = sum / weight per pixel,
+ * resolved on the GPU; width*height*3 floats. */
+int cr_film_resolve(cr_scene* scene, float* rgb);
+
+/* PathTraceIntegrator::dispatch(scene, spp), Core/Integrator.cu:233-262:
+ * renders spp samples per pixel with sample indices first_sample ..
+ * first_sample+spp-1 into the film, on the given stream, without waiting.
+ * rays_out (host, may be NULL) receives the number of closest-hit and
+ * occlusion traversals after the next cr_film_read / stream sync. */
+int cr_render(cr_scene* scene, const cr_integrator_config* cfg, uint32_t spp,
+              uint32_t first_sample, void* stream);
+
+/* Number of traversals (camera/continuation, shadow, MIS-BSDF rays) the
+ * renders since the last cr_film_clear performed; synchronises the film. */
+int cr_render_ray_count(cr_scene* scene, uint64_t* rays);
+
+/* SceneView::intersect (Scene/Scene.cu:5-14) on a batch of rays: closest
+ * hit with the reference's traversal order (Core/BVH.cu:13-84) and
+ * intersection arithmetic (Scene/Triangle.cu:40-75), so that prim, t, u and
+ * v equal the reference's bit for bit.  Host arrays; copies in and out are
+ * pipelined with the traversal. */
+int cr_trace_closest(cr_scene* scene, const cr_ray* rays, uint64_t n,
+                     cr_hit* hits);
+int cr_trace_closest_device(cr_scene* scene, const cr_ray* rays, uint64_t n,
+                            cr_hit* hits, void* stream);
+
+/* SceneView::intersectOcclusion (Scene/Scene.cu:16-29): 1 when any
+ * triangle is hit with t in [tmin, tmax].  The reference finds this with a
+ * full closest-hit traversal; an any-hit traversal with early exit gives the
+ * same answer. */
+int cr_trace_occluded(cr_scene* scene, const cr_ray* rays, uint64_t n,
+                      uint8_t* occluded);
+int cr_trace_occluded_device(cr_scene* scene, const cr_ray* rays, uint64_t n,
+                             uint8_t* occluded, void* stream);
+
+/* CameraProxy::generateRay (Core/CameraProxy.h:25-40) on the GPU for a
+ * batch of film positions (sensor_pos: n pairs x, y in pixels). */
+int cr_camera_generate_rays(const cr_camera* cam, const float* sensor_pos,
+                            uint64_t n, cr_ray* rays);
+
+/* BSDF::evaluate and BSDF::evaluatePdf (Material/BSDF.cu:36-70) on the GPU
+ * for a batch: the shading frame is Frame(n) (Core/Frame.cu:6-23), wo / wi
+ * world directions; f = n*3 floats (BSDF value times |cos|), pdf = n. */
+int cr_bsdf_evaluate(const cr_material* mat, const float* n, const float* wo,
+                     const float* wi, uint64_t count, float* f, float* pdf);
+
+/* BSDF::sampleEvaluate (Material/BSDF.cu:87-103) with the two uniform
+ * numbers given (u = count*2 floats) instead of drawn: wi = count*3,
+ * f = count*3, pdf = count. */
+int cr_bsdf_sample(const cr_material* mat, const float* n, const float* wo,
+                   const float* u, uint64_t count, float* wi, float* f,
+                   float* pdf);
+
+/* Number of kernel launches this library issued since the process started
+ * (all entry points); for launch accounting in benchmarks. */
+uint64_t cr_kernel_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,156 @@
+"""GPU parity of the BVH build and the ray queries against the CPU oracle.
+
+Contract: the GPU builder produces the reference's tree (same topology and
+boxes, bit for bit), and closest hits (prim, t, u, v) equal the
+reference's on identical FP32 rays bit for bit.  The one allowed
+difference is which of two triangles hit at exactly the same t in the same
+leaf is reported; the oracle flags those rays ("ties") and they are counted
+and bounded, not ignored silently."""
+import numpy as np
+import pytest
+
+import oracle
+from craystal_gb300 import scenes
+from craystal_gb300.api import Scene, flatten_scene
+
+pytestmark = pytest.mark.gpu
+
+MISS = 0xFFFFFFFF
+
+
+def both(data):
+    return Scene(data), oracle.OracleScene(flatten_scene(data))
+
+
+def assert_same_tree(gpu: Scene, orc):
+    gn, gmap = gpu.bvh_export()
+    on, omap = orc.bvh_export()
+    assert len(gn) == len(on)
+    assert np.array_equal(gn["is_leaf"], on["is_leaf"])
+    assert np.array_equal(gn["bmin"].view(np.uint32), on["bmin"].view(np.uint32))
+    assert np.array_equal(gn["bmax"].view(np.uint32), on["bmax"].view(np.uint32))
+    assert np.array_equal(gn["a"], on["a"]) and np.array_equal(gn["b"], on["b"])
+    for nd in gn[gn["is_leaf"] == 1]:
+        s, c = nd["a"], nd["b"]
+        assert sorted(gmap[s:s + c]) == sorted(omap[s:s + c])
+    gs, os_ = gpu.bvh_stats(), orc.bvh_stats()
+    for k in ("node_count", "leaf_count", "max_depth", "max_leaf_size"):
+        assert gs[k] == os_[k], k
+
+
+def assert_same_hits(gh, oh, ties, max_tie_frac=1e-4):
+    ok = (gh["prim"] == oh["prim"])
+    hit = oh["prim"] != MISS
+    ok &= ~hit | (gh["t"].view(np.uint32) == oh["t"].view(np.uint32))
+    ok &= ~hit | (gh["u"].view(np.uint32) == oh["u"].view(np.uint32))
+    ok &= ~hit | (gh["v"].view(np.uint32) == oh["v"].view(np.uint32))
+    bad = ~ok & ~ties
+    assert not bad.any(), f"{bad.sum()} rays differ, first {np.flatnonzero(bad)[:5]}"
+    assert ties.mean() <= max_tie_frac
+    # tie rays still agree on t
+    assert np.array_equal(gh["t"][ties].view(np.uint32), oh["t"][ties].view(np.uint32))
+
+
+@pytest.mark.parametrize("n", [1, 4, 5, 37, 2048, 2049, 30000, 200000])
+def test_bvh_matches_reference_build(gpu_lib, n):
+    g, o = both(scenes.random_triangle_scene(n, seed=n))
+    assert_same_tree(g, o)
+
+
+def test_bvh_cornell_flat_boxes(gpu_lib):
+    g, o = both(scenes.cornell_box()[0])
+    assert_same_tree(g, o)
+
+
+def test_bvh_coincident_centroids(gpu_lib):
+    """Every triangle with the same centroid: the split fails (one side
+    empty) and the node becomes a leaf holding everything."""
+    pos = np.tile(np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32), (50, 1))
+    from craystal_gb300.api import MaterialData, MeshData, SceneData
+    data = SceneData(meshes=[MeshData(position=pos, index=np.arange(150, dtype=np.uint32))],
+                     materials=[MaterialData()])
+    g, o = both(data)
+    assert_same_tree(g, o)
+    assert g.bvh_stats()["leaf_count"] == 1
+
+
+def test_closest_hits_bit_exact(gpu_lib):
+    g, o = both(scenes.random_triangle_scene(200000, seed=21))
+    rays = scenes.random_rays(1 << 20, seed=22)
+    gh = g.trace_closest(rays)
+    oh, ties = o.trace_closest(rays)
+    assert (oh["prim"] != MISS).mean() > 0.5
+    assert_same_hits(gh, oh, ties)
+
+
+def test_device_and_host_entry_points_agree(gpu_lib):
+    import torch
+    g, _ = both(scenes.random_triangle_scene(20000, seed=23))
+    rays = scenes.random_rays(100000, seed=24)
+    host = g.trace_closest(rays)
+    dr = torch.from_numpy(rays.view(np.uint8)).cuda()
+    dh = torch.empty(len(rays) * 16, dtype=torch.uint8, device="cuda")
+    s = torch.cuda.current_stream()
+    g.trace_closest_device(dr.data_ptr(), len(rays), dh.data_ptr(), s.cuda_stream)
+    s.synchronize()
+    dev = dh.cpu().numpy().view(host.dtype)
+    assert np.array_equal(dev.view(np.uint32), host.view(np.uint32))
+
+
+def test_occlusion_exact(gpu_lib):
+    g, o = both(scenes.random_triangle_scene(50000, seed=25))
+    rays = scenes.random_rays(300000, seed=26)
+    rays["tmax"] = np.random.default_rng(1).uniform(0.2, 3.5, len(rays)).astype(np.float32)
+    assert np.array_equal(g.trace_occluded(rays), o.trace_occluded(rays))
+
+
+def test_edge_cases(gpu_lib):
+    # empty scene: everything misses
+    from craystal_gb300.api import MaterialData, SceneData
+    g = Scene(SceneData(materials=[MaterialData()]))
+    h = g.trace_closest(scenes.random_rays(1000))
+    assert (h["prim"] == MISS).all() and np.isinf(h["t"]).all()
+    assert g.trace_closest(scenes.random_rays(0)).shape == (0,)
+    # single triangle (the root is a leaf), rays aimed at it
+    pos = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)
+    from craystal_gb300.api import MeshData
+    data = SceneData(meshes=[MeshData(position=pos, index=np.arange(3, dtype=np.uint32))], materials=[MaterialData()])
+    g, o = both(data)
+    rays = scenes.random_rays(5000, seed=27)
+    aim = np.random.default_rng(2).random((5000, 3)).astype(np.float32) * np.float32([0.7, 0.7, 0])
+    d = aim - rays["o"]
+    rays["d"] = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+    gh = g.trace_closest(rays)
+    oh, ties = o.trace_closest(rays)
+    assert (oh["prim"] == 0).mean() > 0.5
+    assert_same_hits(gh, oh, ties, 0.0)
+
+
+def test_cornell_axis_parallel_rays(gpu_lib):
+    """Flat boxes (degenerate slabs), axis-parallel directions (zero
+    components, infinite inverse direction), ray windows [tmin, tmax]."""
+    g, o = both(scenes.cornell_box()[0])
+    rng = np.random.default_rng(3)
+    rays = scenes.random_rays(200000, seed=28)
+    rays["o"] *= np.float32(0.45)
+    d = rays["d"].copy()
+    d[rng.random((len(d), 3)) < 0.3] = 0.0
+    d[(d == 0).all(1), 1] = -1.0
+    rays["d"] = d
+    rays["tmin"] = rng.choice(np.float32([0, 1e-4, 0.5]), len(rays))
+    rays["tmax"] = rng.choice(np.float32([np.inf, 1.0, 2.0]), len(rays))
+    gh = g.trace_closest(rays)
+    oh, ties = o.trace_closest(rays)
+    assert_same_hits(gh, oh, ties, 1e-2)
+    assert np.array_equal(g.trace_occluded(rays), o.trace_occluded(rays))
+
+
+def test_full_size_ray_cast(gpu_lib):
+    """The ray-cast benchmark at its full size: 1M triangles, 16M rays, every
+    hit compared with the oracle."""
+    g, o = both(scenes.random_triangle_scene(1 << 20, seed=0))
+    assert_same_tree(g, o)
+    rays = scenes.random_rays(1 << 24, seed=1)
+    gh = g.trace_closest(rays)
+    oh, ties = o.trace_closest(rays)
+    assert_same_hits(gh, oh, ties)
