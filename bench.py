@@ -38,7 +38,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 N_TRIS = 1 << 20
-N_RAYS = 1 << 24
+N_RAYS = 1 << 24  # --rays / --tris shrink the workload for profiler captures
 TRI_SEED, RAY_SEED = 0, 1
 METRIC = "Mrays/s (closest-hit ray cast, 1M triangles, 16M rays)"
 WORKLOAD = "raycast_1M_tris_16M_rays"
@@ -316,7 +316,10 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU baseline leg")
     ap.add_argument("--skip-extra", action="store_true", help="omit the path-tracer figures")
+    ap.add_argument("--rays", type=int, default=N_RAYS, help="rays per step (profiling a smaller case)")
+    ap.add_argument("--tris", type=int, default=N_TRIS, help="triangles (profiling a smaller case)")
     args = ap.parse_args()
+    globals()["N_RAYS"], globals()["N_TRIS"] = args.rays, args.tris
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

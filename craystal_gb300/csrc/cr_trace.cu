@@ -10,8 +10,13 @@ namespace {
 
 constexpr int kTraceThreads = 128;
 
-__global__ void __launch_bounds__(kTraceThreads) kTraceClosest(const SceneView sc, const cr_ray* __restrict__ rays,
-                                                               uint64_t n, cr_hit* __restrict__ hits) {
+// One thread per ray.  (A persistent variant that refills the lanes of a
+// warp from a per-warp ray range measured slower on GB300 for this
+// incoherent workload: the lanes' rounds synchronise on the slowest lane.)
+template <bool kAnyHit>
+__global__ void __launch_bounds__(kTraceThreads) kTrace(const SceneView sc, const cr_ray* __restrict__ rays,
+                                                        uint64_t n, cr_hit* __restrict__ hits,
+                                                        uint8_t* __restrict__ occ) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float4* rp = reinterpret_cast<const float4*>(rays + i);
@@ -19,54 +24,39 @@ __global__ void __launch_bounds__(kTraceThreads) kTraceClosest(const SceneView s
     const TRay r = makeTRay(mk3(a.x, a.y, a.z), a.w, mk3(b.x, b.y, b.z), b.w);
     THit h;
     h.t = INFINITY;
-    h.u = 0.0f;
-    h.v = 0.0f;
+    h.u = h.v = 0.0f;
     h.prim = CR_MISS;
-    bool hit = traverse<false>(sc, r, h);
-    float4 o;
-    if (hit) o = make_float4(__uint_as_float(h.prim), h.t, h.u, h.v);
-    else o = make_float4(__uint_as_float(CR_MISS), INFINITY, 0.0f, 0.0f);
-    reinterpret_cast<float4*>(hits)[i] = o;
+    const bool hit = traverse<kAnyHit>(sc, r, h);
+    if (kAnyHit) {
+        occ[i] = hit ? 1 : 0;
+    } else {
+        reinterpret_cast<float4*>(hits)[i] = hit ? make_float4(__uint_as_float(h.prim), h.t, h.u, h.v)
+                                                 : make_float4(__uint_as_float(CR_MISS), INFINITY, 0.0f, 0.0f);
+    }
 }
 
-__global__ void __launch_bounds__(kTraceThreads) kTraceOccluded(const SceneView sc, const cr_ray* __restrict__ rays,
-                                                                uint64_t n, uint8_t* __restrict__ occ) {
-    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float4* rp = reinterpret_cast<const float4*>(rays + i);
-    const float4 a = __ldg(rp), b = __ldg(rp + 1);
-    const TRay r = makeTRay(mk3(a.x, a.y, a.z), a.w, mk3(b.x, b.y, b.z), b.w);
-    THit h;
-    h.t = INFINITY;
-    occ[i] = traverse<true>(sc, r, h) ? 1 : 0;
+constexpr uint64_t kMaxRaysPerLaunch = 0x7fffffffull * kTraceThreads;
+
+template <bool kAnyHit>
+int launchTrace(cr_scene* s, const cr_ray* rays, uint64_t n, cr_hit* hits, uint8_t* occ, cudaStream_t st) {
+    const SceneView v = s->view();
+    for (uint64_t off = 0; off < n; off += kMaxRaysPerLaunch) {
+        const uint64_t m = std::min(n - off, kMaxRaysPerLaunch);
+        kTrace<kAnyHit><<<(unsigned)((m + kTraceThreads - 1) / kTraceThreads), kTraceThreads, 0, st>>>(
+            v, rays + off, m, hits ? hits + off : nullptr, occ ? occ + off : nullptr);
+        CR_LAUNCH_CHECK();
+    }
+    return CR_OK;
 }
-
-inline unsigned blocksFor(uint64_t n, unsigned t) { return (unsigned)((n + t - 1) / t); }
-
-constexpr uint64_t kMaxGrid = 0x7fffffffull;
 
 }  // namespace
 
 int traceClosestDevice(cr_scene* s, const cr_ray* rays, uint64_t n, cr_hit* hits, cudaStream_t st) {
-    if (n == 0) return CR_OK;
-    const SceneView v = s->view();
-    for (uint64_t off = 0; off < n; off += kMaxGrid * kTraceThreads) {
-        uint64_t m = std::min<uint64_t>(n - off, kMaxGrid * kTraceThreads);
-        kTraceClosest<<<blocksFor(m, kTraceThreads), kTraceThreads, 0, st>>>(v, rays + off, m, hits + off);
-        CR_LAUNCH_CHECK();
-    }
-    return CR_OK;
+    return launchTrace<false>(s, rays, n, hits, nullptr, st);
 }
 
 int traceOccludedDevice(cr_scene* s, const cr_ray* rays, uint64_t n, uint8_t* occ, cudaStream_t st) {
-    if (n == 0) return CR_OK;
-    const SceneView v = s->view();
-    for (uint64_t off = 0; off < n; off += kMaxGrid * kTraceThreads) {
-        uint64_t m = std::min<uint64_t>(n - off, kMaxGrid * kTraceThreads);
-        kTraceOccluded<<<blocksFor(m, kTraceThreads), kTraceThreads, 0, st>>>(v, rays + off, m, occ + off);
-        CR_LAUNCH_CHECK();
-    }
-    return CR_OK;
+    return launchTrace<true>(s, rays, n, nullptr, occ, st);
 }
 
 }  // namespace cr

@@ -9,6 +9,13 @@
 // 1/d the reference recomputes per box is the same float), and each leaf
 // slot holds a pre-gathered 48-byte triangle block (v0, e1, e2) whose
 // edges are the differences the reference forms per test.
+//
+// Visiting order.  The reference pushes the far child, then the near child,
+// and pops the near child at once; here the near child becomes the current
+// node directly and only the far child is pushed.  That is the same order
+// with the same culling decisions: nothing changes closestT between the push
+// and the pop of the near child, so its pop-time test "tEntry > closestT" is
+// the push-time test "tEntry < closestT" negated.
 #pragma once
 
 #include "cr_internal.cuh"
@@ -40,38 +47,53 @@ struct THit {
     uint32_t prim;
 };
 
-// One slab of Math/AABB.cu:10-29.  Returns false for the degenerate-slab
-// early out; the per-axis "tMin > tMax" test of the reference is folded into
-// the final test, which is equivalent because tMin only grows and tMax only
-// shrinks afterwards.
-__device__ __forceinline__ bool slab(float mn, float mx, float o, float d, float inv, bool degenerate,
-                                     float& tMin, float& tMax) {
-    if (degenerate) {
-        if (fabsf(d) < kFltEps) return fabsf(o - mn) <= kFltEps;
-        float t = (mn - o) / d;
-        tMin = smax(tMin, t);
-        tMax = smin(tMax, t);
-        return true;
-    }
-    float t0 = (mn - o) * inv;
-    float t1 = (mx - o) * inv;
-    float tn = (inv < 0.0f) ? t1 : t0;
-    float tf = (inv < 0.0f) ? t0 : t1;
-    tMin = smax(tMin, tn);
-    tMax = smin(tMax, tf);
+// One slab of Math/AABB.cu:10-29.
+//
+// fmaxf / fminf stand for the reference's std::max / std::min: they differ
+// only for a NaN second operand, where both keep the first (a NaN slab
+// distance arises as 0 * inf when the origin lies on the slab plane and the
+// direction component is zero; tMin / tMax themselves never become NaN), and
+// in the sign of a zero result, which no comparison downstream can see.
+// The per-axis "tMin > tMax" early out of the reference is folded into one
+// final test: tMin only grows and tMax only shrinks, and tMin starts at
+// ray.tMin, tMax at ray.tMax, so the final "tMin > ray.tMax || tMax <
+// ray.tMin" test is implied by "tMin > tMax" as well.
+__device__ __forceinline__ void slabFast(float mn, float mx, float o, float inv, float& tMin, float& tMax) {
+    const float t0 = (mn - o) * inv;
+    const float t1 = (mx - o) * inv;
+    const bool neg = inv < 0.0f;
+    tMin = fmaxf(tMin, neg ? t1 : t0);
+    tMax = fminf(tMax, neg ? t0 : t1);
+}
+
+// Degenerate slab (|max - min| < FLT_EPSILON), Math/AABB.cu:11-19.  Returns
+// false for the early out of a ray parallel to the slab and outside it.
+__device__ __forceinline__ bool slabDegenerate(float mn, float o, float d, float& tMin, float& tMax) {
+    if (fabsf(d) < kFltEps) return !(fabsf(o - mn) > kFltEps);
+    const float t = (mn - o) / d;
+    tMin = fmaxf(tMin, t);
+    tMax = fminf(tMax, t);
     return true;
 }
 
 // AABB::intersect (Math/AABB.cu:6-46); flags bits 0-2 = degenerate axes.
 __device__ __forceinline__ bool boxTest(float3 mn, float3 mx, uint32_t flags, const TRay& r, float& tEntry) {
     float tMin = r.tMin, tMax = r.tMax;
-    bool ok = slab(mn.x, mx.x, r.o.x, r.d.x, r.inv.x, flags & 1u, tMin, tMax);
-    ok &= slab(mn.y, mx.y, r.o.y, r.d.y, r.inv.y, flags & 2u, tMin, tMax);
-    ok &= slab(mn.z, mx.z, r.o.z, r.d.z, r.inv.z, flags & 4u, tMin, tMax);
-    if (!ok || tMin > tMax) return false;
-    if (tMin > r.tMax || tMax < r.tMin) return false;
+    bool ok = true;
+    if (flags == 0u) {
+        slabFast(mn.x, mx.x, r.o.x, r.inv.x, tMin, tMax);
+        slabFast(mn.y, mx.y, r.o.y, r.inv.y, tMin, tMax);
+        slabFast(mn.z, mx.z, r.o.z, r.inv.z, tMin, tMax);
+    } else {
+        if (flags & 1u) ok &= slabDegenerate(mn.x, r.o.x, r.d.x, tMin, tMax);
+        else slabFast(mn.x, mx.x, r.o.x, r.inv.x, tMin, tMax);
+        if (flags & 2u) ok &= slabDegenerate(mn.y, r.o.y, r.d.y, tMin, tMax);
+        else slabFast(mn.y, mx.y, r.o.y, r.inv.y, tMin, tMax);
+        if (flags & 4u) ok &= slabDegenerate(mn.z, r.o.z, r.d.z, tMin, tMax);
+        else slabFast(mn.z, mx.z, r.o.z, r.inv.z, tMin, tMax);
+    }
     tEntry = tMin;
-    return true;
+    return ok && !(tMin > tMax);
 }
 
 __host__ __device__ __forceinline__ uint32_t degenerateFlags(float3 mn, float3 mx) {
@@ -82,14 +104,14 @@ __host__ __device__ __forceinline__ uint32_t degenerateFlags(float3 mn, float3 m
 // TriangleMeshSOA::intersect (Scene/Triangle.cu:40-75) on a pre-gathered block.
 __device__ __forceinline__ bool triTest(const float3& v0, const float3& e1, const float3& e2, const TRay& r,
                                         float& t, float& u, float& v) {
-    float3 p = cross(r.d, e2);
-    float det = dot(e1, p);
+    const float3 p = cross(r.d, e2);
+    const float det = dot(e1, p);
     if (fabsf(det) < 1e-6f) return false;
-    float invDet = 1.0f / det;
-    float3 tv = sub(r.o, v0);
+    const float invDet = 1.0f / det;
+    const float3 tv = sub(r.o, v0);
     u = dot(tv, p) * invDet;
     if (u < 0.0f || u > 1.0f) return false;
-    float3 q = cross(tv, e1);
+    const float3 q = cross(tv, e1);
     v = dot(r.d, q) * invDet;
     if (v < 0.0f || u + v > 1.0f) return false;
     t = dot(e2, q) * invDet;
@@ -100,7 +122,7 @@ __device__ __forceinline__ bool triTest(const float3& v0, const float3& e1, cons
 __device__ __forceinline__ void loadTri(const TriBlock* tris, uint32_t slot, float3& v0, float3& e1, float3& e2,
                                         uint32_t& prim) {
     const float4* p = reinterpret_cast<const float4*>(tris + slot);
-    float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
+    const float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
     v0 = mk3(a.x, a.y, a.z);
     prim = __float_as_uint(a.w);
     e1 = mk3(b.x, b.y, b.z);
@@ -109,65 +131,85 @@ __device__ __forceinline__ void loadTri(const TriBlock* tris, uint32_t slot, flo
 
 constexpr int kStackSize = 32;  // depth <= 20 bounds a near-first stack by 21
 
-// BVHData::intersect (Core/BVH.cu:13-84).  h.t must hold the initial
-// closest t (infinity for a fresh RayHit).  Returns whether any triangle
-// was hit inside [tMin, tMax] (not only closer ones), as the reference does.
+// Tests the triangles of leaf `ref` with the closest-hit rule of
+// Scene/Shape.h:26-31.  Returns true when the any-hit query can stop.
+template <bool kAnyHit>
+__device__ __forceinline__ bool leafTest(const SceneView& sc, const TRay& r, THit& h, bool& isHit, uint32_t ref) {
+    const uint2 leaf = __ldg(sc.leaves + (ref & ~kLeafBit));
+    for (uint32_t i = 0; i < leaf.y; ++i) {
+        float3 v0, e1, e2;
+        uint32_t prim;
+        loadTri(sc.tris, leaf.x + i, v0, e1, e2, prim);
+        float t, u, v;
+        if (triTest(v0, e1, e2, r, t, u, v)) {
+            if (t < r.tMin || t > r.tMax) continue;
+            isHit = true;
+            if (kAnyHit) return true;
+            if (t < h.t) {
+                h.t = t;
+                h.u = u;
+                h.v = v;
+                h.prim = prim;
+            }
+        }
+    }
+    return false;
+}
+
+// BVHData::intersect (Core/BVH.cu:13-84) for one ray.  h.t must hold the
+// initial closest t (infinity for a fresh RayHit).  Returns whether any
+// triangle was hit inside [tMin, tMax] (not only closer ones), as the
+// reference does.
+//
+// One loop; the entry e being visited lives in registers.  When both
+// children pass, the far one is pushed and the near one becomes e (the
+// reference pushes both and pops the near one at once); an entry taken from
+// the stack is culled at the top of the loop when its distance is beyond
+// the closest hit, as at Core/BVH.cu:34-36.
 template <bool kAnyHit>
 __device__ __forceinline__ bool traverse(const SceneView& sc, const TRay& r, THit& h) {
-    if (!sc.hasRoot) return false;
     float tr;
-    if (!boxTest(sc.rootMin, sc.rootMax, sc.rootFlags, r, tr)) return false;
+    if (!sc.hasRoot || !boxTest(sc.rootMin, sc.rootMax, sc.rootFlags, r, tr)) return false;
     uint2 stack[kStackSize];
     int sp = 0;
-    stack[sp++] = make_uint2(sc.rootRef, __float_as_uint(0.0f));
-    bool isHit = false;
-    while (sp > 0) {
-        const uint2 e = stack[--sp];
-        if (__uint_as_float(e.y) > h.t) continue;
+    uint2 e = make_uint2(sc.rootRef, __float_as_uint(0.0f));
+    bool have = true, isHit = false;
+    while (have) {
+        if (__uint_as_float(e.y) > h.t) {
+            have = sp > 0;
+            if (have) e = stack[--sp];
+            continue;
+        }
         if (e.x & kLeafBit) {
-            const uint2 leaf = __ldg(sc.leaves + (e.x & ~kLeafBit));
-            for (uint32_t i = 0; i < leaf.y; ++i) {
-                float3 v0, e1, e2;
-                uint32_t prim;
-                loadTri(sc.tris, leaf.x + i, v0, e1, e2, prim);
-                float t, u, v;
-                if (triTest(v0, e1, e2, r, t, u, v)) {
-                    if (t < r.tMin || t > r.tMax) continue;
-                    isHit = true;
-                    if (kAnyHit) return true;
-                    if (t < h.t) {
-                        h.t = t;
-                        h.u = u;
-                        h.v = v;
-                        h.prim = prim;
-                    }
-                }
-            }
-        } else {
-            const float4* np = reinterpret_cast<const float4*>(sc.pairs + e.x);
-            const float4 p0 = __ldg(np), p1 = __ldg(np + 1), p2 = __ldg(np + 2);
-            const uint4 ref = __ldg(reinterpret_cast<const uint4*>(np + 3));
-            float lt = INFINITY, rt = INFINITY;
-            bool hl = boxTest(mk3(p0.x, p0.y, p0.z), mk3(p0.w, p1.x, p1.y), ref.z & 7u, r, lt);
-            bool hr = boxTest(mk3(p1.z, p1.w, p2.x), mk3(p2.y, p2.z, p2.w), (ref.z >> 3) & 7u, r, rt);
-            const float ct = h.t;
-            if (hl && hr) {
-                if (lt > rt) {
-                    if (lt < ct) stack[sp++] = make_uint2(ref.x, __float_as_uint(lt));
-                    if (rt < ct) stack[sp++] = make_uint2(ref.y, __float_as_uint(rt));
-                } else {
-                    if (rt < ct) stack[sp++] = make_uint2(ref.y, __float_as_uint(rt));
-                    if (lt < ct) stack[sp++] = make_uint2(ref.x, __float_as_uint(lt));
-                }
-            } else if (hl && lt < ct) {
-                stack[sp++] = make_uint2(ref.x, __float_as_uint(lt));
-            } else if (hr && rt < ct) {
-                stack[sp++] = make_uint2(ref.y, __float_as_uint(rt));
-            }
-            if (sp > kStackSize - 2) {  // unreachable for depth <= 20; never overrun
+            if (leafTest<kAnyHit>(sc, r, h, isHit, e.x)) return true;
+            have = sp > 0;
+            if (have) e = stack[--sp];
+            continue;
+        }
+        const float4* np = reinterpret_cast<const float4*>(sc.pairs + e.x);
+        const float4 p0 = __ldg(np), p1 = __ldg(np + 1), p2 = __ldg(np + 2);
+        const uint4 ref = __ldg(reinterpret_cast<const uint4*>(np + 3));
+        float lt = INFINITY, rt = INFINITY;
+        const bool hl = boxTest(mk3(p0.x, p0.y, p0.z), mk3(p0.w, p1.x, p1.y), ref.z & 7u, r, lt);
+        const bool hr = boxTest(mk3(p1.z, p1.w, p2.x), mk3(p2.y, p2.z, p2.w), (ref.z >> 3) & 7u, r, rt);
+        const float ct = h.t;
+        const bool gl = hl && lt < ct, gr = hr && rt < ct;
+        if (gl && gr) {
+            // near = the child the reference pushes last: right when lt > rt
+            const bool rightNear = lt > rt;
+            if (sp >= kStackSize) {  // unreachable for depth <= 20; never overrun
                 atomicOr(sc.errFlags, kErrStackOverflow);
                 break;
             }
+            stack[sp++] = rightNear ? make_uint2(ref.x, __float_as_uint(lt)) : make_uint2(ref.y, __float_as_uint(rt));
+            e = rightNear ? make_uint2(ref.y, __float_as_uint(rt)) : make_uint2(ref.x, __float_as_uint(lt));
+        } else if (gl) {
+            e = make_uint2(ref.x, __float_as_uint(lt));
+        } else if (gr) {
+            e = make_uint2(ref.y, __float_as_uint(rt));
+        } else {
+            have = sp > 0;
+            if (have) e = stack[--sp];
         }
     }
     return isHit;

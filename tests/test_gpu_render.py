@@ -107,9 +107,11 @@ def test_bsdf_sample(gpu_lib, kind):
     m = _material(kind)
     gw, gf, gp = _gpu_bsdf_sample(m, n, wo, u)
     ow, of, op = oracle.bsdf_sample(m, n, wo, u)
+    # near the horizon z = sqrt(1 - x^2 - y^2) turns ulp differences of sin / cos
+    # into absolute errors of ~1e-6 in z, hence pdf and f (both <= 1/pi * max albedo)
     np.testing.assert_allclose(gw, ow, rtol=0, atol=2e-5)
-    np.testing.assert_allclose(gp, op, rtol=1e-4, atol=1e-6)
-    np.testing.assert_allclose(gf, of, rtol=1e-4, atol=1e-6)
+    np.testing.assert_allclose(gp, op, rtol=1e-4, atol=1e-5)
+    np.testing.assert_allclose(gf, of, rtol=1e-4, atol=1e-5)
 
 
 def _cornell(w=64, h=64, seed=0):
@@ -175,8 +177,12 @@ def test_film_accumulates_and_clears(gpu_lib):
     integ = PathTraceIntegrator()
     integ.dispatch(g, 4)
     w1 = cam.sensor.weight.copy()
-    integ.dispatch(g, 4, first_sample=4)  # the reference never clears the film between dispatches
+    # the reference never clears the film and restarts at sample index 0 on
+    # every dispatch: a second dispatch adds the same samples again
+    integ.dispatch(g, 4)
     assert np.allclose(cam.sensor.weight, 2 * w1, rtol=1e-5)
+    integ.dispatch(g, 4, first_sample=4)  # new sample indices: new jitter, more weight
+    assert (cam.sensor.weight > 2 * w1).mean() > 0.3
     g.film_clear()
     rgb, w = g.film_read()
     assert not rgb.any() and not w.any()
