@@ -18,6 +18,7 @@ CR_ERR_OUT_OF_MEMORY = 3
 CR_ERR_DEVICE = 4
 CR_ERR_UNSUPPORTED = 5
 CR_MISS = 0xFFFFFFFF
+CR_NOALLOC_MAX_RAYS = 65536
 
 RAY_DTYPE = np.dtype([("o", "<f4", 3), ("tmin", "<f4"), ("d", "<f4", 3), ("tmax", "<f4")])
 HIT_DTYPE = np.dtype([("prim", "<u4"), ("t", "<f4"), ("u", "<f4"), ("v", "<f4")])
@@ -80,6 +81,7 @@ SIGNATURES = [
     ("cr_camera_generate_rays", ctypes.c_int, [ctypes.POINTER(CrCamera), _P, _U64, _P]),
     ("cr_bsdf_evaluate", ctypes.c_int, [_P, _P, _P, _P, _U64, _P, _P]),
     ("cr_bsdf_sample", ctypes.c_int, [_P, _P, _P, _P, _U64, _P, _P, _P]),
+    ("cr_trace_closest_noalloc", ctypes.c_int, [_P, _P, _U64, _P, _P]),
     ("cr_kernel_launch_count", ctypes.c_uint64, []),
 ]
 

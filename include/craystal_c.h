@@ -227,6 +227,26 @@ int cr_bsdf_sample(const cr_material* mat, const float* n, const float* wo,
                    const float* u, uint64_t count, float* wi, float* f,
                    float* pdf);
 
+/* Closest-hit query on host buffers that allocates no GPU memory.  This
+ * entry point has no counterpart in the reference.  It is for callers that
+ * cannot let a library allocate device memory: a host that has already
+ * committed its GPU memory budget to its own pool, a render thread that must
+ * not stall on the device synchronisation cudaMalloc / cudaFree imply, or a
+ * plugin whose host forbids allocation after start-up.  Rays and hits pass
+ * through a fixed staging area inside the library's device image
+ * (CR_NOALLOC_MAX_RAYS rays and hits, 3 MiB, held by every GPU that loads the
+ * library until the process exits); n above CR_NOALLOC_MAX_RAYS is rejected
+ * with CR_ERR_INVALID_ARGUMENT.  The staging area is shared by all calls on a
+ * device: calls whose work overlaps on the GPU race on it, so callers
+ * serialise them.  The first call on a device looks up the staging area's
+ * device address (set-up, done once per device); make that first call before
+ * any stream capture begins.  Results equal cr_trace_closest's.  Returns when
+ * the hits are in the host array; the copies and the traversal run on
+ * `stream` (NULL = legacy default stream). */
+#define CR_NOALLOC_MAX_RAYS 65536u
+int cr_trace_closest_noalloc(cr_scene* scene, const cr_ray* rays, uint64_t n,
+                             cr_hit* hits, void* stream);
+
 /* Number of kernel launches this library issued since the process started
  * (all entry points); for launch accounting in benchmarks. */
 uint64_t cr_kernel_launch_count(void);
