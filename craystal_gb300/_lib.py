@@ -46,6 +46,11 @@ class CrBvhStats(ctypes.Structure):
                 ("build_ms", ctypes.c_double), ("device_bytes", ctypes.c_uint64)]
 
 
+class CrMlpConfig(ctypes.Structure):
+    _fields_ = [("lr", ctypes.c_float), ("beta1", ctypes.c_float), ("beta2", ctypes.c_float), ("eps", ctypes.c_float),
+                ("seed", ctypes.c_uint32)]
+
+
 class CrayError(RuntimeError):
     """Raised for a non-zero status of the C ABI (the reference throws
     RuntimeError from CRAYSTAL_CHECK / CRAYSTAL_CUDA_CHECK)."""
@@ -82,6 +87,14 @@ SIGNATURES = [
     ("cr_bsdf_evaluate", ctypes.c_int, [_P, _P, _P, _P, _U64, _P, _P]),
     ("cr_bsdf_sample", ctypes.c_int, [_P, _P, _P, _P, _U64, _P, _P, _P]),
     ("cr_trace_closest_noalloc", ctypes.c_int, [_P, _P, _U64, _P, _P]),
+    ("cr_mlp_param_count", ctypes.c_uint64, []),
+    ("cr_mlp_create", ctypes.c_int, [ctypes.POINTER(CrMlpConfig), ctypes.POINTER(ctypes.c_void_p)]),
+    ("cr_mlp_destroy", ctypes.c_int, [_P]),
+    ("cr_mlp_get_params", ctypes.c_int, [_P, _P]),
+    ("cr_mlp_set_params", ctypes.c_int, [_P, _P]),
+    ("cr_mlp_infer", ctypes.c_int, [_P, _P, _U64, _P]),
+    ("cr_mlp_gradients", ctypes.c_int, [_P, _P, _P, _U64, _P, _P]),
+    ("cr_mlp_train_step", ctypes.c_int, [_P, _P, _P, _U64, _P]),
     ("cr_kernel_launch_count", ctypes.c_uint64, []),
 ]
 

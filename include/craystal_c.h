@@ -247,6 +247,38 @@ int cr_bsdf_sample(const cr_material* mat, const float* n, const float* wo,
 int cr_trace_closest_noalloc(cr_scene* scene, const cr_ray* rays, uint64_t n,
                              cr_hit* hits, void* stream);
 
+/* ---- radiance-cache network (no counterpart in the reference) ----
+ * MLP with 7 inputs (position and direction mapped to [0,1]^3, roughness in
+ * [0,1]), a 12-frequency sin / cos encoding of each input (168 features), five
+ * hidden layers of 64 ReLU units and 3 linear outputs (RGB radiance); FP16
+ * weights and activations with FP32 accumulation on the tensor cores; Adam on
+ * FP32 master weights; loss = mean over samples and channels of
+ * (y - t)^2 / (sg(y)^2 + 0.01).  Parameters are a flat FP32 vector, layer
+ * after layer, each layer k-major (W[k][n] at k * N + n; layer shapes
+ * 176x64, 64x64 four times, 64x3; rows 168..175 of the first layer meet
+ * zero features). */
+typedef struct {
+    float lr;       /* Adam step size (1e-2) */
+    float beta1;    /* 0.9 */
+    float beta2;    /* 0.99 */
+    float eps;      /* 1e-8 */
+    uint32_t seed;  /* initialisation */
+} cr_mlp_config;
+typedef struct cr_mlp cr_mlp;
+uint64_t cr_mlp_param_count(void);
+int cr_mlp_create(const cr_mlp_config* cfg, cr_mlp** out);
+int cr_mlp_destroy(cr_mlp* mlp);
+int cr_mlp_get_params(cr_mlp* mlp, float* params);
+int cr_mlp_set_params(cr_mlp* mlp, const float* params);
+/* inputs: n x 7 host floats; outputs: n x 3 host floats (not clamped) */
+int cr_mlp_infer(cr_mlp* mlp, const float* inputs, uint64_t n, float* outputs);
+/* gradient of the loss over n samples (no update); grads = param_count floats */
+int cr_mlp_gradients(cr_mlp* mlp, const float* inputs, const float* targets,
+                     uint64_t n, float* grads, float* loss);
+/* one Adam step on n samples; loss (may be NULL) before the step */
+int cr_mlp_train_step(cr_mlp* mlp, const float* inputs, const float* targets,
+                      uint64_t n, float* loss);
+
 /* Number of kernel launches this library issued since the process started
  * (all entry points); for launch accounting in benchmarks. */
 uint64_t cr_kernel_launch_count(void);

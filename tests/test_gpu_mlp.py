@@ -1,0 +1,95 @@
+"""The radiance-cache network on the tensor cores against its FP64 numpy
+definition (oracle/mlp.py): inference, gradients, and that training on the
+GPU lowers the loss.  Tolerances: outputs agree to 1e-3 relative (FP32
+accumulation of FP16 products); gradients to 2e-2 in relative norm per layer
+(FP16 rounding of intermediate gradients amplified through five layers)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from oracle import mlp as ref
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture()
+def net(gpu_lib):
+    from craystal_gb300._lib import CrMlpConfig, check, load
+    cfg = CrMlpConfig(1e-2, 0.9, 0.99, 1e-8, 7)
+    h = ctypes.c_void_p()
+    check(load().cr_mlp_create(ctypes.byref(cfg), ctypes.byref(h)))
+    yield h
+    load().cr_mlp_destroy(h)
+
+
+def _params(h):
+    from craystal_gb300._lib import check, load, ptr
+    p = np.zeros(load().cr_mlp_param_count(), np.float32)
+    check(load().cr_mlp_get_params(h, ptr(p)))
+    return p
+
+
+def _inputs(n, seed):
+    rng = np.random.default_rng(seed)
+    x = rng.random((n, 7)).astype(np.float32)
+    t = (0.5 + 0.4 * np.sin(6 * x[:, :3]) * np.cos(3 * x[:, 3:6])).astype(np.float32)
+    return x, t
+
+
+def test_param_count_and_layout(gpu_lib):
+    from craystal_gb300._lib import load
+    assert load().cr_mlp_param_count() == ref.N_PARAMS == 27840
+
+
+def test_inference_matches_fp64(net):
+    from craystal_gb300._lib import check, load, ptr
+    x, _ = _inputs(3000, 1)
+    out = np.zeros((len(x), 3), np.float32)
+    check(load().cr_mlp_infer(net, ptr(x), len(x), ptr(out)))
+    y, _ = ref.forward(_params(net), x)
+    np.testing.assert_allclose(out, y, rtol=1e-3, atol=1e-3 * np.abs(y).max())
+
+
+def test_gradients_match_fp64(net):
+    from craystal_gb300._lib import check, load, ptr
+    x, t = _inputs(4096, 2)
+    g = np.zeros(load().cr_mlp_param_count(), np.float32)
+    loss = ctypes.c_float()
+    check(load().cr_mlp_gradients(net, ptr(x), ptr(t), len(x), ptr(g), ctypes.byref(loss)))
+    lref, gref = ref.loss_and_grads(_params(net), x, t)
+    assert abs(loss.value - lref) <= 1e-3 * lref
+    o = 0
+    for k, n in ref.SHAPES:
+        a, b = g[o:o + k * n], gref[o:o + k * n]
+        assert np.linalg.norm(a - b) <= 2e-2 * np.linalg.norm(b), (k, n)
+        o += k * n
+
+
+def test_training_reduces_loss(net):
+    from craystal_gb300._lib import check, load, ptr
+    x, t = _inputs(1 << 14, 3)
+    losses = []
+    for _ in range(300):
+        loss = ctypes.c_float()
+        check(load().cr_mlp_train_step(net, ptr(x), ptr(t), len(x), ctypes.byref(loss)))
+        losses.append(loss.value)
+    assert losses[-1] < 0.1 * losses[0], (losses[0], losses[-1])
+
+
+def test_adam_step_matches_fp64(net):
+    """One GPU Adam step equals the FP64 update computed from the GPU's own
+    gradient (isolates the optimiser from gradient rounding)."""
+    from craystal_gb300._lib import check, load, ptr
+    x, t = _inputs(2048, 4)
+    p0 = _params(net).astype(np.float64)
+    g = np.zeros(load().cr_mlp_param_count(), np.float32)
+    check(load().cr_mlp_gradients(net, ptr(x), ptr(t), len(x), ptr(g), None))
+    check(load().cr_mlp_train_step(net, ptr(x), ptr(t), len(x), None))
+    p1 = _params(net)
+    expect, _, _ = ref.adam_step(p0, 0.0, 0.0, g.astype(np.float64), 1)
+    # the first Adam step moves each weight by lr * g / (|g| + eps); compare
+    # where |g| is well above the float-atomic noise of the two gradient passes
+    m = np.abs(g) > 1e-6
+    assert m.mean() > 0.5
+    np.testing.assert_allclose(p1[m], expect[m], rtol=1e-5, atol=1e-6)
