@@ -193,6 +193,59 @@ def cornell_extra(torch):
             "rays_per_path": round(rays / paths, 3)}
 
 
+def cache_extra(torch, res=512):
+    """Equal-time relMSE of the radiance-cache integrator against the plain
+    path tracer on the Cornell box (res x res, max depth 8, NEE + MIS).  The
+    reference is the plain tracer at 4096 spp with its films of 512-spp
+    passes summed in FP64.  The plain arm renders 64 spp; the cache arm,
+    after 64 untimed training frames, renders as many frames (1 spp each,
+    training included) as fit in the plain arm's time."""
+    from craystal_gb300 import scenes
+    from craystal_gb300.api import CachedPathTraceIntegrator, PathTraceIntegrator, Scene
+    data, cam = scenes.cornell_box(seed=0, width=res, height=res)
+    sc = Scene(data)
+    sc.setCamera(cam)
+    cfg = PathTraceIntegrator.Configs(maxDepth=8, rrThreshold=0.05, useMIS=True)
+    plain = PathTraceIntegrator(cfg, compat=False)
+    acc = np.zeros((res, res, 3))
+    accw = np.zeros((res, res))
+    for k in range(8):
+        sc.film_clear()
+        plain.dispatch(sc, 512, first_sample=1_000_000 + 512 * k, readback=False)
+        rgb, w = sc.film_read()
+        acc += rgb
+        accw += w
+    ref = acc / accw[..., None]
+
+    def rel_mse(rgb, w):
+        img = np.nan_to_num((rgb / w[..., None]).astype(np.float64))
+        return float(np.mean((img - ref) ** 2 / (ref ** 2 + 1e-2)))
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        fn()
+        torch.cuda.synchronize()
+        return time.perf_counter() - t
+
+    sc.film_clear()
+    t_plain = timed(lambda: plain.dispatch(sc, 64, readback=False))
+    e_plain = rel_mse(*sc.film_read())
+    integ = CachedPathTraceIntegrator(cfg, train_every=16)
+    integ.dispatch(sc, 64, first_sample=2_000_000, readback=False)
+    sc.film_clear()
+    t16 = timed(lambda: integ.dispatch(sc, 16, first_sample=3_000_000, readback=False))
+    frames = max(1, int(16 * t_plain / t16))
+    sc.film_clear()
+    t_cache = timed(lambda: integ.dispatch(sc, frames, readback=False))
+    e_cache = rel_mse(*sc.film_read())
+    return {"config": f"cornell {res}x{res}, max depth 8, NEE+MIS; reference 4096 spp plain, FP64 film sum",
+            "plain_spp": 64, "plain_s": round(t_plain, 4), "plain_relmse": round(e_plain, 5),
+            "cache_frames": frames, "cache_s": round(t_cache, 4), "cache_relmse": round(e_cache, 5),
+            "relmse_ratio_plain_over_cache": round(e_plain / e_cache, 3),
+            "train_every": 16, "query_vertex": 1, "last_loss": round(float(integ.stats.last_loss), 5)}
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -273,6 +326,7 @@ def run_ours(args):
              "hit_fraction": round(float((hits_dev["prim"] != cg.CR_MISS).mean()), 4)}
     if not args.skip_extra:
         extra["path_tracer"] = cornell_extra(torch)
+        extra["radiance_cache_equal_time"] = cache_extra(torch)
 
     out = {"metric": METRIC, "value": round(value, 2), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,

@@ -51,6 +51,17 @@ class CrMlpConfig(ctypes.Structure):
                 ("seed", ctypes.c_uint32)]
 
 
+class CrCacheConfig(ctypes.Structure):
+    _fields_ = [("query_vertex", ctypes.c_uint32), ("train_every", ctypes.c_uint32),
+                ("train_samples", ctypes.c_uint32), ("train_steps", ctypes.c_uint32), ("freeze", ctypes.c_uint32),
+                ("scene_min", ctypes.c_float * 3), ("scene_max", ctypes.c_float * 3)]
+
+
+class CrCacheStats(ctypes.Structure):
+    _fields_ = [("frames", ctypes.c_uint64), ("queries", ctypes.c_uint64), ("train_records", ctypes.c_uint64),
+                ("last_loss", ctypes.c_float)]
+
+
 class CrayError(RuntimeError):
     """Raised for a non-zero status of the C ABI (the reference throws
     RuntimeError from CRAYSTAL_CHECK / CRAYSTAL_CUDA_CHECK)."""
@@ -95,6 +106,8 @@ SIGNATURES = [
     ("cr_mlp_infer", ctypes.c_int, [_P, _P, _U64, _P]),
     ("cr_mlp_gradients", ctypes.c_int, [_P, _P, _P, _U64, _P, _P]),
     ("cr_mlp_train_step", ctypes.c_int, [_P, _P, _P, _U64, _P]),
+    ("cr_render_cached", ctypes.c_int, [_P, ctypes.POINTER(CrIntegratorConfig), ctypes.POINTER(CrCacheConfig), _P,
+                                        _U32, _U32, _P, ctypes.POINTER(CrCacheStats)]),
     ("cr_kernel_launch_count", ctypes.c_uint64, []),
 ]
 

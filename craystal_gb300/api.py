@@ -312,3 +312,73 @@ def kernel_launch_count() -> int:
 
 def version() -> str:
     return load().cr_version().decode()
+
+
+class RadianceCache:
+    """The online-trained MLP radiance cache (no counterpart in the
+    reference): cr_mlp_* plus cr_render_cached."""
+
+    def __init__(self, lr=1e-2, beta1=0.9, beta2=0.99, eps=1e-8, seed=0):
+        from ._lib import CrMlpConfig
+        h = ctypes.c_void_p()
+        cfg = CrMlpConfig(lr, beta1, beta2, eps, seed)
+        check(load().cr_mlp_create(ctypes.byref(cfg), ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            load().cr_mlp_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def params(self) -> np.ndarray:
+        p = np.zeros(load().cr_mlp_param_count(), np.float32)
+        check(load().cr_mlp_get_params(self._h, ptr(p)))
+        return p
+
+    def set_params(self, p: np.ndarray):
+        p = np.ascontiguousarray(p, np.float32)
+        check(load().cr_mlp_set_params(self._h, ptr(p)))
+
+    def infer(self, x: np.ndarray) -> np.ndarray:
+        x = np.ascontiguousarray(x, np.float32)
+        out = np.zeros((len(x), 3), np.float32)
+        check(load().cr_mlp_infer(self._h, ptr(x), len(x), ptr(out)))
+        return out
+
+
+class CachedPathTraceIntegrator(PathTraceIntegrator):
+    """Path tracing with the radiance cache: one frame = one sample per pixel
+    (cr_render_cached)."""
+
+    def __init__(self, configs=None, compat=False, query_vertex=1, train_every=16, train_samples=65536,
+                 train_steps=1, cache: "RadianceCache" = None):
+        super().__init__(configs or PathTraceIntegrator.Configs(), compat)
+        from ._lib import CrCacheConfig, CrCacheStats
+        self.cache = cache or RadianceCache()
+        self.cc = CrCacheConfig(query_vertex, train_every, train_samples, train_steps, 0)
+        self.stats = CrCacheStats()
+
+    def dispatch(self, scene: "Scene", frames: int, first_sample: int = 0, stream: int = 0, readback: bool = True,
+                 freeze: bool = False):
+        cam = scene.getCamera()
+        if cam is None or cam.sensor is None:
+            raise _lib.CrayError(_lib.CR_ERR_INVALID_ARGUMENT, "scene has no camera with a sensor")
+        scene.setCamera(cam)
+        cfg = self.device_config()
+        self.cc.freeze = 1 if freeze else 0
+        check(load().cr_render_cached(scene.handle, ctypes.byref(cfg), ctypes.byref(self.cc), self.cache.handle,
+                                      int(frames), int(first_sample), stream or None, ctypes.byref(self.stats)))
+        if readback:
+            rgb, wt = scene.film_read()
+            cam.sensor.data[...] = rgb
+            cam.sensor.weight[...] = wt

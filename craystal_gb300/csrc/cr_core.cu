@@ -96,6 +96,7 @@ void freeScene(cr_scene* s) {
                     s->buildNodes, s->errFlags, s->filmRgb, s->filmW, s->rayCounter};
     for (void* p : ptrs)
         if (p) cudaFree(p);
+    freeCacheBuffers(s->cacheBuffers);
     for (int k = 0; k < 2; k++) {
         if (s->stageRays[k]) cudaFree(s->stageRays[k]);
         if (s->stageHits[k]) cudaFree(s->stageHits[k]);

@@ -176,6 +176,8 @@ struct cr_scene {
     cr_hit* stageHits[2] = {nullptr, nullptr};
     uint8_t* stageOcc[2] = {nullptr, nullptr};
     uint64_t stageCap = 0;
+    // buffers of the radiance-cache integrator (cr_cache.cu), created on first use
+    void* cacheBuffers = nullptr;
 
     cr::SceneView view() const {
         cr::SceneView v;
@@ -213,5 +215,7 @@ int traceOccludedDevice(cr_scene* s, const cr_ray* rays, uint64_t n, uint8_t* oc
 int renderDevice(cr_scene* s, const cr_integrator_config* cfg, uint32_t spp, uint32_t first,
                  cudaStream_t st);
 int resolveFilm(cr_scene* s, float* rgbHost);
+// implemented in cr_cache.cu
+void freeCacheBuffers(void* buffers);
 
 }  // namespace cr

@@ -71,6 +71,7 @@ __host__ __device__ constexpr int bwdOffset(int l) {
 constexpr int kBwdHalves = bwdOffset(kLayers);
 
 constexpr int kWarps = 4;
+constexpr float kGradClip = 256.0f;  // |dL/dy| per sample and channel
 constexpr int kThreads = kWarps * 32;
 
 __device__ __forceinline__ void mma16816(float c[4], const uint32_t a[4], uint32_t b0, uint32_t b1) {
@@ -316,7 +317,10 @@ __global__ void __launch_bounds__(kThreads) kTrainFwdBwd(const __half* __restric
             if (r < n && col < 3) {
                 const float y = o[q], t = target[r * 3 + col];
                 const float den = y * y + 0.01f;
-                d[q] = 2.0f * (y - t) / den;
+                // per-sample gradient clipped to +-kGradClip: the relative loss
+                // gradient of a far-off prediction (y ~ 0, t large) would
+                // otherwise overflow the FP16 gradient path
+                d[q] = fminf(fmaxf(2.0f * (y - t) / den, -kGradClip), kGradClip);
                 lossLocal += (y - t) * (y - t) / den;
             }
         }
@@ -599,10 +603,6 @@ float* mlpLossPtr(MlpState* s) { return s->loss; }
 }  // namespace cr
 
 using namespace cr;
-
-struct cr_mlp {
-    MlpState* s;
-};
 
 extern "C" {
 

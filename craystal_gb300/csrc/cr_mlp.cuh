@@ -20,3 +20,7 @@ int mlpAdamDevice(MlpState* s, cudaStream_t st);
 float* mlpLossPtr(MlpState* s);
 
 }  // namespace cr
+
+struct cr_mlp {
+    cr::MlpState* s;
+};

@@ -1,0 +1,203 @@
+// cr_path.cuh -- the path-tracing loop of pathTraceKernel<useMIS>
+// (Core/Integrator.cu:142-227) with sampleLight (:21-72) and evalMIS
+// (:74-140), shared by the plain megakernel (cr_render.cu) and the
+// radiance-cache integrator (cr_cache.cu) through a hook called at every
+// surface vertex.
+#pragma once
+
+#include "cr_internal.cuh"
+#include "cr_math.cuh"
+#include "cr_shading.cuh"
+#include "cr_traverse.cuh"
+
+namespace cr {
+
+struct Params {
+    uint32_t maxDepth;
+    float rrThreshold;
+    uint32_t useMIS;
+    uint32_t spp;
+    uint32_t first;
+    uint32_t sppPerBlock;
+};
+
+struct PathCtx {
+    const SceneView& sc;
+    uint32_t rays;
+};
+
+__device__ __forceinline__ bool closest(PathCtx& c, float3 o, float3 d, THit& h) {
+    c.rays++;
+    h.t = INFINITY;
+    h.prim = CR_MISS;
+    h.u = h.v = 0.0f;
+    return traverse<false>(c.sc, makeTRay(o, 0.0f, d, INFINITY), h);
+}
+
+__device__ __forceinline__ bool occluded(PathCtx& c, float3 o, float3 d, float tMax) {
+    c.rays++;
+    THit h;
+    h.t = INFINITY;
+    return traverse<true>(c.sc, makeTRay(o, 0.0f, d, tMax), h);
+}
+
+struct LightSample {
+    Spec weight;
+    float3 dirW;
+    float pdf;
+    uint32_t id;
+    float selectPdf;
+};
+
+// sampleLight, Core/Integrator.cu:21-72
+__device__ __forceinline__ LightSample sampleLight(PathCtx& c, const Isect& it, const Bsdf& bsdf, Sampler& smp) {
+    const SceneView& sc = c.sc;
+    LightSample ls;
+    ls.weight = sp(0.0f);
+    ls.dirW = mk3(0.0f, 0.0f, 0.0f);
+    ls.pdf = 0.0f;
+    ls.id = 0;
+    ls.selectPdf = 0.0f;
+    const int cnt = (int)sc.nEmissive;
+    if (cnt == 0) return ls;
+    const int pick = min(f2iX86((float)cnt * smp.next1D()), cnt - 1);
+    const uint32_t id = sc.emissive[pick];
+    const TriVerts tri = loadTriangle(sc, id);
+    const float2 b = sampleBarycentric(smp.next2D());
+    const float3 w = mk3((1.f - b.x) - b.y, b.x, b.y);
+    const float3 vp = interp(tri.p, w);
+    const float3 vn = interp(tri.n, w);
+    const float3 target = offsetRayOrigin(vp, faceNormal(tri));
+    const float3 toLight = sub(target, it.posW);
+    const float distSqr = dot(toLight, toLight);
+    const float dist = sqrtf(distSqr);
+    const float3 dir = divs(toLight, dist);
+    const float3 ofn = it.orientedFaceNormal();
+    if (dot(ofn, dir) < 0.0f || dot(vn, dir) > 0.0f || dist < kEps) return ls;
+    const float3 so = offsetRayOrigin(it.posW, ofn);
+    const float tMax = length(sub(so, target)) - kEps;
+    if (occluded(c, so, dir, tMax)) return ls;
+    const MaterialGpu& m = materialOf(sc, id);
+    ls.weight = mul(bsdf.evaluate(it.viewW, dir), sp(m.em[0], m.em[1], m.em[2]));
+    ls.dirW = dir;
+    ls.pdf = distSqr / (triArea(tri) * absDot(dir, vn));
+    ls.id = id;
+    ls.selectPdf = (float)(1.0 / (double)cnt);
+    return ls;
+}
+
+// evalMIS, Core/Integrator.cu:74-140
+__device__ __forceinline__ Spec evalMIS(PathCtx& c, const Isect& it, const Bsdf& bsdf, Sampler& smp) {
+    const SceneView& sc = c.sc;
+    Spec value = sp(0.0f);
+    const LightSample ls = sampleLight(c, it, bsdf, smp);
+    if (ls.pdf <= 0.0f) return value;
+    {
+        const float lightPdf = ls.pdf;
+        if (lightPdf > 0.0f) {
+            const float bsdfPdf = bsdf.evaluatePdf(it.viewW, ls.dirW);
+            if (bsdfPdf > 0.0f) value = add(value, divs(mul(powerHeuristic(lightPdf, bsdfPdf), ls.weight), lightPdf));
+        }
+    }
+    {
+        float3 dir;
+        float bsdfPdf = 0.0f;
+        const Spec w = bsdf.sampleEvaluate(smp.next2D(), it.viewW, dir, bsdfPdf);
+        if (maxValue(w) > 0.0f && bsdfPdf > 0.0f) {
+            const float3 o = offsetRayOrigin(it.posW, it.orientedFaceNormal());
+            THit h;
+            if (closest(c, o, dir, h) && h.prim == ls.id) {
+                // createIntersection of the light hit: only its position and
+                // face normal are read
+                const TriVerts tri = loadTriangle(sc, h.prim);
+                const float3 lpos = add(o, mul(h.t, dir));
+                const float3 lfn = faceNormal(tri);
+                const MaterialGpu& m = materialOf(sc, h.prim);
+                if (m.flags & CR_MATERIAL_EMISSIVE) {
+                    const Spec em = sp(m.em[0], m.em[1], m.em[2]);
+                    const float3 toLight = sub(lpos, it.posW);
+                    const float distSqr = dot(toLight, toLight);
+                    const float3 lv = divs(toLight, sqrtf(distSqr));
+                    const float cosL = absDot(lv, lfn);
+                    if (cosL != 0.0f) {
+                        const float area = triArea(tri);
+                        const float lightPdf = distSqr / (area * cosL);
+                        value = add(value, divs(mul(mul(powerHeuristic(bsdfPdf, lightPdf), em), w), bsdfPdf));
+                    }
+                }
+            }
+        }
+    }
+    return divs(value, ls.selectPdf);
+}
+
+// CameraProxy::generateRay, Core/CameraProxy.h:25-40
+__device__ __forceinline__ float3 cameraDir(const CameraGpu& cam, float2 s) {
+    const float u = 2.0f * (s.x / (float)cam.width) - 1.0f;
+    const float v = 1.0f - 2.0f * (s.y / (float)cam.height);
+    return normalize(add(add(mul(cam.U, u * cam.halfW), mul(cam.V, v * cam.halfH)), cam.W));
+}
+
+// Hooks of tracePath: called at every surface vertex before it is shaded
+// (depth = vertex index, 0 = the camera ray's hit); returning true ends the
+// path there.  The plain integrator uses NoHooks.
+struct NoHooks {
+    __device__ __forceinline__ bool atVertex(uint32_t, const Isect&, const MaterialGpu&, const Spec&, const Spec&) {
+        return false;
+    }
+};
+
+// pathTraceKernel body for one (pixel, sample index).
+template <class Hooks>
+__device__ __forceinline__ Spec tracePath(PathCtx& c, const CameraGpu& cam, const Params& p, uint32_t x, uint32_t y,
+                                          uint32_t si, float2& pixel, Hooks& hk) {
+    const SceneView& sc = c.sc;
+    Sampler smp(x, y, si);
+    const float2 j = smp.next2D();
+    pixel = make_float2((float)x + j.x, (float)y + j.y);
+    float3 ro = cam.pos;
+    float3 rd = cameraDir(cam, pixel);
+    Spec radiance = sp(0.0f), beta = sp(1.0f);
+    for (uint32_t depth = 0; depth < p.maxDepth; depth++) {
+        bool terminate = false;
+        THit h;
+        if (closest(c, ro, rd, h)) {
+            const Isect it = makeIsect(sc, ro, rd, h.t, h.u, h.v, h.prim);
+            const MaterialGpu& m = materialOf(sc, h.prim);
+            if (hk.atVertex(depth, it, m, beta, radiance)) break;
+            if (m.flags & CR_MATERIAL_EMISSIVE) {
+                radiance = add(radiance, mul(sp(m.em[0], m.em[1], m.em[2]), beta));
+                break;
+            }
+            Bsdf bsdf;
+            bsdf.init(m, it.frame);
+            if (p.useMIS) {
+                radiance = add(radiance, mul(evalMIS(c, it, bsdf, smp), beta));
+            } else {
+                const LightSample ls = sampleLight(c, it, bsdf, smp);
+                if (ls.pdf > 0.0f) radiance = add(radiance, divs(divs(mul(ls.weight, beta), ls.pdf), ls.selectPdf));
+            }
+            float3 wi;
+            float pdf = 0.0f;
+            const Spec f = bsdf.sampleEvaluate(smp.next2D(), it.viewW, wi, pdf);
+            if (pdf <= 0.0f) break;
+            beta = mul(beta, divs(f, pdf));
+            ro = offsetRayOrigin(it.posW, it.orientedFaceNormal());
+            rd = wi;
+        } else {
+            terminate = true;
+        }
+        if (smp.next1D() < p.rrThreshold) terminate = true;
+        if (terminate) break;
+        if (depth > 5) {
+            float q = smax(p.rrThreshold, 1.0f - maxValue(beta));
+            q = q < 0.0f ? 0.0f : (1.0f < q ? 1.0f : q);
+            if (smp.next1D() < q) break;
+            beta = divs(beta, 1.0f - q);
+        }
+    }
+    return radiance;
+}
+
+
+}  // namespace cr

@@ -279,6 +279,37 @@ int cr_mlp_gradients(cr_mlp* mlp, const float* inputs, const float* targets,
 int cr_mlp_train_step(cr_mlp* mlp, const float* inputs, const float* targets,
                       uint64_t n, float* loss);
 
+/* ---- path tracing with the radiance cache (no counterpart in the
+ * reference) ----
+ * Each frame renders one sample per pixel.  Most paths stop at
+ * query_vertex (1 = the hit of the first bounce) and take the network's
+ * radiance there, weighted by the path throughput; one pixel in train_every
+ * (a hash of pixel and sample index) traces its whole path with the plain
+ * estimator, adds that unbiased sample to the film, and turns every vertex
+ * v >= 1 into a training record (inputs at v, target = radiance gathered from
+ * v on / throughput at v).  After each frame the network takes train_steps
+ * Adam steps on at most train_samples records (none when freeze is set).
+ * Frames use sample indices first_sample, first_sample + 1, ... */
+typedef struct {
+    uint32_t query_vertex;   /* 1 */
+    uint32_t train_every;    /* 16 */
+    uint32_t train_samples;  /* 65536 (2^16 path suffixes per frame) */
+    uint32_t train_steps;    /* 1 */
+    uint32_t freeze;         /* 1 = render with the cache as it is, no training */
+    float scene_min[3];      /* position normalisation box; scene_max <= scene_min */
+    float scene_max[3];      /* selects the scene's bounds */
+} cr_cache_config;
+typedef struct {
+    uint64_t frames;
+    uint64_t queries;
+    uint64_t train_records;
+    float last_loss;
+} cr_cache_stats;
+/* stats (may be NULL) is added to, not reset. */
+int cr_render_cached(cr_scene* scene, const cr_integrator_config* cfg,
+                     const cr_cache_config* cache, cr_mlp* mlp, uint32_t frames,
+                     uint32_t first_sample, void* stream, cr_cache_stats* stats);
+
 /* Number of kernel launches this library issued since the process started
  * (all entry points); for launch accounting in benchmarks. */
 uint64_t cr_kernel_launch_count(void);

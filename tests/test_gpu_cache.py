@@ -1,0 +1,101 @@
+"""The radiance-cache integrator (cr_render_cached) against the plain path
+tracer, which is the judge of its error.
+
+- With every pixel a training path the cached integrator traces exactly the
+  plain tracer's paths: equal films (float-atomic summation order aside).
+- Queries, training records and the loss stay finite.
+- At equal time the cached image is closer to a 4096-spp reference (plain
+  tracer, films of 512-spp passes summed in FP64) than the plain image.
+relMSE = mean((I - R)^2 / (R^2 + 1e-2))."""
+import time
+
+import numpy as np
+import pytest
+
+from craystal_gb300 import scenes
+from craystal_gb300.api import CachedPathTraceIntegrator, PathTraceIntegrator, Scene
+
+pytestmark = pytest.mark.gpu
+
+CFG = PathTraceIntegrator.Configs(maxDepth=8, rrThreshold=0.05, useMIS=True)
+
+
+def rel_mse(a, b):
+    a = np.nan_to_num(np.asarray(a, np.float64))
+    b = np.nan_to_num(np.asarray(b, np.float64))
+    return float(np.mean((a - b) ** 2 / (b ** 2 + 1e-2)))
+
+
+def cornell(res):
+    data, cam = scenes.cornell_box(seed=0, width=res, height=res)
+    sc = Scene(data)
+    sc.setCamera(cam)
+    return sc, cam
+
+
+def test_all_training_paths_equal_plain(gpu_lib):
+    sc, cam = cornell(64)
+    PathTraceIntegrator(CFG, compat=False).dispatch(sc, 8, first_sample=3)
+    plain_rgb, plain_w = cam.sensor.data.copy(), cam.sensor.weight.copy()
+    plain_rays = sc.render_ray_count()
+    sc.film_clear()
+    integ = CachedPathTraceIntegrator(CFG, train_every=1)
+    integ.dispatch(sc, 8, first_sample=3)
+    np.testing.assert_allclose(cam.sensor.weight, plain_w, rtol=1e-5)
+    np.testing.assert_allclose(cam.sensor.data, plain_rgb, rtol=1e-4, atol=1e-5)
+    assert sc.render_ray_count() == plain_rays
+    assert integ.stats.queries == 0 and integ.stats.train_records > 0
+
+
+def test_cache_bookkeeping_and_finite(gpu_lib):
+    sc, cam = cornell(128)
+    integ = CachedPathTraceIntegrator(CFG, train_every=8)
+    integ.dispatch(sc, 32)
+    st = integ.stats
+    assert st.frames == 32
+    assert st.queries > 0.5 * 32 * 128 * 128 * (7 / 8)  # most rendering paths reach the query vertex
+    assert st.train_records > 0
+    assert np.isfinite(st.last_loss)
+    img = cam.sensor.createImage()
+    assert np.isfinite(img).all()
+    # the cache's predictions stay finite and non-negative after clamping
+    x = np.random.default_rng(0).random((1000, 7)).astype(np.float32)
+    assert np.isfinite(integ.cache.infer(x)).all()
+
+
+def test_equal_time_cache_beats_plain(gpu_lib):
+    import torch
+    res = 256
+    sc, cam = cornell(res)
+    plain = PathTraceIntegrator(CFG, compat=False)
+    acc = np.zeros((res, res, 3))
+    accw = np.zeros((res, res))
+    for k in range(8):
+        sc.film_clear()
+        plain.dispatch(sc, 512, first_sample=1_000_000 + 512 * k, readback=False)
+        rgb, w = sc.film_read()
+        acc += rgb
+        accw += w
+    ref = acc / accw[..., None]
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        fn()
+        torch.cuda.synchronize()
+        return time.perf_counter() - t
+
+    integ = CachedPathTraceIntegrator(CFG, train_every=16)
+    integ.dispatch(sc, 64, first_sample=2_000_000, readback=False)  # warm-up training
+    sc.film_clear()
+    t_cache = timed(lambda: integ.dispatch(sc, 64, readback=False))
+    rgb, w = sc.film_read()
+    e_cache = rel_mse(rgb / w[..., None], ref)
+    sc.film_clear()
+    t64 = timed(lambda: plain.dispatch(sc, 64, readback=False))
+    spp = max(1, int(64 * t_cache / t64))
+    sc.film_clear()
+    plain.dispatch(sc, spp, readback=False)
+    rgb, w = sc.film_read()
+    e_plain = rel_mse(rgb / w[..., None], ref)
+    assert e_cache < e_plain, (e_cache, e_plain, spp, t_cache, t64)
