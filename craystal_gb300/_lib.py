@@ -26,6 +26,7 @@ MATERIAL_DTYPE = np.dtype([("diffuse", "<f4", 3), ("specular", "<f4", 3), ("emis
                            ("shininess", "<f4"), ("type", "<u4"), ("flags", "<u4")])
 MESH_DTYPE = np.dtype([("index_offset", "<u4"), ("index_count", "<u4"), ("vertex_offset", "<u4"),
                        ("material_id", "<u4")])
+SPHERE_LIGHT_DTYPE = np.dtype([("center", "<f4", 3), ("radius", "<f4"), ("emission", "<f4", 3), ("pad", "<f4")])
 BVH_NODE_DTYPE = np.dtype([("bmin", "<f4", 3), ("bmax", "<f4", 3), ("is_leaf", "<u4"), ("a", "<u4"), ("b", "<u4")])
 
 
@@ -85,6 +86,8 @@ SIGNATURES = [
     ("cr_scene_bvh_stats", ctypes.c_int, [_P, ctypes.POINTER(CrBvhStats)]),
     ("cr_scene_bvh_export", ctypes.c_int, [_P, _P, _P]),
     ("cr_scene_set_camera", ctypes.c_int, [_P, ctypes.POINTER(CrCamera)]),
+    ("cr_scene_set_environment", ctypes.c_int, [_P, _P]),
+    ("cr_scene_set_sphere_lights", ctypes.c_int, [_P, _P, _U32]),
     ("cr_film_clear", ctypes.c_int, [_P]),
     ("cr_film_read", ctypes.c_int, [_P, _P, _P]),
     ("cr_film_resolve", ctypes.c_int, [_P, _P]),

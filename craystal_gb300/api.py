@@ -202,6 +202,18 @@ class Scene:
     def getCamera(self) -> Optional[Camera]:
         return self._camera
 
+    # --- lights beyond the reference (extensions) ---
+    def set_environment(self, radiance):
+        e = np.asarray(radiance, np.float32).reshape(3)
+        check(load().cr_scene_set_environment(self._h, ptr(e)))
+
+    def set_sphere_lights(self, lights):
+        """lights: iterable of (center xyz, radius, emission rgb)."""
+        arr = np.zeros(len(lights), _lib.SPHERE_LIGHT_DTYPE)
+        for i, (c, r, em) in enumerate(lights):
+            arr[i] = (c, r, em, 0.0)
+        check(load().cr_scene_set_sphere_lights(self._h, ptr(arr) if len(arr) else None, len(arr)))
+
     # --- BVH introspection (Core/BVH.cu:111-115 logs the same figures) ---
     def bvh_stats(self) -> dict:
         st = CrBvhStats()
@@ -275,9 +287,10 @@ class PathTraceIntegrator:
             self.rrThreshold = rrThreshold
             self.useMIS = useMIS
 
-    def __init__(self, configs: "PathTraceIntegrator.Configs" = None, compat: bool = True):
+    def __init__(self, configs: "PathTraceIntegrator.Configs" = None, compat: bool = True, spectral: bool = False):
         self.configs = configs or PathTraceIntegrator.Configs()
         self.compat = compat
+        self.spectral = spectral  # hero-wavelength spectral rendering (an extension)
 
     def device_config(self) -> CrIntegratorConfig:
         c = CrIntegratorConfig()
@@ -286,7 +299,7 @@ class PathTraceIntegrator:
         else:
             c.max_depth, c.rr_threshold = self.configs.maxDepth, self.configs.rrThreshold
         c.use_mis = 1 if self.configs.useMIS else 0
-        c.flags = 0
+        c.flags = 1 if self.spectral else 0
         return c
 
     def dispatch(self, scene: Scene, spp: int, first_sample: int = 0, stream: int = 0, readback: bool = True):

@@ -115,7 +115,7 @@ __global__ void __launch_bounds__(256) kRenderCached(const SceneView sc, const C
                                                      float* __restrict__ tTarget, uint32_t* __restrict__ tCount,
                                                      unsigned long long* __restrict__ rayCounter) {
     const uint32_t x = blockIdx.x * 16 + threadIdx.x, y = blockIdx.y * 16 + threadIdx.y;
-    PathCtx c{sc, 0u};
+    PathCtx c{sc, 0u, SpectralPath{}};
     if (x < cam.width && y < cam.height) {
         const uint32_t si = p.first;
         const bool train = cp.trainEvery > 0 && hash3(x, y, si) % cp.trainEvery == 0;
@@ -266,7 +266,11 @@ int renderCached(cr_scene* s, const cr_integrator_config* cfg, const cr_cache_co
     cp.sceneInvExtent = mk3(ext.x > 0 ? 1.0f / ext.x : 0.0f, ext.y > 0 ? 1.0f / ext.y : 0.0f,
                             ext.z > 0 ? 1.0f / ext.z : 0.0f);
     cp.queryVertex = cc->query_vertex;
-    cp.trainEvery = cc->train_every;
+    // train_every 0: about train_samples records per frame at ~3 records per
+    // training path
+    const uint64_t px = (uint64_t)s->cam.width * s->cam.height;
+    cp.trainEvery = cc->train_every ? cc->train_every
+                                    : (uint32_t)std::max<uint64_t>(1, (px * 3 + trainCap / 2) / trainCap);
     cp.trainCap = trainCap;
     Params p;
     p.maxDepth = cfg->max_depth;
@@ -274,6 +278,8 @@ int renderCached(cr_scene* s, const cr_integrator_config* cfg, const cr_cache_co
     p.useMIS = cfg->use_mis ? 1u : 0u;
     p.spp = 1;
     p.sppPerBlock = 1;
+    p.spectral = 0;
+    p.wb = mk3(1.0f, 1.0f, 1.0f);
     const uint32_t W = s->cam.width, H = s->cam.height;
     dim3 grid((W + 15) / 16, (H + 15) / 16), block(16, 16);
     const uint32_t steps = cc->train_steps ? cc->train_steps : 1u;
@@ -328,6 +334,8 @@ extern "C" int cr_render_cached(cr_scene* scene, const cr_integrator_config* cfg
     if (!scene || !cfg || !cc || !mlp) return fail(CR_ERR_INVALID_ARGUMENT, "NULL argument");
     if (!scene->hasCamera) return fail(CR_ERR_INVALID_ARGUMENT, "scene has no camera; call cr_scene_set_camera");
     if (cfg->max_depth > 1024) return fail(CR_ERR_INVALID_ARGUMENT, "max_depth %u", cfg->max_depth);
+    if (cfg->flags & CR_RENDER_SPECTRAL)
+        return fail(CR_ERR_UNSUPPORTED, "the radiance cache learns RGB radiance; spectral rendering is not cached");
     if (cc->query_vertex == 0 || cc->query_vertex >= cfg->max_depth)
         return fail(CR_ERR_INVALID_ARGUMENT, "query_vertex %u must be in [1, max_depth)", cc->query_vertex);
     CR_CUDA(cudaSetDevice(scene->device));

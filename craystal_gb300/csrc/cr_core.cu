@@ -93,7 +93,7 @@ void freeScene(cr_scene* s) {
     cudaSetDevice(s->device);
     void* ptrs[] = {s->pos,  s->nrm,      s->uv,         s->idx,        s->primToMesh, s->meshes,
                     s->mats, s->emissive, s->pairs,      s->leaves,     s->tris,       s->slotToPrim,
-                    s->buildNodes, s->errFlags, s->filmRgb, s->filmW, s->rayCounter};
+                    s->buildNodes, s->errFlags, s->filmRgb, s->filmW, s->rayCounter, s->spheres, s->sphereEm};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     freeCacheBuffers(s->cacheBuffers);
@@ -260,6 +260,44 @@ int cr_scene_set_camera(cr_scene* scene, const cr_camera* cam) {
     }
     scene->cam = c;
     scene->hasCamera = true;
+    return CR_OK;
+}
+
+int cr_scene_set_environment(cr_scene* scene, const float radiance[3]) {
+    clearError();
+    if (!scene || !radiance) return fail(CR_ERR_INVALID_ARGUMENT, "NULL argument");
+    for (int k = 0; k < 3; k++)
+        if (!std::isfinite(radiance[k]) || radiance[k] < 0.0f)
+            return fail(CR_ERR_INVALID_ARGUMENT, "environment radiance must be finite and non-negative");
+    scene->env = mk3(radiance[0], radiance[1], radiance[2]);
+    return CR_OK;
+}
+
+int cr_scene_set_sphere_lights(cr_scene* scene, const cr_sphere_light* lights, uint32_t n) {
+    clearError();
+    if (!scene || (n && !lights)) return fail(CR_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (n > kMaxSphereLights) return fail(CR_ERR_INVALID_ARGUMENT, "at most %u sphere lights", kMaxSphereLights);
+    std::vector<float4> sp(n), em(n);
+    for (uint32_t i = 0; i < n; i++) {
+        const cr_sphere_light& l = lights[i];
+        if (!(l.radius > 0.0f) || !std::isfinite(l.radius))
+            return fail(CR_ERR_INVALID_ARGUMENT, "sphere light %u radius %g", i, l.radius);
+        sp[i] = make_float4(l.center[0], l.center[1], l.center[2], l.radius);
+        em[i] = make_float4(l.emission[0], l.emission[1], l.emission[2], 0.0f);
+    }
+    CR_CUDA(cudaSetDevice(scene->device));
+    CR_CUDA(cudaDeviceSynchronize());
+    if (scene->spheres) cudaFree(scene->spheres);
+    if (scene->sphereEm) cudaFree(scene->sphereEm);
+    scene->spheres = scene->sphereEm = nullptr;
+    scene->nSpheres = 0;
+    if (n) {
+        CR_CUDA(cudaMalloc(&scene->spheres, n * sizeof(float4)));
+        CR_CUDA(cudaMalloc(&scene->sphereEm, n * sizeof(float4)));
+        CR_CUDA(cudaMemcpy(scene->spheres, sp.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
+        CR_CUDA(cudaMemcpy(scene->sphereEm, em.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
+    }
+    scene->nSpheres = n;
     return CR_OK;
 }
 

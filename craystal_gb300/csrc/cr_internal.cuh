@@ -135,7 +135,14 @@ struct SceneView {
     float3 rootMin, rootMax;
     uint32_t hasRoot;
     uint32_t* errFlags;
+    float3 env;                    // constant environment radiance (0 = none)
+    uint32_t nSpheres;             // sphere lights
+    const float4* spheres;         // (center, radius)
+    const float4* sphereEm;        // (emission, 0)
 };
+
+constexpr uint32_t kSpherePrim = 0xFFFFFF00u;  // hit ids kSpherePrim + i for sphere light i
+constexpr uint32_t kMaxSphereLights = 64;
 
 }  // namespace cr
 
@@ -178,6 +185,11 @@ struct cr_scene {
     uint64_t stageCap = 0;
     // buffers of the radiance-cache integrator (cr_cache.cu), created on first use
     void* cacheBuffers = nullptr;
+    // lights beyond the reference
+    float3 env{0, 0, 0};
+    uint32_t nSpheres = 0;
+    float4* spheres = nullptr;
+    float4* sphereEm = nullptr;
 
     cr::SceneView view() const {
         cr::SceneView v;
@@ -199,6 +211,10 @@ struct cr_scene {
         v.rootMax = rootMax;
         v.hasRoot = hasRoot;
         v.errFlags = errFlags;
+        v.env = env;
+        v.nSpheres = nSpheres;
+        v.spheres = spheres;
+        v.sphereEm = sphereEm;
         return v;
     }
 };

@@ -8,6 +8,7 @@
 #include "cr_internal.cuh"
 #include "cr_math.cuh"
 #include "cr_shading.cuh"
+#include "cr_spectral.cuh"
 #include "cr_traverse.cuh"
 
 namespace cr {
@@ -19,23 +20,68 @@ struct Params {
     uint32_t spp;
     uint32_t first;
     uint32_t sppPerBlock;
+    uint32_t spectral;  // CR_RENDER_SPECTRAL: channels carry three wavelengths
+    float3 wb;          // white balance of the spectral film conversion
 };
 
 struct PathCtx {
     const SceneView& sc;
     uint32_t rays;
+    SpectralPath spec;  // set by tracePath
 };
 
+__device__ __forceinline__ Spec emissionOf(const PathCtx& c, const MaterialGpu& m) {
+    return toPathSpec(c.spec, m.em[0], m.em[1], m.em[2]);
+}
+
+__device__ __forceinline__ void initBsdf(const PathCtx& c, Bsdf& b, const MaterialGpu& m, const Frame& f) {
+    b.init(m, f);
+    if (c.spec.on) {
+        b.kd = toPathSpec(c.spec, m.kd[0], m.kd[1], m.kd[2]);
+        b.ks = toPathSpec(c.spec, m.ks[0], m.ks[1], m.ks[2]);
+    }
+}
+
+// Nearest intersection t of a ray with a sphere (centre c, radius r) in
+// (tMin, tMax), or INFINITY (geometric form: oc = o - c, b = oc.d / d.d).
+__device__ __forceinline__ float raySphere(float3 o, float3 d, float4 s, float tMin, float tMax) {
+    const float3 oc = sub(o, mk3(s.x, s.y, s.z));
+    const float a = dot(d, d);
+    const float b = dot(oc, d) / a;
+    const float c = (dot(oc, oc) - s.w * s.w) / a;
+    const float disc = b * b - c;
+    if (disc < 0.0f) return INFINITY;
+    const float q = sqrtf(disc);
+    const float t0 = -b - q, t1 = -b + q;
+    if (t0 > tMin && t0 < tMax) return t0;
+    if (t1 > tMin && t1 < tMax) return t1;
+    return INFINITY;
+}
+
+// SceneView::intersect (Scene/Scene.cu:5-14): the BVH, then the sphere
+// lights (an extension) under the closest-hit rule.
 __device__ __forceinline__ bool closest(PathCtx& c, float3 o, float3 d, THit& h) {
     c.rays++;
     h.t = INFINITY;
     h.prim = CR_MISS;
     h.u = h.v = 0.0f;
-    return traverse<false>(c.sc, makeTRay(o, 0.0f, d, INFINITY), h);
+    bool hit = traverse<false>(c.sc, makeTRay(o, 0.0f, d, INFINITY), h);
+    for (uint32_t i = 0; i < c.sc.nSpheres; i++) {
+        const float t = raySphere(o, d, __ldg(c.sc.spheres + i), 0.0f, h.t);
+        if (t < h.t) {
+            h.t = t;
+            h.prim = kSpherePrim + i;
+            hit = true;
+        }
+    }
+    return hit;
 }
 
+// SceneView::intersectOcclusion (Scene/Scene.cu:16-29), spheres included.
 __device__ __forceinline__ bool occluded(PathCtx& c, float3 o, float3 d, float tMax) {
     c.rays++;
+    for (uint32_t i = 0; i < c.sc.nSpheres; i++)
+        if (raySphere(o, d, __ldg(c.sc.spheres + i), 0.0f, tMax) < INFINITY) return true;
     THit h;
     h.t = INFINITY;
     return traverse<true>(c.sc, makeTRay(o, 0.0f, d, tMax), h);
@@ -78,7 +124,7 @@ __device__ __forceinline__ LightSample sampleLight(PathCtx& c, const Isect& it, 
     const float tMax = length(sub(so, target)) - kEps;
     if (occluded(c, so, dir, tMax)) return ls;
     const MaterialGpu& m = materialOf(sc, id);
-    ls.weight = mul(bsdf.evaluate(it.viewW, dir), sp(m.em[0], m.em[1], m.em[2]));
+    ls.weight = mul(bsdf.evaluate(it.viewW, dir), emissionOf(c, m));
     ls.dirW = dir;
     ls.pdf = distSqr / (triArea(tri) * absDot(dir, vn));
     ls.id = id;
@@ -114,7 +160,7 @@ __device__ __forceinline__ Spec evalMIS(PathCtx& c, const Isect& it, const Bsdf&
                 const float3 lfn = faceNormal(tri);
                 const MaterialGpu& m = materialOf(sc, h.prim);
                 if (m.flags & CR_MATERIAL_EMISSIVE) {
-                    const Spec em = sp(m.em[0], m.em[1], m.em[2]);
+                    const Spec em = emissionOf(c, m);
                     const float3 toLight = sub(lpos, it.posW);
                     const float distSqr = dot(toLight, toLight);
                     const float3 lv = divs(toLight, sqrtf(distSqr));
@@ -152,6 +198,7 @@ template <class Hooks>
 __device__ __forceinline__ Spec tracePath(PathCtx& c, const CameraGpu& cam, const Params& p, uint32_t x, uint32_t y,
                                           uint32_t si, float2& pixel, Hooks& hk) {
     const SceneView& sc = c.sc;
+    c.spec = makeSpectralPath(p.spectral != 0, x, y, si);
     Sampler smp(x, y, si);
     const float2 j = smp.next2D();
     pixel = make_float2((float)x + j.x, (float)y + j.y);
@@ -162,15 +209,20 @@ __device__ __forceinline__ Spec tracePath(PathCtx& c, const CameraGpu& cam, cons
         bool terminate = false;
         THit h;
         if (closest(c, ro, rd, h)) {
+            if (h.prim >= kSpherePrim) {  // a sphere light (extension)
+                const float4 e = __ldg(sc.sphereEm + (h.prim - kSpherePrim));
+                radiance = add(radiance, mul(toPathSpec(c.spec, e.x, e.y, e.z), beta));
+                break;
+            }
             const Isect it = makeIsect(sc, ro, rd, h.t, h.u, h.v, h.prim);
             const MaterialGpu& m = materialOf(sc, h.prim);
             if (hk.atVertex(depth, it, m, beta, radiance)) break;
             if (m.flags & CR_MATERIAL_EMISSIVE) {
-                radiance = add(radiance, mul(sp(m.em[0], m.em[1], m.em[2]), beta));
+                radiance = add(radiance, mul(emissionOf(c, m), beta));
                 break;
             }
             Bsdf bsdf;
-            bsdf.init(m, it.frame);
+            initBsdf(c, bsdf, m, it.frame);
             if (p.useMIS) {
                 radiance = add(radiance, mul(evalMIS(c, it, bsdf, smp), beta));
             } else {
@@ -185,6 +237,10 @@ __device__ __forceinline__ Spec tracePath(PathCtx& c, const CameraGpu& cam, cons
             ro = offsetRayOrigin(it.posW, it.orientedFaceNormal());
             rd = wi;
         } else {
+            // a miss ends the path (Core/Integrator.cu:205-207), after
+            // collecting the constant environment when there is one (extension)
+            if (sc.env.x > 0.0f || sc.env.y > 0.0f || sc.env.z > 0.0f)
+                radiance = add(radiance, mul(toPathSpec(c.spec, sc.env.x, sc.env.y, sc.env.z), beta));
             terminate = true;
         }
         if (smp.next1D() < p.rrThreshold) terminate = true;

@@ -32,14 +32,14 @@ __global__ void __launch_bounds__(kTileW* kTileW) kRender(const SceneView sc, co
     __syncthreads();
     const int tx0 = blockIdx.x * kTileW, ty0 = blockIdx.y * kTileW;
     const uint32_t x = tx0 + threadIdx.x, y = ty0 + threadIdx.y;
-    PathCtx c{sc, 0u};
+    PathCtx c{sc, 0u, SpectralPath{}};
     if (x < cam.width && y < cam.height) {
         const uint32_t s0 = blockIdx.z * p.sppPerBlock;
         const uint32_t s1 = min(p.spp, s0 + p.sppPerBlock);
         for (uint32_t s = s0; s < s1; s++) {
             float2 pix;
             NoHooks hk;
-            const Spec L = tracePath(c, cam, p, x, y, p.first + s, pix, hk);
+            const Spec L = pathSpecToRgb(c.spec, tracePath(c, cam, p, x, y, p.first + s, pix, hk), p.wb);
             // SensorData::addSample, Core/Sensor.cu:19-43
             if (isnan(L.r) || isnan(L.g) || isnan(L.b) || isinf(L.r) || isinf(L.g) || isinf(L.b)) continue;
             int xa = (int)floorf(pix.x - 1.0f), ya = (int)floorf(pix.y - 1.0f);
@@ -112,6 +112,8 @@ int renderDevice(cr_scene* s, const cr_integrator_config* cfg, uint32_t spp, uin
     p.useMIS = cfg->use_mis ? 1u : 0u;
     p.spp = spp;
     p.first = first;
+    p.spectral = (cfg->flags & CR_RENDER_SPECTRAL) ? 1u : 0u;
+    p.wb = whiteBalance();
     const uint32_t tilesX = (s->cam.width + kTileW - 1) / kTileW, tilesY = (s->cam.height + kTileW - 1) / kTileW;
     // enough blocks to fill every SM several times over, at most 8 samples
     // per thread per launch run

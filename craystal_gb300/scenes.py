@@ -158,3 +158,110 @@ def random_rays(n: int, seed: int = 1, tmin: float = 1e-4) -> np.ndarray:
     rays["tmin"] = np.float32(tmin)
     rays["tmax"] = np.float32(np.inf)
     return rays
+
+
+# ---------------------------------------------------------------------------
+# radiance-cache scene: displaced icospheres on a ground plane
+# ---------------------------------------------------------------------------
+def icosphere(level: int):
+    """Unit icosphere: vertices (float64) and faces after `level` 4:1 subdivisions."""
+    t = (1.0 + 5.0 ** 0.5) / 2.0
+    v = np.array([[-1, t, 0], [1, t, 0], [-1, -t, 0], [1, -t, 0], [0, -1, t], [0, 1, t], [0, -1, -t], [0, 1, -t],
+                  [t, 0, -1], [t, 0, 1], [-t, 0, -1], [-t, 0, 1]], np.float64)
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    f = np.array([[0, 11, 5], [0, 5, 1], [0, 1, 7], [0, 7, 10], [0, 10, 11], [1, 5, 9], [5, 11, 4], [11, 10, 2],
+                  [10, 7, 6], [7, 1, 8], [3, 9, 4], [3, 4, 2], [3, 2, 6], [3, 6, 8], [3, 8, 9], [4, 9, 5],
+                  [2, 4, 11], [6, 2, 10], [8, 6, 7], [9, 8, 1]], np.int64)
+    for _ in range(level):
+        n = len(v)
+        e = np.stack([f[:, [0, 1]], f[:, [1, 2]], f[:, [2, 0]]], 1).reshape(-1, 2)
+        es = np.sort(e, 1)
+        key = es[:, 0] * n + es[:, 1]
+        uniq, inv = np.unique(key, return_inverse=True)
+        i, j = np.divmod(uniq, n)
+        mid = v[i] + v[j]
+        mid /= np.linalg.norm(mid, axis=1, keepdims=True)
+        v = np.concatenate([v, mid])
+        m = (n + inv).reshape(-1, 3)  # ab, bc, ca
+        a, b, c = f[:, 0], f[:, 1], f[:, 2]
+        ab, bc, ca = m[:, 0], m[:, 1], m[:, 2]
+        f = np.concatenate([np.stack([a, ab, ca], 1), np.stack([b, bc, ab], 1), np.stack([c, ca, bc], 1),
+                            np.stack([ab, bc, ca], 1)])
+    return v, f
+
+
+def _hash3(ix, iy, iz, seed):
+    h = (ix.astype(np.uint32) * np.uint32(0x8DA6B343)) ^ (iy.astype(np.uint32) * np.uint32(0xD8163841)) ^ \
+        (iz.astype(np.uint32) * np.uint32(0xCB1AB31F)) ^ np.uint32(seed * 0x9E3779B1 & 0xFFFFFFFF)
+    h ^= h >> np.uint32(16)
+    h *= np.uint32(0x7FEB352D)
+    h ^= h >> np.uint32(15)
+    h *= np.uint32(0x846CA68B)
+    h ^= h >> np.uint32(16)
+    return (h >> np.uint32(8)).astype(np.float64) / 16777216.0
+
+
+def value_noise(p, seed=0):
+    """3D value noise in [0, 1]: hashed lattice values, smoothstep-trilinear."""
+    fl = np.floor(p)
+    fr = p - fl
+    w = fr * fr * (3.0 - 2.0 * fr)
+    i = fl.astype(np.int64)
+    out = 0.0
+    with np.errstate(over="ignore"):
+        for dx in (0, 1):
+            for dy in (0, 1):
+                for dz in (0, 1):
+                    val = _hash3(i[:, 0] + dx, i[:, 1] + dy, i[:, 2] + dz, seed)
+                    wx = w[:, 0] if dx else 1.0 - w[:, 0]
+                    wy = w[:, 1] if dy else 1.0 - w[:, 1]
+                    wz = w[:, 2] if dz else 1.0 - w[:, 2]
+                    out = out + val * wx * wy * wz
+    return out
+
+
+def vertex_normals(pos, faces):
+    fn = np.cross(pos[faces[:, 1]] - pos[faces[:, 0]], pos[faces[:, 2]] - pos[faces[:, 0]])
+    vn = np.zeros_like(pos)
+    for k in range(3):
+        np.add.at(vn, faces[:, k], fn)
+    return vn / np.maximum(np.linalg.norm(vn, axis=1, keepdims=True), 1e-20)
+
+
+def cache_scene(seed: int = 0, width: int = 1920, height: int = 1080, level: int = 7):
+    """Returns (SceneData, Camera, environment, sphere_lights) of the radiance-cache
+    workload: 8 displaced icospheres (20 * 4^level triangles each; level 7 gives
+    2,621,440 in all) with Principled materials on a 2-triangle ground plane,
+    a constant environment of 0.5 and one sphere light."""
+    rng = np.random.default_rng(seed)
+    base_v, base_f = icosphere(level)
+    meshes, mats = [], []
+    centers = [(x, z) for z in (-1.2, 1.2) for x in (-3.6, -1.2, 1.2, 3.6)]
+    for k, (cx, cz) in enumerate(centers):
+        disp = 1.0 + 0.05 * value_noise(base_v * 4.0 + 17.0 * k, seed)
+        r = 0.9
+        pos = base_v * (r * disp)[:, None] + np.array([cx, r, cz])
+        mats.append(MaterialData(diffuseRefl=tuple(float(c) for c in rng.uniform(0.0, 1.0, 3)),
+                                 specularRefl=(1.0, 1.0, 1.0) if rng.random() < 0.3 else (0.0, 0.0, 0.0),
+                                 type=MaterialType.Principled))
+        rough = float(rng.uniform(0.05, 1.0))
+        mats[-1].shininess = 2.0 / (rough * rough) - 1.0  # PrincipledBRDF.cu:51-55: r = sqrt(2 / (s + 1))
+        meshes.append(MeshData(position=pos.astype(np.float32), normal=vertex_normals(pos, base_f).astype(np.float32),
+                               index=base_f.astype(np.uint32).reshape(-1), materialID=len(mats) - 1))
+    g = 20.0
+    gp = np.array([[-g, 0, -g], [g, 0, -g], [g, 0, g], [-g, 0, g]], np.float32)
+    mats.append(MaterialData(diffuseRefl=(0.5, 0.5, 0.5), type=MaterialType.FullDiffuse))
+    meshes.append(MeshData(position=gp, normal=np.tile(np.float32([0, 1, 0]), (4, 1)),
+                           index=np.array([0, 2, 1, 0, 3, 2], np.uint32), materialID=len(mats) - 1))
+    for m in mats:
+        m.finalize()
+    data = SceneData(meshes=meshes, materials=mats, emissiveIndex=[])
+    cam = Camera()
+    cam.setWorldPosition((0.0, 3.2, 8.5))
+    cam.setTarget((0.0, 0.6, 0.0))
+    cam.setUp((0.0, 1.0, 0.0))
+    cam.setFovY(40.0)
+    cam.setSensor(Sensor((width, height)))
+    env = (0.5, 0.5, 0.5)
+    spheres = [((2.5, 6.0, 3.0), 1.0, (40.0, 38.0, 34.0))]
+    return data, cam, env, spheres

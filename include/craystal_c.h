@@ -97,8 +97,14 @@ typedef struct {
     uint32_t max_depth;
     float rr_threshold;
     uint32_t use_mis;
-    uint32_t flags;     /* reserved, 0 */
+    uint32_t flags;     /* CR_RENDER_* bits */
 } cr_integrator_config;
+
+/* Hero-wavelength spectral rendering (an extension; the reference renders
+ * RGB): every path carries three wavelengths over 360-830 nm, material RGB
+ * is upsampled to spectra, the film receives linear sRGB white-balanced so
+ * that a flat spectrum renders as in RGB. */
+#define CR_RENDER_SPECTRAL 1u
 
 /* Binary BVH node in the reference's layout (Core/BVH.h:17-30): nodes in
  * post-order with the root last; leaf: (a, b) = (first leaf slot, count),
@@ -165,6 +171,24 @@ int cr_scene_bvh_export(const cr_scene* scene, cr_bvh_node* nodes,
  * (Scene/Scene.h:56-58, Core/Camera.cu:35-39, Core/Sensor.cu:46-60).  A
  * sensor of a new size gets a new film, cleared to zero. */
 int cr_scene_set_camera(cr_scene* scene, const cr_camera* cam);
+
+/* ---- lights beyond the reference (extensions) ----
+ * The reference has neither: its paths end with 0 on a miss
+ * (Core/Integrator.cu:205-207) and it shades no sphere (bug 0.5k).
+ * Environment: constant radiance collected by every ray that leaves the
+ * scene.  Sphere lights: analytic emitting spheres, intersected in a linear
+ * loop after the BVH (as SceneView::intersect does for spheres,
+ * Scene/Scene.cu:5-14), occluding shadow rays, reached by BSDF sampling (not
+ * by next-event estimation, whose emitter list stays the triangle list). */
+typedef struct {
+    float center[3];
+    float radius;
+    float emission[3];
+    float pad;
+} cr_sphere_light;
+int cr_scene_set_environment(cr_scene* scene, const float radiance[3]);
+int cr_scene_set_sphere_lights(cr_scene* scene, const cr_sphere_light* lights,
+                               uint32_t n);
 
 /* Zeroes the film (the reference never clears its film, Core/Sensor.cu:55-59). */
 int cr_film_clear(cr_scene* scene);
@@ -292,7 +316,7 @@ int cr_mlp_train_step(cr_mlp* mlp, const float* inputs, const float* targets,
  * Frames use sample indices first_sample, first_sample + 1, ... */
 typedef struct {
     uint32_t query_vertex;   /* 1 */
-    uint32_t train_every;    /* 16 */
+    uint32_t train_every;    /* 16; 0 = about train_samples records per frame */
     uint32_t train_samples;  /* 65536 (2^16 path suffixes per frame) */
     uint32_t train_steps;    /* 1 */
     uint32_t freeze;         /* 1 = render with the cache as it is, no training */

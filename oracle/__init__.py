@@ -31,7 +31,7 @@ class OrcCamera(ctypes.Structure):
 
 class OrcConfig(ctypes.Structure):
     _fields_ = [("max_depth", ctypes.c_uint32), ("rr_threshold", ctypes.c_float), ("use_mis", ctypes.c_uint32),
-                ("reserved", ctypes.c_uint32)]
+                ("flags", ctypes.c_uint32)]
 
 
 class OrcStats(ctypes.Structure):
@@ -66,6 +66,7 @@ def lib():
             "orc_triangle_intersect": (None, [_P, _P, _P, _P, U64, _P, _P, _P, _P]),
             "orc_scene_create": (_P, [_P, _P, _P, U64, _P, U64, _P, U32, _P, U32, _P, U32]),
             "orc_scene_destroy": (None, [_P]),
+            "orc_scene_set_lights": (None, [_P, _P, _P, U32]),
             "orc_scene_bvh_stats": (None, [_P, ctypes.POINTER(OrcStats)]),
             "orc_scene_bvh_export": (None, [_P, _P, _P]),
             "orc_trace_closest": (None, [_P, _P, U64, _P, _P, I, ctypes.POINTER(OrcCounters)]),
@@ -75,6 +76,9 @@ def lib():
             "orc_bsdf_sample": (None, [_P, _P, _P, _P, U64, _P, _P, _P]),
             "orc_render": (None, [_P, ctypes.POINTER(OrcCamera), ctypes.POINTER(OrcConfig), U32, U32, U32, U32,
                                   _P, _P, I, ctypes.POINTER(ctypes.c_uint64)]),
+            "orc_spectral_cmf": (None, [_P, U64, _P]),
+            "orc_spectral_white_balance": (None, [_P]),
+            "orc_spectral_upsample": (None, [_P, _P, U64, _P]),
             "orc_hardware_threads": (I, []),
         }
         for name, (res, args) in sig.items():
@@ -165,6 +169,13 @@ class OracleScene:
             lib().orc_scene_destroy(self.h)
             self.h = None
 
+    def set_lights(self, env=(0.0, 0.0, 0.0), spheres=()):
+        """Environment radiance and sphere lights [(center, radius, emission)] (extensions)."""
+        e = np.asarray(env, np.float32)
+        sp = np.asarray([[*c, r, *em] for c, r, em in spheres], np.float32).reshape(-1, 7)
+        self._lights = (e, sp)
+        lib().orc_scene_set_lights(self.h, _p(e), _p(sp) if len(sp) else None, len(sp))
+
     def bvh_stats(self):
         st = OrcStats()
         lib().orc_scene_bvh_stats(self.h, ctypes.byref(st))
@@ -201,12 +212,12 @@ class OracleScene:
         return hits
 
     def render(self, cam: OrcCamera, max_depth=10, rr_threshold=0.05, use_mis=True, spp=1, first_sample=0,
-               rows=None, threads=0, film=None):
+               rows=None, threads=0, film=None, spectral=False):
         """FP64 film (rgb sum HxWx3, weight HxW) of spp samples; accumulates into film if given."""
         W, H = cam.width, cam.height
         if film is None:
             film = (np.zeros((H, W, 3), np.float64), np.zeros((H, W), np.float64))
-        cfg = OrcConfig(max_depth, rr_threshold, 1 if use_mis else 0, 0)
+        cfg = OrcConfig(max_depth, rr_threshold, 1 if use_mis else 0, 1 if spectral else 0)
         rays = ctypes.c_uint64()
         r0, r1 = rows if rows else (0, 0)
         lib().orc_render(self.h, ctypes.byref(cam), ctypes.byref(cfg), spp, first_sample, r0, r1, _p(film[0]),
@@ -236,3 +247,24 @@ def bsdf_sample(mat, n, wo, u):
 
 def hardware_threads() -> int:
     return int(lib().orc_hardware_threads())
+
+
+def spectral_cmf(lam):
+    lam = np.ascontiguousarray(lam, np.float32)
+    out = np.empty((len(lam), 3), np.float32)
+    lib().orc_spectral_cmf(_p(lam), len(lam), _p(out))
+    return out
+
+
+def spectral_white_balance():
+    out = np.empty(3, np.float32)
+    lib().orc_spectral_white_balance(_p(out))
+    return out
+
+
+def spectral_upsample(rgb, lam):
+    rgb = np.ascontiguousarray(rgb, np.float32).reshape(-1, 3)
+    lam = np.ascontiguousarray(lam, np.float32)
+    out = np.empty(len(lam), np.float32)
+    lib().orc_spectral_upsample(_p(rgb), _p(lam), len(lam), _p(out))
+    return out

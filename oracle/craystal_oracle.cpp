@@ -148,6 +148,91 @@ struct Sampler {
 };
 
 // ---------------------------------------------------------------------------
+// Hero-wavelength spectral mode (an extension; the reference is RGB only):
+// three wavelengths per path (hero ~ U[360, 830) nm from a hash of pixel and
+// sample index, plus rotations by 470/3 nm), RGB upsampled with the
+// partition of unity B_b = 1 - S((l-490)/15), B_r = S((l-590)/15),
+// B_g = 1 - B_b - B_r, film conversion with the Wyman-Sloan-Shirley (2013)
+// multi-lobe CIE 1931 fit and the IEC 61966-2-1 XYZ -> sRGB matrix,
+// white-balanced to the flat spectrum.
+// ---------------------------------------------------------------------------
+static float sigmoidf(float x) { return 1.0f / (1.0f + std::exp(-x)); }
+static float lobe(float l, float mu, float s1, float s2) {
+    float t = (l - mu) / (l < mu ? s1 : s2);
+    return std::exp(-0.5f * t * t);
+}
+static V3 cieXYZ(float l) {
+    float x = 1.056f * lobe(l, 599.8f, 37.9f, 31.0f) + 0.362f * lobe(l, 442.0f, 16.0f, 26.7f) -
+              0.065f * lobe(l, 501.1f, 20.4f, 26.2f);
+    float y = 0.821f * lobe(l, 568.8f, 46.9f, 40.5f) + 0.286f * lobe(l, 530.9f, 16.3f, 31.1f);
+    float z = 1.217f * lobe(l, 437.0f, 11.8f, 36.0f) + 0.681f * lobe(l, 459.0f, 26.0f, 13.8f);
+    return {x, y, z};
+}
+static V3 xyzToSrgb(V3 c) {
+    return {3.2404542f * c.x - 1.5371385f * c.y - 0.4985314f * c.z,
+            -0.9692660f * c.x + 1.8760108f * c.y + 0.0415560f * c.z,
+            0.0556434f * c.x - 0.2040259f * c.y + 1.0572252f * c.z};
+}
+struct Spectral {
+    bool on = false;
+    float lambda[3], br[3], bg[3], bb[3];
+};
+static uint32_t spectralHash(uint32_t x, uint32_t y, uint32_t s) {
+    uint32_t h = x * 0x9E3779B1u ^ (y + 0x7F4A7C15u) * 0x85EBCA77u ^ (s + 0x165667B1u) * 0xC2B2AE3Du;
+    h ^= h >> 15;
+    h *= 0x2C1B3C6Du;
+    h ^= h >> 12;
+    h *= 0x297A2D39u;
+    h ^= h >> 15;
+    return h;
+}
+static Spectral makeSpectral(bool on, uint32_t x, uint32_t y, uint32_t s) {
+    Spectral p;
+    p.on = on;
+    if (!on) return p;
+    float u = (float)(spectralHash(x, y, s) >> 8) * (1.0f / 16777216.0f);
+    for (int i = 0; i < 3; i++) {
+        float t = u + (float)i / 3.0f;
+        if (t >= 1.0f) t -= 1.0f;
+        float l = 360.0f + 470.0f * t;
+        p.lambda[i] = l;
+        p.bb[i] = 1.0f - sigmoidf((l - 490.0f) / 15.0f);
+        p.br[i] = sigmoidf((l - 590.0f) / 15.0f);
+        p.bg[i] = 1.0f - p.bb[i] - p.br[i];
+    }
+    return p;
+}
+static S3 toPathSpec(const Spectral& p, const float c[3]) {
+    if (!p.on) return {{c[0], c[1], c[2]}};
+    S3 r;
+    for (int i = 0; i < 3; i++) r.c[i] = (c[0] * p.br[i] + c[1] * p.bg[i]) + c[2] * p.bb[i];
+    return r;
+}
+static V3 whiteBalanceOracle();
+static S3 pathSpecToRgb(const Spectral& p, S3 L) {
+    if (!p.on) return L;
+    static const V3 wb = whiteBalanceOracle();
+    V3 xyz{0, 0, 0};
+    for (int i = 0; i < 3; i++) xyz = xyz + cieXYZ(p.lambda[i]) * L.c[i];
+    xyz = xyz * (470.0f / 3.0f);
+    V3 rgb = xyzToSrgb(xyz);
+    return {{rgb.x * wb.x, rgb.y * wb.y, rgb.z * wb.z}};
+}
+static V3 whiteBalanceOracle() {
+    double acc[3] = {0, 0, 0};
+    const int n = 4700;
+    const double dl = 470.0 / n;
+    for (int i = 0; i < n; i++) {
+        V3 c = cieXYZ((float)(360.0 + (i + 0.5) * dl));
+        acc[0] += c.x * dl;
+        acc[1] += c.y * dl;
+        acc[2] += c.z * dl;
+    }
+    V3 rgb = xyzToSrgb({(float)acc[0], (float)acc[1], (float)acc[2]});
+    return {1.0f / rgb.x, 1.0f / rgb.y, 1.0f / rgb.z};
+}
+
+// ---------------------------------------------------------------------------
 // Ray, offset, AABB, Math/Ray.cu, Math/AABB.cu
 // ---------------------------------------------------------------------------
 struct Ray {
@@ -269,6 +354,9 @@ struct orc_scene {
     std::vector<uint32_t> primMap;  // leaf slot -> primitive id
     AABB rootBounds;
     uint32_t rootIndex = 0;
+    // lights beyond the reference (extensions)
+    V3 env{0, 0, 0};
+    std::vector<float> spheres;  // center xyz, radius, emission xyz per light (7 floats)
     uint32_t maxDepth = 0, maxLeaf = 0, maxLeafDepth = 0;
 };
 
@@ -829,22 +917,48 @@ struct Bsdf {
     }
 };
 
-static S3 matEmission(const orc_material& m) {
-    return {{m.emission[0], m.emission[1], m.emission[2]}};
-}
 
 // ---------------------------------------------------------------------------
 // Integrator, Core/Integrator.cu:13-227
 // ---------------------------------------------------------------------------
+// Ray / sphere (extension), nearest t in (tMin, tMax) or +inf.
+static float raySphere(const Ray& r, const float* sph, float tMin, float tMax) {
+    V3 oc = r.o - V3{sph[0], sph[1], sph[2]};
+    float a = dot(r.d, r.d);
+    float b = dot(oc, r.d) / a;
+    float c = (dot(oc, oc) - sph[3] * sph[3]) / a;
+    float disc = b * b - c;
+    if (disc < 0.0f) return kFltInf;
+    float q = std::sqrt(disc);
+    float t0 = -b - q, t1 = -b + q;
+    if (t0 > tMin && t0 < tMax) return t0;
+    if (t1 > tMin && t1 < tMax) return t1;
+    return kFltInf;
+}
+
+constexpr uint32_t kSpherePrim = 0xFFFFFF00u;
+
 struct Tracer {
     const orc_scene& s;
     uint64_t rays = 0;
+    Spectral spec;
     bool intersect(const Ray& r, Hit& h) {
         rays++;
-        return bvhIntersect(s, r, h, nullptr);
+        bool hit = bvhIntersect(s, r, h, nullptr);
+        for (size_t i = 0; i < s.spheres.size() / 7; i++) {
+            float t = raySphere(r, &s.spheres[7 * i], 0.0f, h.t);
+            if (t < h.t) {
+                h.t = t;
+                h.prim = kSpherePrim + (uint32_t)i;
+                hit = true;
+            }
+        }
+        return hit;
     }
     bool occluded(const Ray& r) {
         rays++;
+        for (size_t i = 0; i < s.spheres.size() / 7; i++)
+            if (raySphere(r, &s.spheres[7 * i], 0.0f, r.tMax) < kFltInf) return true;
         Hit h;
         return bvhIntersect(s, r, h, nullptr);
     }
@@ -880,7 +994,7 @@ static LightSample sampleLight(Tracer& tr, const Intersection& it, const Bsdf& b
     sr.tMax = length(sr.o - target) - kEps;
     if (tr.occluded(sr)) return {};
     LightSample ls;
-    ls.weight = bsdf.evaluate(it.viewW, dir) * matEmission(materialOf(s, id));
+    ls.weight = bsdf.evaluate(it.viewW, dir) * toPathSpec(tr.spec, materialOf(s, id).emission);
     ls.dirW = dir;
     ls.pdf = distSqr / (tri.area() * absDot(dir, vd.n));
     ls.id = id;
@@ -914,7 +1028,7 @@ static S3 evalMIS(Tracer& tr, const Intersection& it, const Bsdf& bsdf, Sampler&
                 Intersection li = createIntersection(s, r, h);
                 const orc_material& m = materialOf(s, h.prim);
                 if (m.flags & 1u) {
-                    S3 em = matEmission(m);
+                    S3 em = toPathSpec(tr.spec, m.emission);
                     V3 toLight = li.posW - it.posW;
                     float distSqr = dot(toLight, toLight);
                     V3 lv = toLight / std::sqrt(distSqr);
@@ -973,6 +1087,7 @@ static Ray generateRay(const CameraData& c, V2 sp) {
 static S3 tracePath(Tracer& tr, const CameraData& cam, const orc_integrator_config& cfg,
                     uint32_t x, uint32_t y, uint32_t sampleIndex, V2& pixel) {
     const orc_scene& s = tr.s;
+    tr.spec = makeSpectral((cfg.flags & 1u) != 0, x, y, sampleIndex);
     Sampler sp(x, y, sampleIndex);
     V2 j = sp.next2D();
     pixel = {(float)x + j.x, (float)y + j.y};
@@ -982,13 +1097,22 @@ static S3 tracePath(Tracer& tr, const CameraData& cam, const orc_integrator_conf
         bool terminate = false;
         Hit h;
         if (tr.intersect(ray, h)) {
+            if (h.prim >= kSpherePrim) {  // sphere light (extension)
+                const float* sl = &s.spheres[7 * (h.prim - kSpherePrim)];
+                radiance = radiance + toPathSpec(tr.spec, sl + 4) * beta;
+                break;
+            }
             Intersection it = createIntersection(s, ray, h);
             const orc_material& m = materialOf(s, h.prim);
             if (m.flags & 1u) {
-                radiance = radiance + matEmission(m) * beta;
+                radiance = radiance + toPathSpec(tr.spec, m.emission) * beta;
                 break;
             }
             Bsdf bsdf(m, it.frame);
+            if (tr.spec.on) {
+                bsdf.kd = toPathSpec(tr.spec, m.diffuse);
+                bsdf.ks = toPathSpec(tr.spec, m.specular);
+            }
             if (cfg.use_mis) {
                 radiance = radiance + evalMIS(tr, it, bsdf, sp) * beta;
             } else {
@@ -1003,6 +1127,10 @@ static S3 tracePath(Tracer& tr, const CameraData& cam, const orc_integrator_conf
             ray.o = offsetRayOrigin(it.posW, it.orientedFaceNormal());
             ray.d = wi;
         } else {
+            if (s.env.x > 0.0f || s.env.y > 0.0f || s.env.z > 0.0f) {  // environment (extension)
+                const float e[3] = {s.env.x, s.env.y, s.env.z};
+                radiance = radiance + toPathSpec(tr.spec, e) * beta;
+            }
             terminate = true;
         }
         if (sp.next1D() < cfg.rr_threshold) terminate = true;
@@ -1134,6 +1262,11 @@ orc_scene* orc_scene_create(const float* pos, const float* nrm, const float* uv,
 }
 
 void orc_scene_destroy(orc_scene* s) { delete s; }
+
+void orc_scene_set_lights(orc_scene* s, const float* env3, const float* spheres7, uint32_t n_spheres) {
+    s->env = env3 ? V3{env3[0], env3[1], env3[2]} : V3{0, 0, 0};
+    s->spheres.assign(spheres7, spheres7 + 7 * (size_t)n_spheres);
+}
 
 void orc_scene_bvh_stats(const orc_scene* s, orc_bvh_stats* o) {
     std::memset(o, 0, sizeof(*o));
@@ -1276,7 +1409,7 @@ void orc_render(const orc_scene* s, const orc_camera* cam, const orc_integrator_
                 for (uint32_t x = 0; x < W; x++) {
                     for (uint32_t k = 0; k < spp; k++) {
                         V2 pix;
-                        S3 L = tracePath(tr, c, *cfg, x, y, first + k, pix);
+                        S3 L = pathSpecToRgb(tr.spec, tracePath(tr, c, *cfg, x, y, first + k, pix));
                         addSample(rgb.data(), w.data(), W, H, 0, (int)H, L, pix);
                     }
                 }
@@ -1292,6 +1425,31 @@ void orc_render(const orc_scene* s, const orc_camera* cam, const orc_integrator_
         for (size_t i = 0; i < (size_t)W * H; i++) film_w[i] += bandW[t][i];
     }
     if (rays_traced) *rays_traced = total;
+}
+
+void orc_spectral_cmf(const float* lambda, uint64_t n, float* xyz) {
+    for (uint64_t i = 0; i < n; i++) {
+        V3 c = cieXYZ(lambda[i]);
+        xyz[3 * i] = c.x;
+        xyz[3 * i + 1] = c.y;
+        xyz[3 * i + 2] = c.z;
+    }
+}
+
+void orc_spectral_white_balance(float* out3) {
+    V3 w = whiteBalanceOracle();
+    out3[0] = w.x;
+    out3[1] = w.y;
+    out3[2] = w.z;
+}
+
+void orc_spectral_upsample(const float* rgb, const float* lambda, uint64_t n, float* out) {
+    for (uint64_t i = 0; i < n; i++) {
+        float l = lambda[i];
+        float bb = 1.0f - sigmoidf((l - 490.0f) / 15.0f), br = sigmoidf((l - 590.0f) / 15.0f);
+        float bg = 1.0f - bb - br;
+        out[i] = (rgb[3 * i] * br + rgb[3 * i + 1] * bg) + rgb[3 * i + 2] * bb;
+    }
 }
 
 int orc_hardware_threads(void) { return (int)std::max(1u, std::thread::hardware_concurrency()); }

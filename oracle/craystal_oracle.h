@@ -96,7 +96,7 @@ typedef struct {
     uint32_t max_depth;     /* PathTraceIntegrator::DeviceView::maxDepth */
     float rr_threshold;     /* DeviceView::rrThreshold */
     uint32_t use_mis;       /* Configs::useMIS */
-    uint32_t reserved;
+    uint32_t flags;         /* 1 = hero-wavelength spectral rendering */
 } orc_integrator_config;
 
 /* Per-ray traversal counters, for the algorithmic byte count of the
@@ -140,6 +140,10 @@ orc_scene* orc_scene_create(const float* pos, const float* nrm,
                             const orc_material* mats, uint32_t n_mats,
                             const uint32_t* emissive, uint32_t n_emissive);
 void orc_scene_destroy(orc_scene* s);
+/* Lights beyond the reference (extensions): constant environment radiance
+ * and sphere lights (center xyz, radius, emission rgb per light). */
+void orc_scene_set_lights(orc_scene* s, const float* env3,
+                          const float* spheres7, uint32_t n_spheres);
 void orc_scene_bvh_stats(const orc_scene* s, orc_bvh_stats* out);
 /* Exports nodes (post-order, root last) and the leaf-slot -> primitive map. */
 void orc_scene_bvh_export(const orc_scene* s, orc_bvh_node* nodes,
@@ -173,6 +177,11 @@ void orc_render(const orc_scene* s, const orc_camera* cam,
                 uint32_t first_sample, uint32_t row_begin, uint32_t row_end,
                 double* film_rgb, double* film_w, int threads,
                 uint64_t* rays_traced);
+
+/* ---- hero-wavelength spectral mode (an extension) ---- */
+void orc_spectral_cmf(const float* lambda, uint64_t n, float* xyz);
+void orc_spectral_white_balance(float* out3);
+void orc_spectral_upsample(const float* rgb, const float* lambda, uint64_t n, float* out);
 
 int orc_hardware_threads(void);
 
