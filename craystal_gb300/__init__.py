@@ -6,5 +6,5 @@ its C ABI (include/craystal_c.h).
 """
 from ._lib import CrayError, HIT_DTYPE, MATERIAL_DTYPE, MESH_DTYPE, RAY_DTYPE, CR_MISS, LIB_PATH, load  # noqa: F401
 from .api import (CachedPathTraceIntegrator, Camera, MaterialData, MaterialFlags, MaterialType, MeshData,  # noqa: F401
-                  PathTraceIntegrator, RadianceCache,
+                  PathTraceIntegrator, RadianceCache, BatchRenderer,
                   Scene, SceneData, Sensor, flatten_scene, kernel_launch_count, version)

@@ -63,6 +63,18 @@ class CrCacheStats(ctypes.Structure):
                 ("last_loss", ctypes.c_float)]
 
 
+class CrBatchItem(ctypes.Structure):
+    _fields_ = [("config", CrIntegratorConfig), ("spp", ctypes.c_uint32), ("first_sample", ctypes.c_uint32)]
+
+
+class CrBatchTuning(ctypes.Structure):
+    _fields_ = [("tile", ctypes.c_uint32), ("spp_per_item", ctypes.c_uint32), ("blocks_per_sm", ctypes.c_uint32)]
+
+
+class CrBatchTuningResult(ctypes.Structure):
+    _fields_ = [("tuning", CrBatchTuning), ("ms", ctypes.c_float)]
+
+
 class CrayError(RuntimeError):
     """Raised for a non-zero status of the C ABI (the reference throws
     RuntimeError from CRAYSTAL_CHECK / CRAYSTAL_CUDA_CHECK)."""
@@ -111,6 +123,13 @@ SIGNATURES = [
     ("cr_mlp_train_step", ctypes.c_int, [_P, _P, _P, _U64, _P]),
     ("cr_render_cached", ctypes.c_int, [_P, ctypes.POINTER(CrIntegratorConfig), ctypes.POINTER(CrCacheConfig), _P,
                                         _U32, _U32, _P, ctypes.POINTER(CrCacheStats)]),
+    ("cr_batch_create", ctypes.c_int, [_P, _P, _U32, ctypes.POINTER(ctypes.c_void_p)]),
+    ("cr_batch_destroy", ctypes.c_int, [_P]),
+    ("cr_batch_set_tuning", ctypes.c_int, [_P, ctypes.POINTER(CrBatchTuning)]),
+    ("cr_batch_get_tuning", ctypes.c_int, [_P, ctypes.POINTER(CrBatchTuning)]),
+    ("cr_batch_render", ctypes.c_int, [_P, _P]),
+    ("cr_batch_autotune", ctypes.c_int, [_P, ctypes.POINTER(CrBatchTuning), _P, _U32,
+                                         ctypes.POINTER(ctypes.c_uint32)]),
     ("cr_kernel_launch_count", ctypes.c_uint64, []),
 ]
 

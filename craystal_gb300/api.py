@@ -395,3 +395,67 @@ class CachedPathTraceIntegrator(PathTraceIntegrator):
             rgb, wt = scene.film_read()
             cam.sensor.data[...] = rgb
             cam.sensor.weight[...] = wt
+
+
+class BatchRenderer:
+    """Many scenes in one persistent launch replayed from a CUDA graph
+    (cr_batch_*); items: one (PathTraceIntegrator, spp, first_sample) per scene."""
+
+    def __init__(self, scenes, integrators, spp, first_sample=None):
+        from ._lib import CrBatchItem
+        n = len(scenes)
+        self.scenes = list(scenes)
+        items = (CrBatchItem * n)()
+        for i in range(n):
+            items[i].config = integrators[i].device_config()
+            items[i].spp = int(spp[i])
+            items[i].first_sample = int(first_sample[i]) if first_sample is not None else 0
+        for sc in self.scenes:
+            if sc.getCamera() is None:
+                raise _lib.CrayError(_lib.CR_ERR_INVALID_ARGUMENT, "every scene needs a camera")
+        handles = (ctypes.c_void_p * n)(*[sc.handle.value for sc in self.scenes])
+        h = ctypes.c_void_p()
+        check(load().cr_batch_create(handles, items, n, ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            load().cr_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def render(self, stream: int = 0):
+        check(load().cr_batch_render(self._h, stream or None))
+
+    def set_tuning(self, tile=16, spp_per_item=4, blocks_per_sm=0):
+        from ._lib import CrBatchTuning
+        t = CrBatchTuning(tile, spp_per_item, blocks_per_sm)
+        check(load().cr_batch_set_tuning(self._h, ctypes.byref(t)))
+
+    def tuning(self) -> dict:
+        from ._lib import CrBatchTuning
+        t = CrBatchTuning()
+        check(load().cr_batch_get_tuning(self._h, ctypes.byref(t)))
+        return {"tile": t.tile, "spp_per_item": t.spp_per_item, "blocks_per_sm": t.blocks_per_sm}
+
+    def autotune(self, json_path: str = None) -> dict:
+        """Times every tuning on this batch, keeps the fastest (films are
+        cleared afterwards); optionally writes the table as JSON."""
+        from ._lib import CrBatchTuning, CrBatchTuningResult
+        best = CrBatchTuning()
+        res = (CrBatchTuningResult * 32)()
+        n = ctypes.c_uint32()
+        check(load().cr_batch_autotune(self._h, ctypes.byref(best), res, 32, ctypes.byref(n)))
+        out = {"best": {"tile": best.tile, "spp_per_item": best.spp_per_item},
+               "timings_ms": [{"tile": res[i].tuning.tile, "spp_per_item": res[i].tuning.spp_per_item,
+                               "ms": round(res[i].ms, 4)} for i in range(n.value)]}
+        if json_path:
+            import json
+            with open(json_path, "w") as f:
+                json.dump(out, f, indent=1)
+        return out

@@ -1,0 +1,314 @@
+// cr_batch.cu -- many scenes of uneven size, resolution and sample count
+// rendered by one persistent launch, replayed from a captured CUDA graph,
+// with tile size and work granularity picked by an autotuner.  (No
+// counterpart in the reference, which renders one scene per dispatch with a
+// launch and a device synchronisation per sample, Core/Integrator.cu:246-259.)
+//
+// Work is a flat list of items (scene, tile, run of sample indices), ordered
+// by scene cost, largest first.  Every block of the persistent kernel takes
+// the next item from a global counter (one atomicAdd per item; no block
+// ever waits for another), copies the item's scene descriptor to shared
+// memory and renders the tile with the same code as the per-image launch
+// (cr_tile.cuh), so each scene's film receives exactly the samples a
+// cr_render of that scene would add.
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "cr_internal.cuh"
+#include "cr_tile.cuh"
+
+namespace cr {
+namespace {
+
+struct __align__(16) BatchScene {
+    SceneView view;
+    CameraGpu cam;
+    Params p;
+    float* filmRgb;
+    float* filmW;
+    unsigned long long* rayCounter;
+    uint32_t tilesX, pad[3];
+};
+
+struct __align__(16) BatchItem {
+    uint32_t scene, tile, s0, s1;
+};
+
+template <int TW>
+__global__ void __launch_bounds__(TW* TW) kBatch(const BatchScene* __restrict__ scenes,
+                                                 const BatchItem* __restrict__ items, uint32_t nItems,
+                                                 uint32_t* __restrict__ queue) {
+    __shared__ TileSmem<TW> sm;
+    __shared__ BatchScene bs;
+    __shared__ BatchItem item;
+    const int tid = threadIdx.y * TW + threadIdx.x;
+    while (true) {
+        __syncthreads();  // everyone is done with the previous item's bs / item
+        if (tid == 0) {
+            const uint32_t i = atomicAdd(queue, 1u);
+            item = i < nItems ? items[i] : BatchItem{0xffffffffu, 0, 0, 0};
+        }
+        __syncthreads();
+        if (item.scene == 0xffffffffu) break;
+        constexpr int kWords = sizeof(BatchScene) / 16;
+        for (int k = tid; k < kWords; k += TW * TW)
+            reinterpret_cast<uint4*>(&bs)[k] = reinterpret_cast<const uint4*>(scenes + item.scene)[k];
+        __syncthreads();
+        const int tx0 = (int)(item.tile % bs.tilesX) * TW, ty0 = (int)(item.tile / bs.tilesX) * TW;
+        renderTile<TW>(bs.view, bs.cam, bs.p, tx0, ty0, item.s0, item.s1, bs.filmRgb, bs.filmW, bs.rayCounter, sm);
+    }
+}
+
+}  // namespace
+}  // namespace cr
+
+using namespace cr;
+
+struct cr_batch {
+    int device = 0;
+    std::vector<cr_scene*> scenes;
+    std::vector<cr_batch_item> items;
+    cr_batch_tuning tuning{16, 4, 0};
+    BatchScene* dScenes = nullptr;
+    BatchItem* dItems = nullptr;
+    uint32_t nItems = 0;
+    uint32_t* dQueue = nullptr;
+    cudaStream_t stream = nullptr;  // capture / launch stream when the caller passes none
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    bool built = false;
+    uint64_t replays = 0;
+};
+
+namespace {
+
+void releaseGraph(cr_batch* b) {
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+}
+
+int blocksPerSm(int tw, int* out) {
+    int per = 0;
+    if (tw == 8) CR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kBatch<8>, 64, 0));
+    else CR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kBatch<16>, 256, 0));
+    *out = std::max(per, 1);
+    return CR_OK;
+}
+
+// Descriptors (re-uploaded on every render, so that sample indices can
+// advance between replays) and the work list plus graph (rebuilt when the
+// tuning changes).
+int uploadDescriptors(cr_batch* b, cudaStream_t st) {
+    const int tw = b->tuning.tile;
+    std::vector<BatchScene> d(b->scenes.size());
+    for (size_t i = 0; i < b->scenes.size(); i++) {
+        cr_scene* s = b->scenes[i];
+        const cr_batch_item& it = b->items[i];
+        std::memset(&d[i], 0, sizeof(BatchScene));
+        d[i].view = s->view();
+        d[i].cam = s->cam;
+        Params& p = d[i].p;
+        p.maxDepth = it.config.max_depth;
+        p.rrThreshold = it.config.rr_threshold;
+        p.useMIS = it.config.use_mis ? 1u : 0u;
+        p.spp = it.spp;
+        p.first = it.first_sample + (uint32_t)(b->replays * it.spp);
+        p.sppPerBlock = b->tuning.spp_per_item;
+        p.spectral = (it.config.flags & CR_RENDER_SPECTRAL) ? 1u : 0u;
+        p.wb = whiteBalance();
+        d[i].filmRgb = s->filmRgb;
+        d[i].filmW = s->filmW;
+        d[i].rayCounter = s->rayCounter;
+        d[i].tilesX = (s->cam.width + tw - 1) / tw;
+    }
+    CR_CUDA(cudaMemcpyAsync(b->dScenes, d.data(), d.size() * sizeof(BatchScene), cudaMemcpyHostToDevice, st));
+    return CR_OK;
+}
+
+int buildWork(cr_batch* b, cudaStream_t st) {
+    releaseGraph(b);
+    if (b->dItems) cudaFree(b->dItems);
+    b->dItems = nullptr;
+    const int tw = b->tuning.tile;
+    const uint32_t run = std::max(1u, b->tuning.spp_per_item);
+    // scenes by estimated cost (pixels * spp * depth), largest first
+    std::vector<size_t> order(b->scenes.size());
+    for (size_t i = 0; i < order.size(); i++) order[i] = i;
+    auto cost = [&](size_t i) {
+        const cr_scene* s = b->scenes[i];
+        return (double)s->cam.width * s->cam.height * b->items[i].spp * b->items[i].config.max_depth;
+    };
+    std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t c) { return cost(a) > cost(c); });
+    std::vector<BatchItem> items;
+    for (size_t i : order) {
+        const cr_scene* s = b->scenes[i];
+        const uint32_t tx = (s->cam.width + tw - 1) / tw, ty = (s->cam.height + tw - 1) / tw;
+        const uint32_t spp = b->items[i].spp;
+        for (uint32_t s0 = 0; s0 < spp; s0 += run)
+            for (uint32_t t = 0; t < tx * ty; t++) items.push_back(BatchItem{(uint32_t)i, t, s0, std::min(spp, s0 + run)});
+    }
+    b->nItems = (uint32_t)items.size();
+    CR_CUDA(cudaMalloc(&b->dItems, std::max<size_t>(items.size(), 1) * sizeof(BatchItem)));
+    CR_CUDA(cudaMemcpy(b->dItems, items.data(), items.size() * sizeof(BatchItem), cudaMemcpyHostToDevice));
+    // capture: reset the queue, one persistent launch
+    int sms = 0, per = 0;
+    CR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device));
+    int rc = blocksPerSm(tw, &per);
+    if (rc) return rc;
+    const uint32_t bpsm = b->tuning.blocks_per_sm ? std::min<uint32_t>(b->tuning.blocks_per_sm, per) : per;
+    const uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)sms * bpsm, b->nItems));
+    CR_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    cudaMemsetAsync(b->dQueue, 0, sizeof(uint32_t), st);
+    if (tw == 8) kBatch<8><<<blocks, dim3(8, 8), 0, st>>>(b->dScenes, b->dItems, b->nItems, b->dQueue);
+    else kBatch<16><<<blocks, dim3(16, 16), 0, st>>>(b->dScenes, b->dItems, b->nItems, b->dQueue);
+    cudaError_t launchErr = cudaGetLastError();
+    cudaError_t e = cudaStreamEndCapture(st, &b->graph);
+    if (launchErr != cudaSuccess) return fail(CR_ERR_CUDA, "batch capture launch: %s", cudaGetErrorString(launchErr));
+    if (e != cudaSuccess) return fail(CR_ERR_CUDA, "cudaStreamEndCapture: %s", cudaGetErrorString(e));
+    CR_CUDA(cudaGraphInstantiate(&b->exec, b->graph, 0));
+    b->built = true;
+    return CR_OK;
+}
+
+int renderOnce(cr_batch* b, cudaStream_t st) {
+    if (!b->built) {
+        int rc = buildWork(b, st);
+        if (rc) return rc;
+    }
+    int rc = uploadDescriptors(b, st);
+    if (rc) return rc;
+    CR_CUDA(cudaGraphLaunch(b->exec, st));
+    countLaunch();
+    b->replays++;
+    return CR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int cr_batch_create(cr_scene* const* scenes, const cr_batch_item* items, uint32_t n, cr_batch** out) {
+    clearError();
+    if (!out || (n && (!scenes || !items))) return fail(CR_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (n == 0) return fail(CR_ERR_INVALID_ARGUMENT, "a batch needs at least one scene");
+    *out = nullptr;
+    for (uint32_t i = 0; i < n; i++) {
+        if (!scenes[i] || !scenes[i]->hasCamera)
+            return fail(CR_ERR_INVALID_ARGUMENT, "scene %u is NULL or has no camera", i);
+        if (items[i].config.max_depth > 1024) return fail(CR_ERR_INVALID_ARGUMENT, "scene %u max_depth", i);
+        if (i && scenes[i]->device != scenes[0]->device)
+            return fail(CR_ERR_INVALID_ARGUMENT, "all scenes of a batch must live on one device");
+    }
+    cr_batch* b = new cr_batch();
+    b->device = scenes[0]->device;
+    b->scenes.assign(scenes, scenes + n);
+    b->items.assign(items, items + n);
+    CR_CUDA(cudaSetDevice(b->device));
+    CR_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+    CR_CUDA(cudaMalloc(&b->dScenes, n * sizeof(BatchScene)));
+    CR_CUDA(cudaMalloc(&b->dQueue, sizeof(uint32_t)));
+    *out = b;
+    return CR_OK;
+}
+
+int cr_batch_destroy(cr_batch* b) {
+    clearError();
+    if (!b) return CR_OK;
+    cudaSetDevice(b->device);
+    releaseGraph(b);
+    if (b->dItems) cudaFree(b->dItems);
+    if (b->dScenes) cudaFree(b->dScenes);
+    if (b->dQueue) cudaFree(b->dQueue);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return CR_OK;
+}
+
+int cr_batch_set_tuning(cr_batch* b, const cr_batch_tuning* t) {
+    clearError();
+    if (!b || !t) return fail(CR_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (t->tile != 8 && t->tile != 16) return fail(CR_ERR_INVALID_ARGUMENT, "tile must be 8 or 16");
+    if (t->spp_per_item == 0) return fail(CR_ERR_INVALID_ARGUMENT, "spp_per_item must be positive");
+    b->tuning = *t;
+    b->built = false;
+    return CR_OK;
+}
+
+int cr_batch_get_tuning(const cr_batch* b, cr_batch_tuning* t) {
+    clearError();
+    if (!b || !t) return fail(CR_ERR_INVALID_ARGUMENT, "NULL argument");
+    *t = b->tuning;
+    return CR_OK;
+}
+
+int cr_batch_render(cr_batch* b, void* stream) {
+    clearError();
+    if (!b) return fail(CR_ERR_INVALID_ARGUMENT, "NULL argument");
+    CR_CUDA(cudaSetDevice(b->device));
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : b->stream;
+    int rc = renderOnce(b, st);
+    if (rc) return rc;
+    if (!stream) CR_CUDA(cudaStreamSynchronize(st));
+    return CR_OK;
+}
+
+int cr_batch_autotune(cr_batch* b, cr_batch_tuning* best, cr_batch_tuning_result* results, uint32_t max_results,
+                      uint32_t* n_results) {
+    clearError();
+    if (!b) return fail(CR_ERR_INVALID_ARGUMENT, "NULL argument");
+    CR_CUDA(cudaSetDevice(b->device));
+    const uint32_t tiles[] = {8, 16};
+    const uint32_t runs[] = {1, 2, 4, 8, 16};
+    cudaEvent_t e0, e1;
+    CR_CUDA(cudaEventCreate(&e0));
+    CR_CUDA(cudaEventCreate(&e1));
+    float bestMs = INFINITY;
+    cr_batch_tuning bestT = b->tuning;
+    uint32_t k = 0;
+    for (uint32_t tw : tiles) {
+        for (uint32_t r : runs) {
+            cr_batch_tuning t{tw, r, 0};
+            b->tuning = t;
+            b->built = false;
+            int rc = buildWork(b, b->stream);
+            if (rc) return rc;
+            rc = renderOnce(b, b->stream);  // warm-up replay
+            if (rc) return rc;
+            CR_CUDA(cudaEventRecord(e0, b->stream));
+            rc = renderOnce(b, b->stream);
+            if (rc) return rc;
+            CR_CUDA(cudaEventRecord(e1, b->stream));
+            CR_CUDA(cudaEventSynchronize(e1));
+            float ms = 0;
+            CR_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            if (results && k < max_results) results[k] = cr_batch_tuning_result{t, ms};
+            k++;
+            if (ms < bestMs) {
+                bestMs = ms;
+                bestT = t;
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (n_results) *n_results = k;
+    b->tuning = bestT;
+    b->built = false;
+    b->replays = 0;
+    if (best) *best = bestT;
+    // the tuning renders added samples: clear the films
+    for (cr_scene* s : b->scenes) {
+        const size_t px = (size_t)s->cam.width * s->cam.height;
+        CR_CUDA(cudaMemsetAsync(s->filmRgb, 0, px * 3 * sizeof(float), b->stream));
+        CR_CUDA(cudaMemsetAsync(s->filmW, 0, px * sizeof(float), b->stream));
+        CR_CUDA(cudaMemsetAsync(s->rayCounter, 0, sizeof(unsigned long long), b->stream));
+    }
+    CR_CUDA(cudaStreamSynchronize(b->stream));
+    return CR_OK;
+}
+
+}  // extern "C"

@@ -6,8 +6,7 @@
 // One thread owns one pixel and loops over a run of sample indices; the
 // launch covers (16 x 16 pixel tiles) x (runs of samples), so that small
 // images still fill the GPU.  Film splats go to an 18 x 18 tile in shared
-// memory (the 16 x 16 pixels plus the one-pixel apron the triangle filter
-// of radius 1 reaches) and are added to the global film once per block,
+// memory (cr_tile.cuh) and are added to the global film once per block,
 // instead of 16 global atomics per sample in the reference.
 
 #include "cr_internal.cuh"
@@ -15,82 +14,20 @@
 #include "cr_shading.cuh"
 #include "cr_traverse.cuh"
 #include "cr_path.cuh"
+#include "cr_tile.cuh"
 
 namespace cr {
 namespace {
 
 constexpr int kTileW = 16;
-constexpr int kApron = 18;
 
 __global__ void __launch_bounds__(kTileW* kTileW) kRender(const SceneView sc, const CameraGpu cam, const Params p,
                                                           float* __restrict__ filmRgb, float* __restrict__ filmW,
                                                           unsigned long long* __restrict__ rayCounter) {
-    __shared__ float tile[kApron * kApron * 4];
-    __shared__ uint32_t warpRays[kTileW * kTileW / 32];
-    const int tid = threadIdx.y * kTileW + threadIdx.x;
-    for (int i = tid; i < kApron * kApron * 4; i += kTileW * kTileW) tile[i] = 0.0f;
-    __syncthreads();
-    const int tx0 = blockIdx.x * kTileW, ty0 = blockIdx.y * kTileW;
-    const uint32_t x = tx0 + threadIdx.x, y = ty0 + threadIdx.y;
-    PathCtx c{sc, 0u, SpectralPath{}};
-    if (x < cam.width && y < cam.height) {
-        const uint32_t s0 = blockIdx.z * p.sppPerBlock;
-        const uint32_t s1 = min(p.spp, s0 + p.sppPerBlock);
-        for (uint32_t s = s0; s < s1; s++) {
-            float2 pix;
-            NoHooks hk;
-            const Spec L = pathSpecToRgb(c.spec, tracePath(c, cam, p, x, y, p.first + s, pix, hk), p.wb);
-            // SensorData::addSample, Core/Sensor.cu:19-43
-            if (isnan(L.r) || isnan(L.g) || isnan(L.b) || isinf(L.r) || isinf(L.g) || isinf(L.b)) continue;
-            int xa = (int)floorf(pix.x - 1.0f), ya = (int)floorf(pix.y - 1.0f);
-            int xb = (int)ceilf(pix.x + 1.0f), yb = (int)ceilf(pix.y + 1.0f);
-            xa = max(xa, 0);
-            ya = max(ya, 0);
-            xb = min(xb, (int)cam.width - 1);
-            yb = min(yb, (int)cam.height - 1);
-            for (int yy = ya; yy <= yb; yy++) {
-                for (int xx = xa; xx <= xb; xx++) {
-                    const float dx = pix.x - ((float)xx + 0.5f), dy = pix.y - ((float)yy + 0.5f);
-                    const float w = smax(0.0f, 1.0f - fabsf(dx)) * smax(0.0f, 1.0f - fabsf(dy));
-                    if (w == 0.0f) continue;  // adding +0 leaves the film unchanged
-                    const int lx = xx - tx0 + 1, ly = yy - ty0 + 1;
-                    if (lx >= 0 && lx < kApron && ly >= 0 && ly < kApron) {
-                        float* cell = tile + (ly * kApron + lx) * 4;
-                        atomicAdd(cell + 0, L.r * w);
-                        atomicAdd(cell + 1, L.g * w);
-                        atomicAdd(cell + 2, L.b * w);
-                        atomicAdd(cell + 3, w);
-                    } else {
-                        const size_t pi = (size_t)yy * cam.width + xx;
-                        atomicAdd(filmRgb + 3 * pi + 0, L.r * w);
-                        atomicAdd(filmRgb + 3 * pi + 1, L.g * w);
-                        atomicAdd(filmRgb + 3 * pi + 2, L.b * w);
-                        atomicAdd(filmW + pi, w);
-                    }
-                }
-            }
-        }
-    }
-    uint32_t r = c.rays;
-    for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
-    if ((tid & 31) == 0) warpRays[tid >> 5] = r;
-    __syncthreads();
-    if (tid == 0) {
-        unsigned long long s = 0;
-        for (int k = 0; k < kTileW * kTileW / 32; k++) s += warpRays[k];
-        atomicAdd(rayCounter, s);
-    }
-    for (int i = tid; i < kApron * kApron; i += kTileW * kTileW) {
-        const float* cell = tile + i * 4;
-        if (cell[3] == 0.0f && cell[0] == 0.0f && cell[1] == 0.0f && cell[2] == 0.0f) continue;
-        const int gx = tx0 - 1 + i % kApron, gy = ty0 - 1 + i / kApron;
-        if (gx < 0 || gy < 0 || gx >= (int)cam.width || gy >= (int)cam.height) continue;
-        const size_t pi = (size_t)gy * cam.width + gx;
-        atomicAdd(filmRgb + 3 * pi + 0, cell[0]);
-        atomicAdd(filmRgb + 3 * pi + 1, cell[1]);
-        atomicAdd(filmRgb + 3 * pi + 2, cell[2]);
-        atomicAdd(filmW + pi, cell[3]);
-    }
+    __shared__ TileSmem<kTileW> sm;
+    const uint32_t s0 = blockIdx.z * p.sppPerBlock;
+    const uint32_t s1 = min(p.spp, s0 + p.sppPerBlock);
+    renderTile<kTileW>(sc, cam, p, blockIdx.x * kTileW, blockIdx.y * kTileW, s0, s1, filmRgb, filmW, rayCounter, sm);
 }
 
 __global__ void kResolve(const float* __restrict__ rgb, const float* __restrict__ w, size_t n, float* __restrict__ out) {

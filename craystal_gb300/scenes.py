@@ -265,3 +265,107 @@ def cache_scene(seed: int = 0, width: int = 1920, height: int = 1080, level: int
     env = (0.5, 0.5, 0.5)
     spheres = [((2.5, 6.0, 3.0), 1.0, (40.0, 38.0, 34.0))]
     return data, cam, env, spheres
+
+
+# ---------------------------------------------------------------------------
+# batched workload: random-box clutter scenes of uneven size
+# ---------------------------------------------------------------------------
+_FACE_AXES = [(0, 1, 2, 1.0), (0, 1, 2, -1.0), (1, 2, 0, 1.0), (1, 2, 0, -1.0), (2, 0, 1, 1.0), (2, 0, 1, -1.0)]
+
+
+def _boxes(centers, half, angles):
+    """24 vertices (4 per face, flat normals) and 12 triangles per box."""
+    nb = len(centers)
+    pos = np.empty((nb, 24, 3))
+    nrm = np.empty((nb, 24, 3))
+    quad = np.array([[-1, -1], [1, -1], [1, 1], [-1, 1]], np.float64)
+    for f, (u, v, w, sgn) in enumerate(_FACE_AXES):
+        local = np.zeros((4, 3))
+        local[:, u] = quad[:, 0]
+        local[:, v] = quad[:, 1] * sgn
+        local[:, w] = sgn
+        n = np.zeros(3)
+        n[w] = sgn
+        pos[:, 4 * f:4 * f + 4] = local[None] * half[:, None, :]
+        nrm[:, 4 * f:4 * f + 4] = n
+    ca, sa = np.cos(angles)[:, None], np.sin(angles)[:, None]
+    x, z = pos[..., 0].copy(), pos[..., 2].copy()
+    pos[..., 0], pos[..., 2] = ca * x + sa * z, -sa * x + ca * z
+    nx, nz = nrm[..., 0].copy(), nrm[..., 2].copy()
+    nrm[..., 0], nrm[..., 2] = ca * nx + sa * nz, -sa * nx + ca * nz
+    pos += centers[:, None, :]
+    tri = np.array([[0, 1, 2], [0, 2, 3]])
+    idx = (np.arange(6)[:, None, None] * 4 + tri[None]).reshape(-1, 3)  # 12 x 3 per box
+    idx = (np.arange(nb)[:, None, None] * 24 + idx[None]).reshape(-1)
+    return pos.reshape(-1, 3), nrm.reshape(-1, 3), idx
+
+
+def box_clutter(seed: int = 0, n_tris: int = 100000, width: int = 256, height: int = 256, n_materials: int = 6):
+    """Returns (SceneData, Camera): about n_tris / 12 boxes (scale log-uniform
+    0.05 - 0.6, rotated about y) on a ground quad, lit by a 3 x 3 emissive
+    ceiling quad; materials drawn from Lambertian / Phong / Principled."""
+    rng = np.random.default_rng(seed)
+    nb = max(1, n_tris // 12)
+    centers = np.stack([rng.uniform(-5, 5, nb), np.zeros(nb), rng.uniform(-5, 5, nb)], 1)
+    half = np.exp(rng.uniform(np.log(0.05), np.log(0.6), (nb, 1))) * rng.uniform(0.6, 1.4, (nb, 3))
+    centers[:, 1] = half[:, 1] + rng.uniform(0, 2.5, nb) * (rng.random(nb) < 0.3)
+    pos, nrm, idx = _boxes(centers, half, rng.uniform(0, np.pi / 2, nb))
+    mat_of_box = rng.integers(0, n_materials, nb)
+    meshes, mats = [], []
+    for m in range(n_materials):
+        sel = np.flatnonzero(mat_of_box == m)
+        if len(sel) == 0:
+            continue
+        vsel = (sel[:, None] * 24 + np.arange(24)[None]).reshape(-1)
+        remap = np.full(len(pos), -1, np.int64)
+        remap[vsel] = np.arange(len(vsel))
+        isel = (sel[:, None] * 36 + np.arange(36)[None]).reshape(-1)
+        kind = m % 3
+        kd = tuple(float(c) for c in rng.uniform(0.1, 0.9, 3))
+        if kind == 0:
+            md = MaterialData(diffuseRefl=kd, type=MaterialType.FullDiffuse)
+        elif kind == 1:
+            md = MaterialData(diffuseRefl=kd, specularRefl=(0.15, 0.15, 0.15), shininess=float(rng.uniform(8, 64)),
+                              type=MaterialType.Phong)
+        else:
+            md = MaterialData(diffuseRefl=kd, specularRefl=(0.5, 0.5, 0.5) if rng.random() < 0.3 else (0.0, 0.0, 0.0),
+                              shininess=float(rng.uniform(1, 100)), type=MaterialType.Principled)
+        mats.append(md)
+        meshes.append(MeshData(position=pos[vsel].astype(np.float32), normal=nrm[vsel].astype(np.float32),
+                               index=remap[idx[isel]].astype(np.uint32), materialID=len(mats) - 1))
+    g = 8.0
+    mats.append(MaterialData(diffuseRefl=(0.5, 0.5, 0.5), type=MaterialType.FullDiffuse))
+    meshes.append(MeshData(position=np.array([[-g, 0, -g], [g, 0, -g], [g, 0, g], [-g, 0, g]], np.float32),
+                           normal=np.tile(np.float32([0, 1, 0]), (4, 1)), index=np.array([0, 2, 1, 0, 3, 2], np.uint32),
+                           materialID=len(mats) - 1))
+    y = 6.0
+    mats.append(MaterialData(emission=(8.0, 8.0, 8.0), type=MaterialType.FullDiffuse))
+    meshes.append(MeshData(position=np.array([[-1.5, y, -1.5], [1.5, y, -1.5], [1.5, y, 1.5], [-1.5, y, 1.5]],
+                                             np.float32),
+                           normal=np.tile(np.float32([0, -1, 0]), (4, 1)), index=np.array([0, 1, 2, 0, 2, 3], np.uint32),
+                           materialID=len(mats) - 1))
+    for m in mats:
+        m.finalize()
+    n_total = sum(len(m.index) // 3 for m in meshes)
+    data = SceneData(meshes=meshes, materials=mats, emissiveIndex=[n_total - 2, n_total - 1])
+    cam = Camera()
+    cam.setWorldPosition((0.0, 4.0, 12.0))
+    cam.setTarget((0.0, 0.5, 0.0))
+    cam.setUp((0.0, 1.0, 0.0))
+    cam.setFovY(50.0)
+    cam.setSensor(Sensor((width, height)))
+    return data, cam
+
+
+def batch_workload(n_scenes: int = 64, seed: int = 0):
+    """Per-scene parameters of the batched workload: triangles log-uniform in
+    [10k, 500k], square resolution from {128, 256, 512, 1024}, spp
+    log-uniform in [4, 256], max depth uniform in {8..16}; scene i uses seed i."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n_scenes):
+        out.append({"seed": i, "tris": int(np.exp(rng.uniform(np.log(10e3), np.log(500e3)))),
+                    "res": int(rng.choice([128, 256, 512, 1024])),
+                    "spp": int(round(np.exp(rng.uniform(np.log(4), np.log(256))))),
+                    "depth": int(rng.integers(8, 17))})
+    return out

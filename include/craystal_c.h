@@ -334,6 +334,42 @@ int cr_render_cached(cr_scene* scene, const cr_integrator_config* cfg,
                      const cr_cache_config* cache, cr_mlp* mlp, uint32_t frames,
                      uint32_t first_sample, void* stream, cr_cache_stats* stats);
 
+/* ---- batched rendering (no counterpart in the reference) ----
+ * Many scenes (each with its camera and film set) rendered by one
+ * persistent launch that replays a captured CUDA graph: work items (scene,
+ * pixel tile, run of spp_per_item sample indices) are taken from one queue,
+ * largest scenes first.  Each scene's film receives exactly the samples
+ * cr_render(scene, config, spp, first_sample) would add; the k-th
+ * cr_batch_render of a batch uses sample indices first_sample + k*spp.
+ * cr_batch_autotune times every (tile 8|16) x (spp_per_item 1,2,4,8,16) on the
+ * batch itself, keeps the fastest and clears the films it rendered into.
+ * The scenes must outlive the batch and keep their camera size. */
+typedef struct cr_batch cr_batch;
+typedef struct {
+    cr_integrator_config config;
+    uint32_t spp;
+    uint32_t first_sample;
+} cr_batch_item;
+typedef struct {
+    uint32_t tile;          /* 8 or 16 pixels square */
+    uint32_t spp_per_item;  /* sample indices per work item */
+    uint32_t blocks_per_sm; /* 0 = as many as fit */
+} cr_batch_tuning;
+typedef struct {
+    cr_batch_tuning tuning;
+    float ms;
+} cr_batch_tuning_result;
+int cr_batch_create(cr_scene* const* scenes, const cr_batch_item* items,
+                    uint32_t n, cr_batch** out);
+int cr_batch_destroy(cr_batch* batch);
+int cr_batch_set_tuning(cr_batch* batch, const cr_batch_tuning* tuning);
+int cr_batch_get_tuning(const cr_batch* batch, cr_batch_tuning* tuning);
+/* stream NULL: the batch's own stream, waited for before returning */
+int cr_batch_render(cr_batch* batch, void* stream);
+int cr_batch_autotune(cr_batch* batch, cr_batch_tuning* best,
+                      cr_batch_tuning_result* results, uint32_t max_results,
+                      uint32_t* n_results);
+
 /* Number of kernel launches this library issued since the process started
  * (all entry points); for launch accounting in benchmarks. */
 uint64_t cr_kernel_launch_count(void);
