@@ -1,0 +1,36 @@
+"""Builds the restated reference traversal (baseline/restated/*.cu) into
+baseline/restated/_build/librefkernel.so: default nvcc optimisation flags
+(FMA contraction on, as the reference's build has), relocatable device code
+with the AABB, triangle and BVH functions in separate translation units
+(the reference's CUDA_SEPARABLE_COMPILATION), sm_103a.  A measurement
+comparator for bench.py; not part of the product."""
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+OUT = os.path.join(HERE, "_build")
+LIB = os.path.join(OUT, "librefkernel.so")
+SRC = ["ref_aabb.cu", "ref_triangle.cu", "ref_bvh.cu"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def build(force=False):
+    deps = [os.path.join(HERE, f) for f in SRC + ["ref_common.cuh", "build.py"]]
+    if not force and os.path.exists(LIB) and all(os.path.getmtime(d) <= os.path.getmtime(LIB) for d in deps):
+        return LIB
+    os.makedirs(OUT, exist_ok=True)
+    objs = []
+    for f in SRC:
+        o = os.path.join(OUT, f.replace(".cu", ".o"))
+        subprocess.run(["nvcc", *ARCH, "-rdc=true", "-Xcompiler", "-fPIC", "-c", os.path.join(HERE, f), "-o", o],
+                       check=True)
+        objs.append(o)
+    dlink = os.path.join(OUT, "dlink.o")
+    subprocess.run(["nvcc", *ARCH, "-dlink", "-Xcompiler", "-fPIC", *objs, "-o", dlink], check=True)
+    subprocess.run(["nvcc", *ARCH, "-shared", *objs, dlink, "-o", LIB], check=True)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build("--force" in sys.argv))

@@ -292,6 +292,31 @@ def batch_extra(torch, n_scenes=64):
             "speedup_vs_per_scene": round(t_seq / t_batch, 3), "tuning": tune["best"]}
 
 
+def restated_reference_extra(torch, sc, flat, d_rays, n, d_hits_ours, reps=3):
+    """The reference's own traversal restated in CUDA (baseline/restated:
+    36-byte variant nodes, per-box division, 64-entry local stack, indexed
+    vertex fetches, default FMA contraction) on the same rays and the same
+    reference-layout tree: its Mrays/s and how many of its hits equal ours."""
+    from baseline.restated import RestatedTraversal
+    ref = RestatedTraversal(sc, flat)
+    out = torch.empty(n * 16, dtype=torch.uint8, device=d_rays.device)
+    s = torch.cuda.current_stream()
+    ref.trace_closest_device(d_rays.data_ptr(), n, out.data_ptr(), s.cuda_stream)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(reps):
+        ref.trace_closest_device(d_rays.data_ptr(), n, out.data_ptr(), s.cuda_stream)
+    e1.record(s)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    a = out.view(torch.int32).view(-1, 4).cpu().numpy()
+    b = d_hits_ours.view(torch.int32).view(-1, 4).cpu().numpy()
+    return {"kernel": "restated BVHData::intersect, one thread per ray", "ms_per_launch": round(ms, 3),
+            "Mrays_s": round(n / ms / 1e3, 2), "prim_equal_fraction": round(float((a[:, 0] == b[:, 0]).mean()), 6),
+            "bit_equal_fraction": round(float((a == b).all(axis=1).mean()), 6)}
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -371,9 +396,11 @@ def run_ours(args):
              "host_path_matches_device_path": same,
              "hit_fraction": round(float((hits_dev["prim"] != cg.CR_MISS).mean()), 4)}
     if not args.skip_extra:
+        extra["restated_reference_kernel"] = restated_reference_extra(torch, sc, flatten_scene(data), d_rays, N_RAYS,
+                                                                      d_hits)
         extra["path_tracer"] = cornell_extra(torch)
-        extra["radiance_cache_equal_time"] = cache_extra(torch)
-        extra["batched_scenes"] = batch_extra(torch)
+        extra["radiance_cache_equal_time"] = cache_extra(torch, args.cache_res)
+        extra["batched_scenes"] = batch_extra(torch, args.batch_scenes)
 
     out = {"metric": METRIC, "value": round(value, 2), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
@@ -409,6 +436,20 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_only(args):
+    import torch
+    torch.cuda.set_device(0)
+    import craystal_gb300 as cg
+    cg.load().cr_set_device(0)
+    if args.only == "path_tracer":
+        r = cornell_extra(torch)
+    elif args.only == "radiance_cache":
+        r = cache_extra(torch, args.cache_res)
+    else:
+        r = batch_extra(torch, args.batch_scenes)
+    print(json.dumps({args.only: r}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -419,11 +460,17 @@ def main():
     ap.add_argument("--skip-extra", action="store_true", help="omit the path-tracer figures")
     ap.add_argument("--rays", type=int, default=N_RAYS, help="rays per step (profiling a smaller case)")
     ap.add_argument("--tris", type=int, default=N_TRIS, help="triangles (profiling a smaller case)")
+    ap.add_argument("--only", choices=["path_tracer", "radiance_cache", "batched_scenes"],
+                    help="run one secondary workload alone and print its figures (profiling)")
+    ap.add_argument("--cache-res", type=int, default=512, help="radiance-cache workload resolution")
+    ap.add_argument("--batch-scenes", type=int, default=64, help="scenes in the batched workload")
     args = ap.parse_args()
     globals()["N_RAYS"], globals()["N_TRIS"] = args.rays, args.tris
     if args.warmup < 3:
         args.warmup = 3
-    if args.impl == "reference":
+    if args.only:
+        run_only(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)
