@@ -19,6 +19,7 @@ CR_ERR_DEVICE = 4
 CR_ERR_UNSUPPORTED = 5
 CR_MISS = 0xFFFFFFFF
 CR_NOALLOC_MAX_RAYS = 65536
+CR_NO_TEXTURE = 0xFFFFFFFF
 
 RAY_DTYPE = np.dtype([("o", "<f4", 3), ("tmin", "<f4"), ("d", "<f4", 3), ("tmax", "<f4")])
 HIT_DTYPE = np.dtype([("prim", "<u4"), ("t", "<f4"), ("u", "<f4"), ("v", "<f4")])
@@ -33,6 +34,31 @@ BVH_NODE_DTYPE = np.dtype([("bmin", "<f4", 3), ("bmax", "<f4", 3), ("is_leaf", "
 class CrCamera(ctypes.Structure):
     _fields_ = [("pos", ctypes.c_float * 3), ("target", ctypes.c_float * 3), ("up", ctypes.c_float * 3),
                 ("fov_y", ctypes.c_float), ("width", ctypes.c_uint32), ("height", ctypes.c_uint32)]
+
+
+class CrTexture(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("texels", ctypes.POINTER(ctypes.c_float))]
+
+
+class CrMeshDescC(ctypes.Structure):
+    _fields_ = [("index_offset", ctypes.c_uint32), ("index_count", ctypes.c_uint32),
+                ("vertex_offset", ctypes.c_uint32), ("material_id", ctypes.c_uint32)]
+
+
+class CrImportView(ctypes.Structure):
+    _fields_ = [("pos", ctypes.POINTER(ctypes.c_float)), ("nrm", ctypes.POINTER(ctypes.c_float)),
+                ("uv", ctypes.POINTER(ctypes.c_float)), ("n_vertices", ctypes.c_uint64),
+                ("idx", ctypes.POINTER(ctypes.c_uint32)), ("n_tris", ctypes.c_uint64),
+                ("meshes", ctypes.c_void_p), ("n_meshes", ctypes.c_uint32),
+                ("mats", ctypes.c_void_p), ("material_texture", ctypes.POINTER(ctypes.c_uint32)),
+                ("n_mats", ctypes.c_uint32), ("emissive", ctypes.POINTER(ctypes.c_uint32)),
+                ("n_emissive", ctypes.c_uint32), ("textures", ctypes.POINTER(CrTexture)),
+                ("n_textures", ctypes.c_uint32), ("camera", CrCamera)]
+
+
+class CrImage(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("channels", ctypes.c_uint32),
+                ("pixels", ctypes.POINTER(ctypes.c_float))]
 
 
 class CrIntegratorConfig(ctypes.Structure):
@@ -100,6 +126,8 @@ SIGNATURES = [
     ("cr_scene_set_camera", ctypes.c_int, [_P, ctypes.POINTER(CrCamera)]),
     ("cr_scene_set_environment", ctypes.c_int, [_P, _P]),
     ("cr_scene_set_sphere_lights", ctypes.c_int, [_P, _P, _U32]),
+    ("cr_scene_set_diffuse_textures", ctypes.c_int, [_P, ctypes.POINTER(CrTexture), _U32, _P, _U32]),
+    ("cr_texture_sample", ctypes.c_int, [_P, _U32, _P, _U64, _P]),
     ("cr_film_clear", ctypes.c_int, [_P]),
     ("cr_film_read", ctypes.c_int, [_P, _P, _P]),
     ("cr_film_resolve", ctypes.c_int, [_P, _P]),
@@ -131,6 +159,15 @@ SIGNATURES = [
     ("cr_batch_autotune", ctypes.c_int, [_P, ctypes.POINTER(CrBatchTuning), _P, _U32,
                                          ctypes.POINTER(ctypes.c_uint32)]),
     ("cr_kernel_launch_count", ctypes.c_uint64, []),
+    ("cr_import_xml", ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p)]),
+    ("cr_import_get", ctypes.c_int, [_P, ctypes.POINTER(CrImportView)]),
+    ("cr_import_material_name", ctypes.c_char_p, [_P, _U32]),
+    ("cr_import_create_scene", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_void_p)]),
+    ("cr_import_destroy", ctypes.c_int, [_P]),
+    ("cr_image_load", ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(CrImage)]),
+    ("cr_image_free", ctypes.c_int, [ctypes.POINTER(CrImage)]),
+    ("cr_image_write_exr", ctypes.c_int, [ctypes.c_char_p, _U32, _U32, _U32, _P]),
+    ("cr_image_write_png", ctypes.c_int, [ctypes.c_char_p, _U32, _U32, _U32, _P, ctypes.c_int]),
 ]
 
 _lib = None

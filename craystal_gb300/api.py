@@ -29,6 +29,7 @@ class MaterialFlags(enum.IntFlag):
     """Core/Material.h:26-30."""
     IsEmissive = 1
     IsDiffuse = 2
+    hasDiffuseTexture = 4
 
 
 @dataclass
@@ -40,6 +41,8 @@ class MaterialData:
     shininess: float = 0.0
     type: MaterialType = MaterialType.FullDiffuse
     flags: int = 0
+    diffuseHandle: int = 0  # index into SceneData.textureImages when hasDiffuseTexture
+    name: str = ""          # the material's name in its source file (imported scenes)
 
     def finalize(self):
         """MaterialData::finalize, Core/Material.h:57-65."""
@@ -50,6 +53,9 @@ class MaterialData:
 
     def isEmissive(self) -> bool:
         return bool(self.flags & MaterialFlags.IsEmissive)
+
+    def hasDiffuseTexture(self) -> bool:
+        return bool(self.flags & MaterialFlags.hasDiffuseTexture)
 
 
 @dataclass
@@ -64,10 +70,26 @@ class MeshData:
 
 @dataclass
 class SceneData:
-    """Scene/Scene.h:40-47 (spheres and textures are not part of this path)."""
+    """Scene/Scene.h:40-47.  textureImages: images as HxWxC float arrays
+    (C = 1..4, row 0 first, as Image holds them after loading); spheres are
+    set on the Scene (Scene.set_sphere_lights)."""
     meshes: List[MeshData] = field(default_factory=list)
     materials: List[MaterialData] = field(default_factory=list)
     emissiveIndex: List[int] = field(default_factory=list)
+    textureImages: List[np.ndarray] = field(default_factory=list)
+
+
+def texture_texels(image) -> np.ndarray:
+    """Texture(const Image&), Core/Texture.cu:45-60: row-major RGBA float4
+    texels, channels beyond the image's left at 0."""
+    a = np.asarray(image, np.float32)
+    if a.ndim == 2:
+        a = a[..., None]
+    if a.ndim != 3 or not 1 <= a.shape[2] <= 4 or a.shape[0] == 0 or a.shape[1] == 0:
+        raise ValueError(f"texture image of shape {a.shape}")
+    out = np.zeros((a.shape[0], a.shape[1], 4), np.float32)
+    out[..., : a.shape[2]] = a
+    return out
 
 
 def flatten_scene(data: SceneData):
@@ -91,11 +113,18 @@ def flatten_scene(data: SceneData):
         ni += len(i)
     cat = lambda xs, shape, dt: np.concatenate(xs) if xs else np.zeros(shape, dt)
     mats = np.zeros(len(data.materials), MATERIAL_DTYPE)
+    mat_tex = np.full(len(data.materials), _lib.CR_NO_TEXTURE, np.uint32)
     for k, md in enumerate(data.materials):
-        mats[k] = (md.diffuseRefl, md.specularRefl, md.emission, md.shininess, int(md.type), md.flags)
+        mats[k] = (md.diffuseRefl, md.specularRefl, md.emission, md.shininess, int(md.type),
+                   md.flags & int(MaterialFlags.IsEmissive | MaterialFlags.IsDiffuse))
+        if md.flags & MaterialFlags.hasDiffuseTexture:
+            if not 0 <= md.diffuseHandle < len(data.textureImages):
+                raise ValueError(f"material {k}: texture {md.diffuseHandle} of {len(data.textureImages)}")
+            mat_tex[k] = md.diffuseHandle
     return dict(pos=cat(pos, (0, 3), np.float32), nrm=cat(nrm, (0, 3), np.float32), uv=cat(uv, (0, 2), np.float32),
                 idx=cat(idx, (0,), np.uint32), meshes=descs, mats=mats,
-                emissive=np.asarray(data.emissiveIndex, np.uint32))
+                emissive=np.asarray(data.emissiveIndex, np.uint32),
+                textures=[texture_texels(t) for t in data.textureImages], mat_tex=mat_tex)
 
 
 class Sensor:
@@ -179,6 +208,26 @@ class Scene:
                                   ptr(f["emissive"]), len(f["emissive"]), ctypes.byref(h)))
         self._h = h
         self._camera: Optional[Camera] = None
+        if f["textures"]:
+            self.set_diffuse_textures(f["textures"], f["mat_tex"])
+
+    def set_diffuse_textures(self, textures, material_texture):
+        """Uploads RGBA texel arrays (HxWx4) and the texture of each material
+        (CR_NO_TEXTURE for none)."""
+        keep = [np.ascontiguousarray(t, np.float32) for t in textures]
+        descs = (_lib.CrTexture * max(1, len(keep)))()
+        for i, t in enumerate(keep):
+            descs[i].width, descs[i].height = t.shape[1], t.shape[0]
+            descs[i].texels = t.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+        mt = np.ascontiguousarray(material_texture, np.uint32)
+        check(load().cr_scene_set_diffuse_textures(self._h, descs, len(keep), ptr(mt), len(mt)))
+
+    def texture_sample(self, texture: int, uv: np.ndarray) -> np.ndarray:
+        """TextureView::sample on the device at n texture coordinates -> n x 4."""
+        uv = np.ascontiguousarray(uv, np.float32).reshape(-1, 2)
+        out = np.empty((len(uv), 4), np.float32)
+        check(load().cr_texture_sample(self._h, texture, ptr(uv), len(uv), ptr(out)))
+        return out
 
     def close(self):
         if getattr(self, "_h", None) and self._h.value:
@@ -459,3 +508,129 @@ class BatchRenderer:
             with open(json_path, "w") as f:
                 json.dump(out, f, indent=1)
         return out
+
+
+class Image:
+    """Utils/Image.h: an image of float pixels, held as an HxWxC array (the
+    reference keeps one plane per channel; the pixel values are the same)."""
+
+    def __init__(self, width: int = 0, height: int = 0, channels: int = 3, data: Optional[np.ndarray] = None):
+        if data is None:
+            data = np.zeros((int(height), int(width), int(channels)), np.float32)
+        data = np.asarray(data, np.float32)
+        if data.ndim == 2:
+            data = data[..., None]
+        self.data = np.ascontiguousarray(data)
+
+    def getWidth(self) -> int:
+        return self.data.shape[1]
+
+    def getHeight(self) -> int:
+        return self.data.shape[0]
+
+    def getChannels(self) -> int:
+        return self.data.shape[2]
+
+    def getPixel(self, x: int, y: int, c: int) -> float:
+        return float(self.data[y, x, c])
+
+    def setPixel(self, x: int, y: int, c: int, value: float):
+        self.data[y, x, c] = value
+
+    def writeEXR(self, path: str):
+        """Image::writeEXR, Utils/Image.cpp:49-106."""
+        check(load().cr_image_write_exr(path.encode(), self.getWidth(), self.getHeight(), self.getChannels(),
+                                        ptr(self.data)))
+
+    def writePNG(self, path: str, gammaCorrect: bool):
+        """Image::writePNG, Utils/Image.cpp:182-217."""
+        check(load().cr_image_write_png(path.encode(), self.getWidth(), self.getHeight(), self.getChannels(),
+                                        ptr(self.data), 1 if gammaCorrect else 0))
+
+    @staticmethod
+    def load(path: str, toLinear: bool = True) -> "Image":
+        """Image::load, Utils/Image.cpp:262-270."""
+        img = _lib.CrImage()
+        check(load().cr_image_load(path.encode(), 1 if toLinear else 0, ctypes.byref(img)))
+        try:
+            n = img.width * img.height * img.channels
+            arr = np.ctypeslib.as_array(img.pixels, shape=(n,)).copy() if n else np.zeros(0, np.float32)
+        finally:
+            load().cr_image_free(ctypes.byref(img))
+        return Image(data=arr.reshape(img.height, img.width, img.channels))
+
+
+def sensor_image(sensor: Sensor) -> Image:
+    """Sensor::createImage as an Image (rgb / weight)."""
+    return Image(data=np.nan_to_num(sensor.createImage()).astype(np.float32))
+
+
+class Importer:
+    """Utils/Importer.h: an XML file (camera, emissive materials) beside an
+    OBJ/MTL file of the same name."""
+
+    def load(self, path: str):
+        """The imported SceneData and Camera (host arrays, nothing uploaded)."""
+        lib = load()
+        h = ctypes.c_void_p()
+        check(lib.cr_import_xml(str(path).encode(), ctypes.byref(h)))
+        try:
+            v = _lib.CrImportView()
+            check(lib.cr_import_get(h, ctypes.byref(v)))
+            nv, nt = v.n_vertices, v.n_tris
+
+            def arr(p, n, dt):
+                return np.ctypeslib.as_array(p, shape=(n,)).astype(dt, copy=True) if n else np.zeros(0, dt)
+
+            pos = arr(v.pos, 3 * nv, np.float32).reshape(-1, 3)
+            nrm = arr(v.nrm, 3 * nv, np.float32).reshape(-1, 3)
+            uv = arr(v.uv, 2 * nv, np.float32).reshape(-1, 2)
+            idx = arr(v.idx, 3 * nt, np.uint32)
+            descs = (np.frombuffer(ctypes.string_at(v.meshes, v.n_meshes * MESH_DTYPE.itemsize), MESH_DTYPE).copy()
+                     if v.n_meshes else np.zeros(0, MESH_DTYPE))
+            mats = (np.frombuffer(ctypes.string_at(v.mats, v.n_mats * MATERIAL_DTYPE.itemsize), MATERIAL_DTYPE).copy()
+                    if v.n_mats else np.zeros(0, MATERIAL_DTYPE))
+            mat_tex = arr(v.material_texture, v.n_mats, np.uint32)
+            textures = []
+            for t in range(v.n_textures):
+                tx = v.textures[t]
+                textures.append(np.ctypeslib.as_array(tx.texels, shape=(tx.height * tx.width * 4,))
+                                .astype(np.float32, copy=True).reshape(tx.height, tx.width, 4))
+            data = SceneData()
+            for k, d in enumerate(descs):
+                vo = int(d["vertex_offset"])
+                ve = int(descs[k + 1]["vertex_offset"]) if k + 1 < len(descs) else nv
+                io0, ic = int(d["index_offset"]), int(d["index_count"])
+                data.meshes.append(MeshData(position=pos[vo:ve], normal=nrm[vo:ve], texCrd=uv[vo:ve],
+                                            index=idx[io0:io0 + ic] - np.uint32(vo), materialID=int(d["material_id"])))
+            for k, m in enumerate(mats):
+                md = MaterialData(diffuseRefl=tuple(float(x) for x in m["diffuse"]),
+                                  specularRefl=tuple(float(x) for x in m["specular"]),
+                                  emission=tuple(float(x) for x in m["emission"]), shininess=float(m["shininess"]),
+                                  type=MaterialType(int(m["type"])))
+                md.name = lib.cr_import_material_name(h, k).decode()
+                md.finalize()
+                if mat_tex[k] != _lib.CR_NO_TEXTURE:
+                    md.flags |= int(MaterialFlags.hasDiffuseTexture)
+                    md.diffuseHandle = int(mat_tex[k])
+                data.materials.append(md)
+            data.emissiveIndex = arr(v.emissive, v.n_emissive, np.uint32).tolist()
+            data.textureImages = textures
+            c = v.camera
+            cam = Camera()
+            cam.setWorldPosition(tuple(c.pos))
+            cam.setTarget(tuple(c.target))
+            cam.setUp(tuple(c.up))
+            cam.setFovY(c.fov_y)
+            cam.setSensor(Sensor((c.width, c.height)))
+            return data, cam
+        finally:
+            lib.cr_import_destroy(h)
+
+    def import_(self, path: str) -> Scene:
+        """Importer::import (Utils/Importer.cpp:203-236): the scene, with its
+        camera set."""
+        data, cam = self.load(path)
+        sc = Scene(data)
+        sc.setCamera(cam)
+        return sc

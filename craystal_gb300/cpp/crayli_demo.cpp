@@ -45,7 +45,7 @@ int main(int argc, char** argv) {
         scene.setCamera(cam);
         PathTraceIntegrator integ(PathTraceIntegrator::Configs{});
         integ.dispatch(scene, 8);
-        std::vector<float> img = sensor->createImage();
+        const std::vector<float>& img = sensor->createImage()->data();
         if (argc > 1) {
             FILE* f = std::fopen(argv[1], "wb");
             if (!f) return 2;

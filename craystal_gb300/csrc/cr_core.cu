@@ -57,12 +57,9 @@ MaterialGpu deriveMaterial(const cr_material& m) {
     const Spec em = sp(m.emission[0], m.emission[1], m.emission[2]);
     if (maxValue(em) != 0.0f) g.flags |= CR_MATERIAL_EMISSIVE;
     if (maxValue(ks) == 0.0f) g.flags |= CR_MATERIAL_DIFFUSE_ONLY;
+    g.tex = CR_NO_TEXTURE;
     if (m.type == CR_MATERIAL_PHONG) {
-        float d = smax(averageValue(kd), 0.0f);
-        float s = smax(averageValue(ks), 0.0f);
-        float sum = gmax(d + s, kEps);
-        g.dProb = d / sum;
-        g.sProb = s / sum;
+        phongLobeProbs(kd, ks, kEps, g.dProb, g.sProb);
     } else if (m.type == CR_MATERIAL_PRINCIPLED) {
         float r = sqrtf(2.0f / (m.shininess + 1.0f));
         float met = averageValue(ks);
@@ -93,7 +90,8 @@ void freeScene(cr_scene* s) {
     cudaSetDevice(s->device);
     void* ptrs[] = {s->pos,  s->nrm,      s->uv,         s->idx,        s->primToMesh, s->meshes,
                     s->mats, s->emissive, s->pairs,      s->leaves,     s->tris,       s->slotToPrim,
-                    s->buildNodes, s->errFlags, s->filmRgb, s->filmW, s->rayCounter, s->spheres, s->sphereEm};
+                    s->buildNodes, s->errFlags, s->filmRgb, s->filmW, s->rayCounter, s->spheres, s->sphereEm,
+                    s->texels, s->texDescs};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     freeCacheBuffers(s->cacheBuffers);
@@ -298,6 +296,50 @@ int cr_scene_set_sphere_lights(cr_scene* scene, const cr_sphere_light* lights, u
         CR_CUDA(cudaMemcpy(scene->sphereEm, em.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
     }
     scene->nSpheres = n;
+    return CR_OK;
+}
+
+int cr_scene_set_diffuse_textures(cr_scene* scene, const cr_texture* textures, uint32_t nTex,
+                                  const uint32_t* matTex, uint32_t nMats) {
+    clearError();
+    if (!scene || (nTex && !textures) || (nMats && !matTex)) return fail(CR_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (nMats != scene->nMats)
+        return fail(CR_ERR_INVALID_ARGUMENT, "%u material textures for %u materials", nMats, scene->nMats);
+    std::vector<uint4> descs(nTex);
+    uint64_t total = 0;
+    for (uint32_t t = 0; t < nTex; t++) {
+        const cr_texture& x = textures[t];
+        if (x.width == 0 || x.height == 0 || !x.texels)
+            return fail(CR_ERR_INVALID_ARGUMENT, "texture %u is empty (%u x %u)", t, x.width, x.height);
+        const uint64_t texels = (uint64_t)x.width * x.height;
+        if (texels > 0xFFFFFFFFull || total + texels > 0xFFFFFFFFull)
+            return fail(CR_ERR_INVALID_ARGUMENT, "textures exceed 2^32 texels");
+        descs[t] = make_uint4((uint32_t)total, x.width, x.height, 0u);
+        total += texels;
+    }
+    for (uint32_t m = 0; m < nMats; m++)
+        if (matTex[m] != CR_NO_TEXTURE && matTex[m] >= nTex)
+            return fail(CR_ERR_INVALID_ARGUMENT, "material %u names texture %u of %u", m, matTex[m], nTex);
+    CR_CUDA(cudaSetDevice(scene->device));
+    CR_CUDA(cudaDeviceSynchronize());
+    std::vector<MaterialGpu> mats(nMats);
+    if (nMats) CR_CUDA(cudaMemcpy(mats.data(), scene->mats, nMats * sizeof(MaterialGpu), cudaMemcpyDeviceToHost));
+    for (uint32_t m = 0; m < nMats; m++) mats[m].tex = matTex[m];
+    if (scene->texels) cudaFree(scene->texels);
+    if (scene->texDescs) cudaFree(scene->texDescs);
+    scene->texels = nullptr;
+    scene->texDescs = nullptr;
+    scene->nTex = 0;
+    if (nTex) {
+        CR_CUDA(cudaMalloc(&scene->texels, total * sizeof(float4)));
+        CR_CUDA(cudaMalloc(&scene->texDescs, nTex * sizeof(uint4)));
+        for (uint32_t t = 0; t < nTex; t++)
+            CR_CUDA(cudaMemcpy(scene->texels + descs[t].x, textures[t].texels,
+                               (size_t)descs[t].y * descs[t].z * sizeof(float4), cudaMemcpyHostToDevice));
+        CR_CUDA(cudaMemcpy(scene->texDescs, descs.data(), nTex * sizeof(uint4), cudaMemcpyHostToDevice));
+    }
+    scene->nTex = nTex;
+    if (nMats) CR_CUDA(cudaMemcpy(scene->mats, mats.data(), nMats * sizeof(MaterialGpu), cudaMemcpyHostToDevice));
     return CR_OK;
 }
 

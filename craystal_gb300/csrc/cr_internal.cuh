@@ -106,6 +106,7 @@ struct MaterialGpu {
     // derived once per material, as the BSDF constructors compute them
     float dProb, sProb;       // lobe selection (Phong, Principled)
     float rough, metal;       // Principled
+    uint32_t tex;             // diffuse texture or CR_NO_TEXTURE
 };
 
 struct CameraGpu {
@@ -139,6 +140,8 @@ struct SceneView {
     uint32_t nSpheres;             // sphere lights
     const float4* spheres;         // (center, radius)
     const float4* sphereEm;        // (emission, 0)
+    const float4* texels;          // all diffuse textures, row-major RGBA
+    const uint4* texDescs;         // (first texel, width, height, 0) per texture
 };
 
 constexpr uint32_t kSpherePrim = 0xFFFFFF00u;  // hit ids kSpherePrim + i for sphere light i
@@ -190,6 +193,10 @@ struct cr_scene {
     uint32_t nSpheres = 0;
     float4* spheres = nullptr;
     float4* sphereEm = nullptr;
+    // diffuse textures
+    float4* texels = nullptr;
+    uint4* texDescs = nullptr;
+    uint32_t nTex = 0;
 
     cr::SceneView view() const {
         cr::SceneView v;
@@ -215,6 +222,8 @@ struct cr_scene {
         v.nSpheres = nSpheres;
         v.spheres = spheres;
         v.sphereEm = sphereEm;
+        v.texels = texels;
+        v.texDescs = texDescs;
         return v;
     }
 };

@@ -100,4 +100,13 @@ __host__ __device__ __forceinline__ float averageValue(Spec a) {
     return v / 3.0f;
 }
 
+// PhongBRDF::PhongBRDF lobe-selection probabilities (Material/PhongBRDF.cu:10-19)
+__host__ __device__ __forceinline__ void phongLobeProbs(Spec kd, Spec ks, float eps, float& dProb, float& sProb) {
+    const float d = smax(averageValue(kd), 0.0f);
+    const float s = smax(averageValue(ks), 0.0f);
+    const float sum = gmax(d + s, eps);
+    dProb = d / sum;
+    sProb = s / sum;
+}
+
 }  // namespace cr

@@ -34,10 +34,18 @@ __device__ __forceinline__ Spec emissionOf(const PathCtx& c, const MaterialGpu& 
     return toPathSpec(c.spec, m.em[0], m.em[1], m.em[2]);
 }
 
-__device__ __forceinline__ void initBsdf(const PathCtx& c, Bsdf& b, const MaterialGpu& m, const Frame& f) {
+// getBSDF (Material/BSDF.cu:7-31): the material's lobes, with the diffuse
+// reflectance of a textured material sampled at the hit.
+__device__ __forceinline__ void initBsdf(const PathCtx& c, Bsdf& b, const MaterialGpu& m, const Frame& f,
+                                         uint32_t prim, float u, float v) {
     b.init(m, f);
+    if (m.tex != CR_NO_TEXTURE) {
+        const float4 t = texSample(c.sc, m.tex, texCoordAt(c.sc, prim, u, v));
+        b.kd = sp(t.x, t.y, t.z);
+        if (m.type == CR_MATERIAL_PHONG) phongLobeProbs(b.kd, b.ks, kEps, b.dProb, b.sProb);
+    }
     if (c.spec.on) {
-        b.kd = toPathSpec(c.spec, m.kd[0], m.kd[1], m.kd[2]);
+        b.kd = toPathSpec(c.spec, b.kd.r, b.kd.g, b.kd.b);
         b.ks = toPathSpec(c.spec, m.ks[0], m.ks[1], m.ks[2]);
     }
 }
@@ -222,7 +230,7 @@ __device__ __forceinline__ Spec tracePath(PathCtx& c, const CameraGpu& cam, cons
                 break;
             }
             Bsdf bsdf;
-            initBsdf(c, bsdf, m, it.frame);
+            initBsdf(c, bsdf, m, it.frame, h.prim, h.u, h.v);
             if (p.useMIS) {
                 radiance = add(radiance, mul(evalMIS(c, it, bsdf, smp), beta));
             } else {

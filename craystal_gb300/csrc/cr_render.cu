@@ -132,6 +132,13 @@ __global__ void kBsdf(const MaterialGpu m, const float3* __restrict__ nrm, const
     pdf[i] = p;
 }
 
+__global__ void kTexSample(const SceneView sc, uint32_t tex, const float2* __restrict__ uv, uint64_t n,
+                           float4* __restrict__ out) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[i] = texSample(sc, tex, uv[i]);
+}
+
 template <class T>
 struct Dev {
     T* p = nullptr;
@@ -217,4 +224,21 @@ extern "C" int cr_bsdf_sample(const cr_material* mat, const float* n, const floa
                               uint64_t count, float* wi, float* f, float* pdf) {
     clearError();
     return bsdfBatch(mat, n, wo, nullptr, u, count, wi, f, pdf);
+}
+
+extern "C" int cr_texture_sample(const cr_scene* scene, uint32_t texture, const float* uv, uint64_t n, float* rgba) {
+    clearError();
+    if (!scene || (n && (!uv || !rgba))) return fail(CR_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (texture >= scene->nTex) return fail(CR_ERR_INVALID_ARGUMENT, "texture %u of %u", texture, scene->nTex);
+    if (n == 0) return CR_OK;
+    CR_CUDA(cudaSetDevice(scene->device));
+    Dev<float2> du;
+    Dev<float4> dout;
+    CR_CUDA(cudaMalloc(&du.p, n * sizeof(float2)));
+    CR_CUDA(cudaMalloc(&dout.p, n * sizeof(float4)));
+    CR_CUDA(cudaMemcpy(du.p, uv, n * sizeof(float2), cudaMemcpyHostToDevice));
+    kTexSample<<<(unsigned)((n + 127) / 128), 128>>>(scene->view(), texture, du.p, n, dout.p);
+    CR_LAUNCH_CHECK();
+    CR_CUDA(cudaMemcpy(rgba, dout.p, n * sizeof(float4), cudaMemcpyDeviceToHost));
+    return CR_OK;
 }

@@ -126,6 +126,47 @@ __device__ __forceinline__ const MaterialGpu& materialOf(const SceneView& sc, ui
     return sc.mats[sc.meshes[sc.primToMesh[prim]].material_id];
 }
 
+// Interpolated texture coordinates of a hit (TriangleData::interpolate,
+// Scene/Triangle.cu:18-30, with the weights of HitInfo::getBarycentricWeights,
+// Core/Hit.h:20-23).
+__device__ __forceinline__ float2 texCoordAt(const SceneView& sc, uint32_t prim, float u, float v) {
+    const float w0 = (1.f - u) - v;
+    float2 t[3];
+    for (int k = 0; k < 3; k++) t[k] = sc.uv[__ldg(sc.idx + 3 * prim + k)];
+    return make_float2((t[0].x * w0 + t[1].x * u) + t[2].x * v, (t[0].y * w0 + t[1].y * u) + t[2].y * v);
+}
+
+// TextureView::fetchTexel (Core/Texture.cu:6-13): clamp to the last texel.
+__device__ __forceinline__ float4 texFetch(const SceneView& sc, uint4 d, uint32_t x, uint32_t y) {
+    x = (d.y - 1u) < x ? d.y - 1u : x;
+    y = (d.z - 1u) < y ? d.z - 1u : y;
+    return __ldg(sc.texels + d.x + (y * d.y + x));
+}
+
+__device__ __forceinline__ float4 lerp4(float4 a, float4 b, float t) {
+    const float s = 1.0f - t;
+    return make_float4(a.x * s + b.x * t, a.y * s + b.y * t, a.z * s + b.z * t, a.w * s + b.w * t);
+}
+
+// TextureView::sample (Core/Texture.cu:15-35): bilinear over texel centres
+// at uv * (size - 1).  The float -> uint32 conversions are the device's
+// (truncating and saturating: a negative coordinate gives texel 0 and a
+// negative fraction, which extrapolates as the reference does).
+__device__ __forceinline__ float4 texSample(const SceneView& sc, uint32_t tex, float2 uv) {
+    const uint4 d = __ldg(sc.texDescs + tex);
+    const float px = uv.x * (float)(d.y - 1u);
+    const float py = uv.y * (float)(d.z - 1u);
+    const uint32_t x0 = __float2uint_rz(floorf(px));
+    const uint32_t y0 = __float2uint_rz(floorf(py));
+    const uint32_t x1 = min(x0 + 1u, d.y - 1u);
+    const uint32_t y1 = min(y0 + 1u, d.z - 1u);
+    const float fx = px - (float)x0;
+    const float fy = py - (float)y0;
+    const float4 c0 = lerp4(texFetch(sc, d, x0, y0), texFetch(sc, d, x1, y0), fx);
+    const float4 c1 = lerp4(texFetch(sc, d, x0, y1), texFetch(sc, d, x1, y1), fx);
+    return lerp4(c0, c1, fy);
+}
+
 // ---------------------------------------------------------------------------
 // Math/Sampling.cu, Math/CRayMath.cu
 // ---------------------------------------------------------------------------

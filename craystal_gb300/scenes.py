@@ -15,7 +15,7 @@ import math
 import numpy as np
 
 from ._lib import RAY_DTYPE
-from .api import Camera, MaterialData, MaterialType, MeshData, SceneData, Sensor
+from .api import Camera, MaterialData, MaterialFlags, MaterialType, MeshData, SceneData, Sensor
 
 
 def _quad(p0, p1, p2, p3, normal):
@@ -122,6 +122,34 @@ def cornell_box(seed: int = 0, width: int = 256, height: int = 256):
     cam.setUp((0.0, 1.0, 0.0))
     cam.setFovY(40.0)
     cam.setSensor(Sensor((width, height)))
+    return data, cam
+
+
+def textured_cornell_box(seed: int = 0, width: int = 256, height: int = 256, tex_res: int = 64):
+    """The Cornell box with two diffuse textures: a checkerboard on the floor
+    (Phong, so its lobe probabilities follow the texel) and a colour ramp on
+    the back wall (Lambertian).  The planar texture coordinates run over
+    [-0.1, 1.1], so the edge clamp and the extrapolation below 0 are used."""
+    data, cam = cornell_box(seed, width, height)
+    rng = np.random.default_rng(seed + 1000)
+    k = np.arange(tex_res)
+    checker = ((k[:, None] // 8 + k[None, :] // 8) % 2).astype(np.float32)
+    floor_tex = np.stack([0.15 + 0.7 * checker, 0.15 + 0.6 * checker, 0.1 + 0.5 * (1 - checker)], -1)
+    ramp = np.stack(np.meshgrid(np.linspace(0.1, 0.9, tex_res), np.linspace(0.9, 0.1, tex_res // 2)), -1)
+    wall_tex = np.concatenate([ramp, rng.uniform(0.2, 0.6, (tex_res // 2, tex_res, 1))], -1).astype(np.float32)
+    data.textureImages = [floor_tex, wall_tex]
+    for mesh_id, axes, tex in ((0, (0, 2), 0), (2, (0, 1), 1)):
+        mesh = data.meshes[mesh_id]
+        p = np.asarray(mesh.position, np.float32)
+        mesh.texCrd = (-0.1 + 1.2 * (p[:, list(axes)] + 1.0) / 2.0).astype(np.float32)
+        m = data.materials[mesh.materialID]
+        m.diffuseHandle = tex
+        m.flags |= int(MaterialFlags.hasDiffuseTexture)
+        if tex == 0:
+            m.type = MaterialType.Phong
+            m.specularRefl = (0.3, 0.3, 0.3)
+            m.shininess = 20.0
+            m.flags &= ~int(MaterialFlags.IsDiffuse)
     return data, cam
 
 
@@ -369,3 +397,69 @@ def batch_workload(n_scenes: int = 64, seed: int = 0):
                     "spp": int(round(np.exp(rng.uniform(np.log(4), np.log(256))))),
                     "depth": int(rng.integers(8, 17))})
     return out
+
+
+def export_obj_scene(data: SceneData, cam: Camera, xml_path: str) -> str:
+    """Writes a scene as the importer reads it: <name>.xml (camera, one
+    <light> per emissive material), <name>.obj (one object per mesh) and
+    <name>.mtl (Kd, Ks, Ns; map_Kd to an 8-bit PNG per texture).  Emission
+    goes through the XML, as the reference's scene files carry it."""
+    import os
+
+    from .api import Image
+    base = os.path.splitext(str(xml_path))[0]
+    stem = os.path.basename(base)
+    folder = os.path.dirname(base)
+    tex_names = []
+    for t, img in enumerate(data.textureImages):
+        name = f"{stem}_tex{t}.png"
+        a = np.asarray(img, np.float32)
+        # rows are stored bottom-up after loading, so write them top-down
+        Image(data=a[::-1, :, :3] if a.ndim == 3 else a[::-1]).writePNG(os.path.join(folder, name), False)
+        tex_names.append(name)
+    with open(base + ".mtl", "w") as f:
+        for k, m in enumerate(data.materials):
+            f.write(f"newmtl mat{k}\n")
+            f.write("Kd {:.9g} {:.9g} {:.9g}\n".format(*m.diffuseRefl))
+            f.write("Ks {:.9g} {:.9g} {:.9g}\n".format(*m.specularRefl))
+            f.write(f"Ns {m.shininess:.9g}\n")
+            if m.flags & MaterialFlags.hasDiffuseTexture:
+                f.write(f"map_Kd {tex_names[m.diffuseHandle]}\n")
+    with open(base + ".obj", "w") as f:
+        f.write(f"mtllib {stem}.mtl\n")
+        nv = 0
+        for k, mesh in enumerate(data.meshes):
+            p = np.asarray(mesh.position, np.float32).reshape(-1, 3)
+            n = None if mesh.normal is None else np.asarray(mesh.normal, np.float32).reshape(-1, 3)
+            t = None if mesh.texCrd is None else np.asarray(mesh.texCrd, np.float32).reshape(-1, 2)
+            f.write(f"o mesh{k}\nusemtl mat{mesh.materialID}\n")
+            for v in p:
+                f.write("v {:.9g} {:.9g} {:.9g}\n".format(*v))
+            if n is not None:
+                for v in n:
+                    f.write("vn {:.9g} {:.9g} {:.9g}\n".format(*v))
+            if t is not None:
+                for v in t:
+                    f.write("vt {:.9g} {:.9g}\n".format(*v))
+            for tri in np.asarray(mesh.index, np.int64).reshape(-1, 3) + 1 + nv:
+                if n is not None and t is not None:
+                    f.write("f " + " ".join(f"{i}/{i}/{i}" for i in tri) + "\n")
+                elif n is not None:
+                    f.write("f " + " ".join(f"{i}//{i}" for i in tri) + "\n")
+                elif t is not None:
+                    f.write("f " + " ".join(f"{i}/{i}" for i in tri) + "\n")
+                else:
+                    f.write("f " + " ".join(str(i) for i in tri) + "\n")
+            nv += len(p)
+    w, h = cam.sensor.size if cam.sensor else (512, 512)
+    with open(base + ".xml", "w") as f:
+        f.write('<?xml version="1.0" encoding="utf-8"?>\n')
+        f.write(f'<camera type="perspective" width="{w}" height="{h}" fovy="{cam.fovY:.9g}">\n')
+        for tag, v in (("eye", cam.posW), ("lookat", cam.target), ("up", cam.up)):
+            f.write(f'  <{tag} x="{v[0]:.9g}" y="{v[1]:.9g}" z="{v[2]:.9g}"/>\n')
+        f.write("</camera>\n")
+        for k, m in enumerate(data.materials):
+            if max(m.emission) != 0.0:
+                f.write(f'<light mtlname="mat{k}" radiance="{m.emission[0]:.9g},{m.emission[1]:.9g},'
+                        f'{m.emission[2]:.9g}"/>\n')
+    return base + ".xml"

@@ -9,6 +9,8 @@
 //   CRay::Camera (setters, setSensor)           Core/Camera.h:18-46
 //   CRay::Sensor(size, spp), createImage        Core/Sensor.h:33-61
 //   CRay::PathTraceIntegrator(Configs).dispatch Core/Integrator.h:10-38
+//   CRay::Image (load, writeEXR, writePNG)      Utils/Image.h:24-90
+//   CRay::Importer().import(xml)                Utils/Importer.h:10-28
 //
 // Header-only; link with libcraystal_gb300.so.  Errors throw
 // CRay::RuntimeError, as the reference's CRAYSTAL_CHECK does.
@@ -48,7 +50,45 @@ inline void crCheck(int code) {
 }
 
 enum class MaterialType : uint32_t { FullDiffuse = 0, Principled = 1, Phong = 2 };
-enum class MaterialFlags : uint32_t { IsEmissive = 1, IsDiffuse = 2 };
+enum class MaterialFlags : uint32_t { IsEmissive = 1, IsDiffuse = 2, hasDiffuseTexture = 4 };
+
+/** Utils/Image.h:24-90: float pixels, interleaved (y * width + x) * channels + c. */
+class Image {
+   public:
+    using Ref = std::shared_ptr<Image>;
+    Image(size_t width, size_t height, int channels)
+        : mWidth(uint32_t(width)), mHeight(uint32_t(height)), mChannels(uint32_t(channels)),
+          mData(width * height * size_t(channels), 0.0f) {}
+    int getWidth() const { return int(mWidth); }
+    int getHeight() const { return int(mHeight); }
+    int getChannels() const { return int(mChannels); }
+    int getArea() const { return int(mWidth * mHeight); }
+    float getPixel(int x, int y, int c) const { return mData[(size_t(y) * mWidth + x) * mChannels + c]; }
+    void setPixel(int x, int y, int c, float v) { mData[(size_t(y) * mWidth + x) * mChannels + c] = v; }
+    std::vector<float>& data() { return mData; }
+    const std::vector<float>& data() const { return mData; }
+    /** Image::writeEXR, Utils/Image.cpp:49-106. */
+    void writeEXR(const std::string& path) const {
+        crCheck(cr_image_write_exr(path.c_str(), mWidth, mHeight, mChannels, mData.data()));
+    }
+    /** Image::writePNG, Utils/Image.cpp:182-217. */
+    void writePNG(const std::string& path, bool gammaCorrect) const {
+        crCheck(cr_image_write_png(path.c_str(), mWidth, mHeight, mChannels, mData.data(), gammaCorrect ? 1 : 0));
+    }
+    /** Image::load, Utils/Image.cpp:262-270. */
+    static Image load(const std::string& path, bool toLinear = true) {
+        cr_image img{};
+        crCheck(cr_image_load(path.c_str(), toLinear ? 1 : 0, &img));
+        Image out(img.width, img.height, int(img.channels));
+        std::copy(img.pixels, img.pixels + out.mData.size(), out.mData.begin());
+        cr_image_free(&img);
+        return out;
+    }
+
+   private:
+    uint32_t mWidth, mHeight, mChannels;
+    std::vector<float> mData;
+};
 
 struct MaterialData {
     Float3 diffuseRefl;
@@ -57,6 +97,7 @@ struct MaterialData {
     Float shininess = 0;
     MaterialType type = MaterialType::FullDiffuse;
     uint32_t flags = 0;
+    uint32_t diffuseHandle = 0;  ///< texture index when flags has hasDiffuseTexture
 
     bool isEmissive() const { return flags & uint32_t(MaterialFlags::IsEmissive); }
     // MaterialData::finalize, Core/Material.h:57-65
@@ -79,6 +120,7 @@ struct SceneData {
     std::vector<MeshData> meshes;
     std::vector<MaterialData> materials;
     std::vector<uint32_t> emissiveIndex;
+    std::vector<Image> textureImages;
 };
 
 /** Film of a sensor; the host copy is filled by PathTraceIntegrator::dispatch. */
@@ -93,10 +135,10 @@ class Sensor {
     uint32_t getSPP() const { return mSpp; }
     UInt2 getSize() const { return mSize; }
     /** Sensor::createImage (Core/Sensor.cu:93-112): rgb = sum / weight, row-major, 3 floats per pixel. */
-    std::vector<float> createImage() const {
-        std::vector<float> img(mData.size());
+    Image::Ref createImage() const {
+        auto img = std::make_shared<Image>(mSize.x, mSize.y, 3);
         for (size_t i = 0; i < mWeight.size(); i++)
-            for (int c = 0; c < 3; c++) img[3 * i + c] = mData[3 * i + c] / mWeight[i];
+            for (int c = 0; c < 3; c++) img->data()[3 * i + c] = mData[3 * i + c] / mWeight[i];
         return img;
     }
     std::vector<float>& data() { return mData; }
@@ -140,6 +182,8 @@ class Camera {
     Sensor::Ref mSensor;
 };
 
+class Importer;
+
 class Scene {
    public:
     using Ref = std::shared_ptr<Scene>;
@@ -180,6 +224,27 @@ class Scene {
                                 descs.data(), uint32_t(descs.size()), mats.data(), uint32_t(mats.size()),
                                 data.emissiveIndex.data(), uint32_t(data.emissiveIndex.size()), &s));
         mScene.reset(s, [](cr_scene* p) { cr_scene_destroy(p); });
+        if (!data.textureImages.empty()) {
+            // Texture(const Image&), Core/Texture.cu:45-60: RGBA texels, missing channels 0
+            std::vector<std::vector<float>> texels;
+            std::vector<cr_texture> texs;
+            for (const Image& im : data.textureImages) {
+                std::vector<float> t(size_t(im.getArea()) * 4, 0.0f);
+                for (int p = 0; p < im.getArea(); p++)
+                    for (int c = 0; c < std::min(im.getChannels(), 4); c++)
+                        t[4 * size_t(p) + c] = im.data()[size_t(p) * im.getChannels() + c];
+                texels.push_back(std::move(t));
+            }
+            for (size_t i = 0; i < texels.size(); i++)
+                texs.push_back(cr_texture{uint32_t(data.textureImages[i].getWidth()),
+                                          uint32_t(data.textureImages[i].getHeight()), texels[i].data()});
+            std::vector<uint32_t> matTex;
+            for (const MaterialData& md : data.materials)
+                matTex.push_back(md.flags & uint32_t(MaterialFlags::hasDiffuseTexture) ? md.diffuseHandle
+                                                                                       : CR_NO_TEXTURE);
+            crCheck(cr_scene_set_diffuse_textures(s, texs.data(), uint32_t(texs.size()), matTex.data(),
+                                                  uint32_t(matTex.size())));
+        }
     }
     Camera::Ref getCamera() { return mCamera; }
     void setCamera(const Camera::Ref& c) {
@@ -190,8 +255,35 @@ class Scene {
     cr_scene* handle() const { return mScene.get(); }
 
    private:
+    friend class Importer;
+    explicit Scene(cr_scene* s) { mScene.reset(s, [](cr_scene* p) { cr_scene_destroy(p); }); }
     std::shared_ptr<cr_scene> mScene;
     Camera::Ref mCamera;
+};
+
+/** Utils/Importer.h:10-28: an XML scene description beside an OBJ/MTL file
+ *  of the same name. */
+class Importer {
+   public:
+    /** Importer::import (Utils/Importer.cpp:203-236): the scene with its camera set. */
+    Scene::Ref import(const std::string& path) {
+        cr_import* imp = nullptr;
+        crCheck(cr_import_xml(path.c_str(), &imp));
+        std::unique_ptr<cr_import, int (*)(cr_import*)> guard(imp, cr_import_destroy);
+        cr_import_view v{};
+        crCheck(cr_import_get(imp, &v));
+        cr_scene* s = nullptr;
+        crCheck(cr_import_create_scene(imp, &s));
+        Scene::Ref scene(new Scene(s));
+        auto cam = std::make_shared<Camera>();
+        cam->setWorldPosition({v.camera.pos[0], v.camera.pos[1], v.camera.pos[2]});
+        cam->setTarget({v.camera.target[0], v.camera.target[1], v.camera.target[2]});
+        cam->setUp({v.camera.up[0], v.camera.up[1], v.camera.up[2]});
+        cam->setFovY(v.camera.fov_y);
+        cam->setSensor(std::make_shared<Sensor>(UInt2{v.camera.width, v.camera.height}));
+        scene->setCamera(cam);
+        return scene;
+    }
 };
 
 class PathTraceIntegrator {

@@ -31,6 +31,7 @@ extern "C" {
 #define CR_ERR_OUT_OF_MEMORY 3
 #define CR_ERR_DEVICE 4       /* a kernel reported an error (stack overflow, timeout) */
 #define CR_ERR_UNSUPPORTED 5
+#define CR_ERR_IO 6           /* a file could not be read, written or parsed */
 
 #define CR_MISS 0xFFFFFFFFu
 
@@ -174,7 +175,8 @@ int cr_scene_set_camera(cr_scene* scene, const cr_camera* cam);
 
 /* ---- lights beyond the reference (extensions) ----
  * The reference has neither: its paths end with 0 on a miss
- * (Core/Integrator.cu:205-207) and it shades no sphere (bug 0.5k).
+ * (Core/Integrator.cu:205-207), and its spheres (Scene/Sphere.cu:6-52)
+ * are shaded through the triangle-mesh tables, which is wrong for them.
  * Environment: constant radiance collected by every ray that leaves the
  * scene.  Sphere lights: analytic emitting spheres, intersected in a linear
  * loop after the BVH (as SceneView::intersect does for spheres,
@@ -189,6 +191,92 @@ typedef struct {
 int cr_scene_set_environment(cr_scene* scene, const float radiance[3]);
 int cr_scene_set_sphere_lights(cr_scene* scene, const cr_sphere_light* lights,
                                uint32_t n);
+
+/* ---- diffuse textures ----
+ * SceneData::textureImages + MaterialData::diffuseHandle and the
+ * hasDiffuseTexture flag (Scene/Scene.h:45, Core/Material.h:29-36): a
+ * texture is width x height texels, row-major RGBA float4, row 0 first
+ * (Texture(const Image&), Core/Texture.cu:45-60).  A textured material's
+ * diffuse reflectance is the texture's bilinear sample at the hit's
+ * interpolated texture coordinates (getBSDF, Material/BSDF.cu:11-15;
+ * TextureView::sample, Core/Texture.cu:15-35), and a Phong material's lobe
+ * probabilities follow from that per-hit reflectance
+ * (Material/PhongBRDF.cu:10-19).  material_texture[m] is the texture of
+ * material m or CR_NO_TEXTURE; n_mats must equal the scene's material
+ * count.  A new call replaces all textures. */
+#define CR_NO_TEXTURE 0xFFFFFFFFu
+typedef struct {
+    uint32_t width;
+    uint32_t height;
+    const float* texels; /* width * height * 4 floats */
+} cr_texture;
+int cr_scene_set_diffuse_textures(cr_scene* scene, const cr_texture* textures,
+                                  uint32_t n_textures,
+                                  const uint32_t* material_texture,
+                                  uint32_t n_mats);
+
+/* TextureView::sample (Core/Texture.cu:15-35) on the device for n texture
+ * coordinates (uv: 2n floats, host) into rgba (4n floats, host). */
+int cr_texture_sample(const cr_scene* scene, uint32_t texture, const float* uv,
+                      uint64_t n, float* rgba);
+
+/* ---- scene import ----
+ * Importer::import (Utils/Importer.cpp:203-236): path names an XML file
+ * with the camera and the emissive materials; the geometry is the OBJ file
+ * of the same name beside it, with its MTL library.  All materials are
+ * Phong; a material listed in a <light> element gets that radiance; a
+ * map_Kd texture is loaded (PNG or EXR) and linearised as Image::load does.
+ * The result stays on the host until cr_import_create_scene uploads it:
+ * cr_import_get exposes its arrays (valid until cr_import_destroy) in the
+ * layout cr_scene_create takes. */
+typedef struct cr_import cr_import;
+typedef struct {
+    const float* pos;             /* n_vertices * 3 */
+    const float* nrm;             /* n_vertices * 3 */
+    const float* uv;              /* n_vertices * 2 */
+    uint64_t n_vertices;
+    const uint32_t* idx;          /* n_tris * 3, global vertex indices */
+    uint64_t n_tris;
+    const cr_mesh_desc* meshes;
+    uint32_t n_meshes;
+    const cr_material* mats;
+    const uint32_t* material_texture;  /* per material: texture or CR_NO_TEXTURE */
+    uint32_t n_mats;
+    const uint32_t* emissive;     /* SceneData::emissiveIndex */
+    uint32_t n_emissive;
+    const cr_texture* textures;
+    uint32_t n_textures;
+    cr_camera camera;             /* fovy, eye, lookat, up, width, height */
+} cr_import_view;
+int cr_import_xml(const char* path, cr_import** out);
+int cr_import_get(const cr_import* imp, cr_import_view* out);
+/* The OBJ material name of a material ("" when out of range). */
+const char* cr_import_material_name(const cr_import* imp, uint32_t material);
+/* Scene(SceneData&&) + Scene::setCamera of the imported scene. */
+int cr_import_create_scene(const cr_import* imp, cr_scene** out);
+int cr_import_destroy(cr_import* imp);
+
+/* ---- image files (Utils/Image.cpp) ----
+ * Pixels are interleaved: (y * width + x) * channels + c, row 0 first. */
+typedef struct {
+    uint32_t width;
+    uint32_t height;
+    uint32_t channels;
+    float* pixels;                /* owned by the library: cr_image_free */
+} cr_image;
+/* Image::load (:262-270): ".exr" files by readEXR (R, G, B found by channel
+ * name; other channels read as 0), otherwise PNG by readMisc (rows flipped
+ * to bottom-up; values / 255, raised to 2.2 when to_linear). */
+int cr_image_load(const char* path, int to_linear, cr_image* out);
+int cr_image_free(cr_image* img);
+/* Image::writeEXR (:49-106): channels 0, 1, 2 as R, G, B in half floats. */
+int cr_image_write_exr(const char* path, uint32_t width, uint32_t height,
+                       uint32_t channels, const float* pixels);
+/* Image::writePNG (:182-217): 8-bit; gamma_correct encodes linear values
+ * with pow(v, 1/2.2) and clamps to [0, 1]; values are truncated. */
+int cr_image_write_png(const char* path, uint32_t width, uint32_t height,
+                       uint32_t channels, const float* pixels,
+                       int gamma_correct);
 
 /* Zeroes the film (the reference never clears its film, Core/Sensor.cu:55-59). */
 int cr_film_clear(cr_scene* scene);

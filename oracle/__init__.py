@@ -67,6 +67,8 @@ def lib():
             "orc_scene_create": (_P, [_P, _P, _P, U64, _P, U64, _P, U32, _P, U32, _P, U32]),
             "orc_scene_destroy": (None, [_P]),
             "orc_scene_set_lights": (None, [_P, _P, _P, U32]),
+            "orc_scene_set_textures": (None, [_P, _P, _P, U32, _P, U32]),
+            "orc_texture_sample": (None, [_P, U32, _P, U64, _P]),
             "orc_scene_bvh_stats": (None, [_P, ctypes.POINTER(OrcStats)]),
             "orc_scene_bvh_export": (None, [_P, _P, _P]),
             "orc_trace_closest": (None, [_P, _P, U64, _P, _P, I, ctypes.POINTER(OrcCounters)]),
@@ -163,6 +165,27 @@ class OracleScene:
         self.h = L.orc_scene_create(_p(flat["pos"]), _p(flat["nrm"]), _p(flat["uv"]), len(flat["pos"]),
                                     _p(flat["idx"]), self.n_tris, _p(meshes), len(meshes), _p(mats), len(mats),
                                     _p(flat["emissive"]), len(flat["emissive"]))
+        if flat.get("textures"):
+            self.set_textures(flat["textures"], flat["mat_tex"])
+
+    def set_textures(self, textures, material_texture):
+        """RGBA texel arrays (HxWx4) and the texture of each material (0xFFFFFFFF = none)."""
+        texels = np.concatenate([np.ascontiguousarray(t, np.float32).reshape(-1) for t in textures])
+        descs, first = [], 0
+        for t in textures:
+            descs += [first, t.shape[1], t.shape[0]]
+            first += t.shape[0] * t.shape[1]
+        descs = np.asarray(descs, np.uint32)
+        mt = np.ascontiguousarray(material_texture, np.uint32)
+        self._tex = (texels, descs, mt)
+        lib().orc_scene_set_textures(self.h, _p(texels), _p(descs), len(textures), _p(mt), len(mt))
+
+    def texture_sample(self, texture, uv):
+        """TextureView::sample at n coordinates -> n x 4."""
+        uv = np.ascontiguousarray(uv, np.float32).reshape(-1, 2)
+        out = np.empty((len(uv), 4), np.float32)
+        lib().orc_texture_sample(self.h, texture, _p(uv), len(uv), _p(out))
+        return out
 
     def __del__(self):
         if getattr(self, "h", None):

@@ -357,6 +357,10 @@ struct orc_scene {
     // lights beyond the reference (extensions)
     V3 env{0, 0, 0};
     std::vector<float> spheres;  // center xyz, radius, emission xyz per light (7 floats)
+    // diffuse textures (Core/Texture.cu, Core/Material.h:29-36)
+    std::vector<float> texels;         // RGBA per texel, all textures
+    std::vector<uint32_t> texDescs;    // first texel, width, height per texture
+    std::vector<uint32_t> matTex;      // texture per material or 0xFFFFFFFF
     uint32_t maxDepth = 0, maxLeaf = 0, maxLeafDepth = 0;
 };
 
@@ -739,6 +743,51 @@ static float acosSafe(float v) {  // Math/CRayMath.cu:11-13
 }
 
 // ---------------------------------------------------------------------------
+// TextureView::fetchTexel / sample, Core/Texture.cu:6-35
+// ---------------------------------------------------------------------------
+// static_cast<uint32_t>(float) as the device executes it: truncation toward
+// zero, saturating (negative and NaN -> 0, >= 2^32 -> 2^32 - 1).
+static uint32_t f2uDevice(float f) {
+    if (!(f > 0.0f)) return 0u;
+    if (f >= 4294967296.0f) return 0xFFFFFFFFu;
+    return (uint32_t)f;
+}
+
+struct RGBA {
+    float v[4];
+};
+
+static RGBA texFetch(const orc_scene& s, const uint32_t* d, uint32_t x, uint32_t y) {
+    x = std::clamp<uint32_t>(x, 0u, d[1] - 1u);
+    y = std::clamp<uint32_t>(y, 0u, d[2] - 1u);
+    const uint32_t index = y * d[1] + x;
+    RGBA r;
+    for (int k = 0; k < 4; k++) r.v[k] = s.texels[4 * ((size_t)d[0] + index) + k];
+    return r;
+}
+
+static RGBA lerp4(const RGBA& a, const RGBA& b, float t) {  // Math/CRayMath.h:31-33
+    RGBA r;
+    for (int k = 0; k < 4; k++) r.v[k] = a.v[k] * (1.0f - t) + b.v[k] * t;
+    return r;
+}
+
+static RGBA texSample(const orc_scene& s, uint32_t tex, V2 uv) {
+    const uint32_t* d = &s.texDescs[3 * (size_t)tex];
+    const float px = uv.x * (float)(d[1] - 1u);
+    const float py = uv.y * (float)(d[2] - 1u);
+    const uint32_t x0 = f2uDevice(std::floor(px));
+    const uint32_t y0 = f2uDevice(std::floor(py));
+    const uint32_t x1 = std::min<uint32_t>(x0 + 1u, d[1] - 1u);
+    const uint32_t y1 = std::min<uint32_t>(y0 + 1u, d[2] - 1u);
+    const float fx = px - (float)x0;
+    const float fy = py - (float)y0;
+    const RGBA c0 = lerp4(texFetch(s, d, x0, y0), texFetch(s, d, x1, y0), fx);
+    const RGBA c1 = lerp4(texFetch(s, d, x0, y1), texFetch(s, d, x1, y1), fx);
+    return lerp4(c0, c1, fy);
+}
+
+// ---------------------------------------------------------------------------
 // BSDFs, Material/*.cu
 // ---------------------------------------------------------------------------
 struct Bsdf {
@@ -749,9 +798,10 @@ struct Bsdf {
     float rough, metal;
     Frame frame;
 
-    Bsdf(const orc_material& m, const Frame& f) : frame(f) {
+    Bsdf(const orc_material& m, const Frame& f, const float* diffuse = nullptr) : frame(f) {
         type = m.type;
-        kd = {{m.diffuse[0], m.diffuse[1], m.diffuse[2]}};
+        if (!diffuse) diffuse = m.diffuse;
+        kd = {{diffuse[0], diffuse[1], diffuse[2]}};
         ks = {{m.specular[0], m.specular[1], m.specular[2]}};
         n = m.shininess;
         if (type == 2) {  // PhongBRDF.cu:10-18
@@ -1108,9 +1158,21 @@ static S3 tracePath(Tracer& tr, const CameraData& cam, const orc_integrator_conf
                 radiance = radiance + toPathSpec(tr.spec, m.emission) * beta;
                 break;
             }
-            Bsdf bsdf(m, it.frame);
+            // getBSDF, Material/BSDF.cu:11-15: a textured material's diffuse
+            // reflectance is the texture sampled at the hit
+            const float* diffuse = m.diffuse;
+            float texRgb[3];
+            const uint32_t mid = s.meshes[s.primToMesh[h.prim]].material_id;
+            if (mid < s.matTex.size() && s.matTex[mid] != 0xFFFFFFFFu) {
+                const RGBA t = texSample(s, s.matTex[mid], it.uv);
+                texRgb[0] = t.v[0];
+                texRgb[1] = t.v[1];
+                texRgb[2] = t.v[2];
+                diffuse = texRgb;
+            }
+            Bsdf bsdf(m, it.frame, diffuse);
             if (tr.spec.on) {
-                bsdf.kd = toPathSpec(tr.spec, m.diffuse);
+                bsdf.kd = toPathSpec(tr.spec, diffuse);
                 bsdf.ks = toPathSpec(tr.spec, m.specular);
             }
             if (cfg.use_mis) {
@@ -1266,6 +1328,22 @@ void orc_scene_destroy(orc_scene* s) { delete s; }
 void orc_scene_set_lights(orc_scene* s, const float* env3, const float* spheres7, uint32_t n_spheres) {
     s->env = env3 ? V3{env3[0], env3[1], env3[2]} : V3{0, 0, 0};
     s->spheres.assign(spheres7, spheres7 + 7 * (size_t)n_spheres);
+}
+
+void orc_scene_set_textures(orc_scene* s, const float* texels, const uint32_t* descs, uint32_t n_tex,
+                            const uint32_t* mat_tex, uint32_t n_mats) {
+    size_t total = 0;
+    for (uint32_t t = 0; t < n_tex; t++) total = std::max<size_t>(total, (size_t)descs[3 * t] + (size_t)descs[3 * t + 1] * descs[3 * t + 2]);
+    s->texels.assign(texels, texels + 4 * total);
+    s->texDescs.assign(descs, descs + 3 * (size_t)n_tex);
+    s->matTex.assign(mat_tex, mat_tex + n_mats);
+}
+
+void orc_texture_sample(const orc_scene* s, uint32_t tex, const float* uv, uint64_t n, float* rgba) {
+    for (uint64_t i = 0; i < n; i++) {
+        const RGBA r = texSample(*s, tex, V2{uv[2 * i], uv[2 * i + 1]});
+        for (int k = 0; k < 4; k++) rgba[4 * i + k] = r.v[k];
+    }
 }
 
 void orc_scene_bvh_stats(const orc_scene* s, orc_bvh_stats* o) {

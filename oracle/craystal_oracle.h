@@ -144,6 +144,15 @@ void orc_scene_destroy(orc_scene* s);
  * and sphere lights (center xyz, radius, emission rgb per light). */
 void orc_scene_set_lights(orc_scene* s, const float* env3,
                           const float* spheres7, uint32_t n_spheres);
+/* Diffuse textures: texels = RGBA floats of all textures, descs = (first
+ * texel, width, height) per texture, mat_tex = texture per material or
+ * 0xFFFFFFFF (Core/Texture.cu, Core/Material.h:29-36). */
+void orc_scene_set_textures(orc_scene* s, const float* texels,
+                            const uint32_t* descs, uint32_t n_tex,
+                            const uint32_t* mat_tex, uint32_t n_mats);
+/* TextureView::sample (Core/Texture.cu:15-35) at n coordinates. */
+void orc_texture_sample(const orc_scene* s, uint32_t tex, const float* uv,
+                        uint64_t n, float* rgba);
 void orc_scene_bvh_stats(const orc_scene* s, orc_bvh_stats* out);
 /* Exports nodes (post-order, root last) and the leaf-slot -> primitive map. */
 void orc_scene_bvh_export(const orc_scene* s, orc_bvh_node* nodes,
