@@ -27,6 +27,8 @@ MATERIAL_DTYPE = np.dtype([("diffuse", "<f4", 3), ("specular", "<f4", 3), ("emis
                            ("shininess", "<f4"), ("type", "<u4"), ("flags", "<u4")])
 MESH_DTYPE = np.dtype([("index_offset", "<u4"), ("index_count", "<u4"), ("vertex_offset", "<u4"),
                        ("material_id", "<u4")])
+SPHERE_DTYPE = np.dtype([("center", "<f4", 3), ("radius", "<f4"), ("material", "<u4"), ("pad", "<u4", 3)])
+CR_SPHERE_BIT = 0x80000000
 SPHERE_LIGHT_DTYPE = np.dtype([("center", "<f4", 3), ("radius", "<f4"), ("emission", "<f4", 3), ("pad", "<f4")])
 BVH_NODE_DTYPE = np.dtype([("bmin", "<f4", 3), ("bmax", "<f4", 3), ("is_leaf", "<u4"), ("a", "<u4"), ("b", "<u4")])
 
@@ -126,6 +128,7 @@ SIGNATURES = [
     ("cr_scene_set_camera", ctypes.c_int, [_P, ctypes.POINTER(CrCamera)]),
     ("cr_scene_set_environment", ctypes.c_int, [_P, _P]),
     ("cr_scene_set_sphere_lights", ctypes.c_int, [_P, _P, _U32]),
+    ("cr_scene_set_spheres", ctypes.c_int, [_P, _P, _U32]),
     ("cr_scene_set_diffuse_textures", ctypes.c_int, [_P, ctypes.POINTER(CrTexture), _U32, _P, _U32]),
     ("cr_texture_sample", ctypes.c_int, [_P, _U32, _P, _U64, _P]),
     ("cr_film_clear", ctypes.c_int, [_P]),

@@ -69,14 +69,24 @@ class MeshData:
 
 
 @dataclass
+class SphereData:
+    """Scene/Sphere.h:9-12, with the material the reference's spheres lack."""
+    center: tuple = (0.0, 0.0, 0.0)
+    radius: float = 1.0
+    materialID: int = 0
+
+
+@dataclass
 class SceneData:
     """Scene/Scene.h:40-47.  textureImages: images as HxWxC float arrays
-    (C = 1..4, row 0 first, as Image holds them after loading); spheres are
-    set on the Scene (Scene.set_sphere_lights)."""
+    (C = 1..4, row 0 first, as Image holds them after loading); spheres:
+    analytic spheres with materials (emitting spheres without a material
+    are Scene.set_sphere_lights)."""
     meshes: List[MeshData] = field(default_factory=list)
     materials: List[MaterialData] = field(default_factory=list)
     emissiveIndex: List[int] = field(default_factory=list)
     textureImages: List[np.ndarray] = field(default_factory=list)
+    spheres: List[SphereData] = field(default_factory=list)
 
 
 def texture_texels(image) -> np.ndarray:
@@ -124,7 +134,9 @@ def flatten_scene(data: SceneData):
     return dict(pos=cat(pos, (0, 3), np.float32), nrm=cat(nrm, (0, 3), np.float32), uv=cat(uv, (0, 2), np.float32),
                 idx=cat(idx, (0,), np.uint32), meshes=descs, mats=mats,
                 emissive=np.asarray(data.emissiveIndex, np.uint32),
-                textures=[texture_texels(t) for t in data.textureImages], mat_tex=mat_tex)
+                textures=[texture_texels(t) for t in data.textureImages], mat_tex=mat_tex,
+                sph_geom=np.array([[*sd.center, sd.radius] for sd in data.spheres], np.float32).reshape(-1, 4),
+                sph_mat=np.array([sd.materialID for sd in data.spheres], np.uint32))
 
 
 class Sensor:
@@ -210,6 +222,18 @@ class Scene:
         self._camera: Optional[Camera] = None
         if f["textures"]:
             self.set_diffuse_textures(f["textures"], f["mat_tex"])
+        if len(f["sph_mat"]):
+            self.set_spheres(f["sph_geom"], f["sph_mat"])
+
+    def set_spheres(self, geom, materials):
+        """Analytic spheres: geom n x 4 (centre, radius), a material each;
+        builds their BVH on the GPU."""
+        g = np.asarray(geom, np.float32).reshape(-1, 4)
+        arr = np.zeros(len(g), _lib.SPHERE_DTYPE)
+        arr["center"] = g[:, :3]
+        arr["radius"] = g[:, 3]
+        arr["material"] = np.asarray(materials, np.uint32)
+        check(load().cr_scene_set_spheres(self._h, ptr(arr) if len(arr) else None, len(arr)))
 
     def set_diffuse_textures(self, textures, material_texture):
         """Uploads RGBA texel arrays (HxWx4) and the texture of each material

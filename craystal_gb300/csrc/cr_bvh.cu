@@ -776,6 +776,47 @@ __global__ void kTriBlocks(const float3* __restrict__ pos, const uint32_t* __res
     out[s] = b;
 }
 
+// Sphere records: the centre as centroid, the box centre +- radius widened
+// by a small margin, so that a box's entry distance never exceeds the
+// computed distance of a sphere hit inside it (the quadratic's rounding)
+// and the traversal's culling drops no sphere the linear loop of
+// SceneView::intersect would find.
+__global__ void kPrepSpheres(const float4* __restrict__ geom, uint32_t n, PrimRec* __restrict__ out,
+                             Counters* __restrict__ ctr) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t cl[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, ch[3] = {0u, 0u, 0u};
+    if (i < n) {
+        const float4 g = geom[i];
+        const float ext = g.w * 1.0009765625f + 1e-6f * fmaxf(fmaxf(fabsf(g.x), fabsf(g.y)), fabsf(g.z));
+        PrimRec r;
+        r.c = make_float4(g.x, g.y, g.z, __uint_as_float(i));
+        r.lo = make_float4(g.x - ext, g.y - ext, g.z - ext, 0.0f);
+        r.hi = make_float4(g.x + ext, g.y + ext, g.z + ext, 0.0f);
+        out[i] = r;
+        cl[0] = ch[0] = fenc(g.x);
+        cl[1] = ch[1] = fenc(g.y);
+        cl[2] = ch[2] = fenc(g.z);
+    }
+    for (int k = 0; k < 3; k++) {
+        uint32_t a = warpUmin(cl[k]), b = warpUmax(ch[k]);
+        if (laneId() == 0) {
+            atomicMin(&ctr->cminEnc[k], a);
+            atomicMax(&ctr->cmaxEnc[k], b);
+        }
+    }
+}
+
+__global__ void kSphereBlocks(const float4* __restrict__ geom, const uint32_t* __restrict__ order, uint32_t n,
+                              SphereBlock* __restrict__ out) {
+    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const uint32_t id = order[s];
+    SphereBlock b;
+    b.geom = geom[id];
+    b.meta = make_uint4(id, 0u, 0u, 0u);
+    out[s] = b;
+}
+
 template <class T>
 struct DevBuf {
     T* p = nullptr;
@@ -794,18 +835,28 @@ inline unsigned blocksFor(uint64_t n, unsigned t) { return (unsigned)((n + t - 1
 
 }  // namespace
 
-int buildBvh(cr_scene* s) {
-    const uint32_t N = (uint32_t)s->nt;
-    s->hasRoot = 0;
-    s->stats = cr_bvh_stats{};
-    if (N == 0) return CR_OK;
-    if (s->nt >= 0x7fffffffull) return fail(CR_ERR_UNSUPPORTED, "scene has %llu triangles; the limit is 2^31-1",
-                                            (unsigned long long)s->nt);
-    cudaEvent_t e0, e1;
-    CR_CUDA(cudaEventCreate(&e0));
-    CR_CUDA(cudaEventCreate(&e1));
-    CR_CUDA(cudaEventRecord(e0, 0));
+namespace {
 
+// A built BVH in the traversal layout, plus the build records.
+struct BuiltBvh {
+    NodePair* pairs = nullptr;
+    uint32_t nPairs = 0;
+    uint2* leaves = nullptr;
+    uint32_t nLeaves = 0;
+    uint32_t* order = nullptr;  // leaf slot -> primitive
+    BuildNode* nodes = nullptr;
+    uint32_t nNodes = 0;
+    uint32_t levels = 0;
+    Counters counters{};
+    BuildNode root{};
+};
+
+// The GPU binned-SAH build over N primitive records that prep(rec, ctr)
+// writes (centroid with the primitive id in .w, bounds; centroid bounds
+// into the counters): Morton presort, breadth-first levels for tasks above
+// kTile primitives, a warp per smaller subtree, then the NodePair layout.
+template <class Prep>
+int buildGeneric(uint32_t N, Prep prep, BuiltBvh& out) {
     DevBuf<PrimRec> recA, recB;
     DevBuf<Counters> ctr;
     DevBuf<uint32_t> order, keysIn, keysOut, valsIn, valsOut;
@@ -824,7 +875,7 @@ int buildBvh(cr_scene* s) {
     CR_CUDA(cudaMemcpy(ctr.p, &h0, sizeof(h0), cudaMemcpyHostToDevice));
 
     // 1. centroids, bounds, Morton presort
-    kPrep<<<blocksFor(N, 256), 256>>>(s->pos, s->idx, N, recA.p, ctr.p);
+    prep(recA.p, ctr.p);
     CR_LAUNCH_CHECK();
     CR_CUDA(keysIn.alloc(N));
     CR_CUDA(keysOut.alloc(N));
@@ -951,16 +1002,57 @@ int buildBvh(cr_scene* s) {
     const uint32_t nPairs = nNodes - nLeaves;
     DevBuf<NodePair> pairs;
     DevBuf<uint2> leaves;
-    DevBuf<TriBlock> tris;
     CR_CUDA(pairs.alloc(nPairs));
     CR_CUDA(leaves.alloc(nLeaves));
-    CR_CUDA(tris.alloc(N));
     kLayout<<<blocksFor(nNodes, 256), 256>>>(nodes.p, nNodes, leafPrefix.p, pairs.p, leaves.p);
     CR_LAUNCH_CHECK();
-    kTriBlocks<<<blocksFor(N, 256), 256>>>(s->pos, s->idx, order.p, N, tris.p);
+    CR_CUDA(cudaMemcpy(&out.root, nodes.p, sizeof(BuildNode), cudaMemcpyDeviceToHost));
+    out.pairs = pairs.release();
+    out.nPairs = nPairs;
+    out.leaves = leaves.release();
+    out.nLeaves = nLeaves;
+    out.order = order.release();
+    out.nodes = nodes.release();
+    out.nNodes = nNodes;
+    out.levels = level;
+    out.counters = hc;
+    return CR_OK;
+}
+
+void freeBuilt(BuiltBvh& b) {
+    void* ptrs[] = {b.pairs, b.leaves, b.order, b.nodes};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    b = BuiltBvh{};
+}
+
+}  // namespace
+
+int buildBvh(cr_scene* s) {
+    const uint32_t N = (uint32_t)s->nt;
+    s->hasRoot = 0;
+    s->stats = cr_bvh_stats{};
+    if (N == 0) return CR_OK;
+    if (s->nt >= 0x7fffffffull) return fail(CR_ERR_UNSUPPORTED, "scene has %llu triangles; the limit is 2^31-1",
+                                            (unsigned long long)s->nt);
+    cudaEvent_t e0, e1;
+    CR_CUDA(cudaEventCreate(&e0));
+    CR_CUDA(cudaEventCreate(&e1));
+    CR_CUDA(cudaEventRecord(e0, 0));
+    BuiltBvh b;
+    const float3* pos = s->pos;
+    const uint32_t* idx = s->idx;
+    int rc = buildGeneric(N, [&](PrimRec* rec, Counters* ctr) {
+        kPrep<<<blocksFor(N, 256), 256>>>(pos, idx, N, rec, ctr);
+    }, b);
+    if (rc) {
+        freeBuilt(b);
+        return rc;
+    }
+    DevBuf<TriBlock> tris;
+    CR_CUDA(tris.alloc(N));
+    kTriBlocks<<<blocksFor(N, 256), 256>>>(s->pos, s->idx, b.order, N, tris.p);
     CR_LAUNCH_CHECK();
-    BuildNode root;
-    CR_CUDA(cudaMemcpy(&root, nodes.p, sizeof(root), cudaMemcpyDeviceToHost));
     CR_CUDA(cudaEventRecord(e1, 0));
     CR_CUDA(cudaEventSynchronize(e1));
     float ms = 0.0f;
@@ -968,27 +1060,29 @@ int buildBvh(cr_scene* s) {
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
 
-    s->pairs = pairs.release();
-    s->nPairs = nPairs;
-    s->leaves = leaves.release();
-    s->nLeaves = nLeaves;
+    const BuildNode& root = b.root;
+    s->pairs = b.pairs;
+    s->nPairs = b.nPairs;
+    s->leaves = b.leaves;
+    s->nLeaves = b.nLeaves;
     s->tris = tris.release();
-    s->slotToPrim = order.release();
-    s->buildNodes = nodes.release();
-    s->nBuildNodes = nNodes;
+    s->slotToPrim = b.order;
+    s->buildNodes = b.nodes;
+    s->nBuildNodes = b.nNodes;
     s->hasRoot = 1;
     s->rootMin = mk3(root.lo.x, root.lo.y, root.lo.z);
     s->rootMax = mk3(root.hi.x, root.hi.y, root.hi.z);
     s->rootFlags = degenerateFlags(s->rootMin, s->rootMax);
     s->rootRef = root.info.z ? kLeafBit : 0u;
 
+    const Counters& hc = b.counters;
     cr_bvh_stats& st = s->stats;
-    st.node_count = nNodes;
-    st.leaf_count = nLeaves;
+    st.node_count = b.nNodes;
+    st.leaf_count = b.nLeaves;
     st.max_depth = hc.maxDepth;
     st.max_leaf_size = hc.maxLeafSize;
     st.max_leaf_depth = hc.maxLeafDepth;
-    st.levels = level;
+    st.levels = b.levels;
     st.root_min[0] = root.lo.x;
     st.root_min[1] = root.lo.y;
     st.root_min[2] = root.lo.z;
@@ -996,8 +1090,47 @@ int buildBvh(cr_scene* s) {
     st.root_max[1] = root.hi.y;
     st.root_max[2] = root.hi.z;
     st.build_ms = ms;
-    st.device_bytes = (uint64_t)nPairs * sizeof(NodePair) + (uint64_t)nLeaves * sizeof(uint2) +
+    st.device_bytes = (uint64_t)b.nPairs * sizeof(NodePair) + (uint64_t)b.nLeaves * sizeof(uint2) +
                       (uint64_t)N * sizeof(TriBlock);
+    return CR_OK;
+}
+
+// The sphere BVH over s->sphGeom (s->nSph spheres), replacing any earlier one.
+int buildSphereBvh(cr_scene* s) {
+    void* old[] = {s->sphPairs, s->sphLeaves, s->sphBlocks};
+    for (void* p : old)
+        if (p) cudaFree(p);
+    s->sphPairs = nullptr;
+    s->sphLeaves = nullptr;
+    s->sphBlocks = nullptr;
+    s->sphHasRoot = 0;
+    const uint32_t N = s->nSph;
+    if (N == 0) return CR_OK;
+    BuiltBvh b;
+    const float4* geom = s->sphGeom;
+    int rc = buildGeneric(N, [&](PrimRec* rec, Counters* ctr) {
+        kPrepSpheres<<<blocksFor(N, 256), 256>>>(geom, N, rec, ctr);
+    }, b);
+    if (rc) {
+        freeBuilt(b);
+        return rc;
+    }
+    DevBuf<SphereBlock> blocks;
+    CR_CUDA(blocks.alloc(N));
+    kSphereBlocks<<<blocksFor(N, 256), 256>>>(geom, b.order, N, blocks.p);
+    CR_LAUNCH_CHECK();
+    CR_CUDA(cudaDeviceSynchronize());
+    s->sphPairs = b.pairs;
+    s->sphLeaves = b.leaves;
+    s->sphBlocks = blocks.release();
+    cudaFree(b.order);
+    cudaFree(b.nodes);
+    const BuildNode& root = b.root;
+    s->sphRootMin = mk3(root.lo.x, root.lo.y, root.lo.z);
+    s->sphRootMax = mk3(root.hi.x, root.hi.y, root.hi.z);
+    s->sphRootFlags = degenerateFlags(s->sphRootMin, s->sphRootMax);
+    s->sphRootRef = root.info.z ? kLeafBit : 0u;
+    s->sphHasRoot = 1;
     return CR_OK;
 }
 

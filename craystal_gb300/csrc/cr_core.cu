@@ -91,7 +91,7 @@ void freeScene(cr_scene* s) {
     void* ptrs[] = {s->pos,  s->nrm,      s->uv,         s->idx,        s->primToMesh, s->meshes,
                     s->mats, s->emissive, s->pairs,      s->leaves,     s->tris,       s->slotToPrim,
                     s->buildNodes, s->errFlags, s->filmRgb, s->filmW, s->rayCounter, s->spheres, s->sphereEm,
-                    s->texels, s->texDescs};
+                    s->texels, s->texDescs, s->sphGeom, s->sphMat, s->sphPairs, s->sphLeaves, s->sphBlocks};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     freeCacheBuffers(s->cacheBuffers);
@@ -341,6 +341,37 @@ int cr_scene_set_diffuse_textures(cr_scene* scene, const cr_texture* textures, u
     scene->nTex = nTex;
     if (nMats) CR_CUDA(cudaMemcpy(scene->mats, mats.data(), nMats * sizeof(MaterialGpu), cudaMemcpyHostToDevice));
     return CR_OK;
+}
+
+int cr_scene_set_spheres(cr_scene* scene, const cr_sphere* spheres, uint32_t n) {
+    clearError();
+    if (!scene || (n && !spheres)) return fail(CR_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (n > kMaxSpheres) return fail(CR_ERR_INVALID_ARGUMENT, "%u spheres; the limit is %u", n, kMaxSpheres);
+    std::vector<float4> geom(n);
+    std::vector<uint32_t> mat(n);
+    for (uint32_t i = 0; i < n; i++) {
+        const cr_sphere& x = spheres[i];
+        if (!(x.radius > 0.0f) || !std::isfinite(x.radius) || !std::isfinite(x.center[0]) ||
+            !std::isfinite(x.center[1]) || !std::isfinite(x.center[2]))
+            return fail(CR_ERR_INVALID_ARGUMENT, "sphere %u: centre or radius %g is not finite and positive", i,
+                        x.radius);
+        if (x.material >= scene->nMats)
+            return fail(CR_ERR_INVALID_ARGUMENT, "sphere %u: material %u of %u", i, x.material, scene->nMats);
+        geom[i] = make_float4(x.center[0], x.center[1], x.center[2], x.radius);
+        mat[i] = x.material;
+    }
+    CR_CUDA(cudaSetDevice(scene->device));
+    CR_CUDA(cudaDeviceSynchronize());
+    if (scene->sphGeom) cudaFree(scene->sphGeom);
+    if (scene->sphMat) cudaFree(scene->sphMat);
+    scene->sphGeom = nullptr;
+    scene->sphMat = nullptr;
+    scene->nSph = 0;
+    int rc;
+    if ((rc = upload(&scene->sphGeom, geom.data(), n))) return rc;
+    if ((rc = upload(&scene->sphMat, mat.data(), n))) return rc;
+    scene->nSph = n;
+    return buildSphereBvh(scene);
 }
 
 int cr_film_clear(cr_scene* scene) {

@@ -89,6 +89,25 @@ struct __align__(16) TriBlock {
     float4 e2;
 };
 
+// Sphere block per leaf slot of the sphere BVH (32 B): centre and radius,
+// then (sphere id, 0, 0, 0).
+struct __align__(16) SphereBlock {
+    float4 geom;
+    uint4 meta;
+};
+
+// One binary BVH in the traversal layout: interior NodePairs, the leaf
+// table (first slot, count) and the root (its ref, degenerate-axis flags
+// and box).
+struct BvhView {
+    const NodePair* pairs;
+    const uint2* leaves;
+    uint32_t rootRef;
+    uint32_t rootFlags;
+    float3 rootMin, rootMax;
+    uint32_t hasRoot;
+};
+
 // Node produced by the GPU builder (breadth-first numbering).
 struct __align__(16) BuildNode {
     float4 lo;   // min.xyz
@@ -142,10 +161,19 @@ struct SceneView {
     const float4* sphereEm;        // (emission, 0)
     const float4* texels;          // all diffuse textures, row-major RGBA
     const uint4* texDescs;         // (first texel, width, height, 0) per texture
+    // analytic spheres with materials (Scene/Sphere.cu), in their own BVH
+    BvhView sph;
+    const SphereBlock* sphBlocks;  // per leaf slot
+    const float4* sphGeom;         // per sphere id: centre, radius
+    const uint32_t* sphMat;        // per sphere id: material
 };
 
 constexpr uint32_t kSpherePrim = 0xFFFFFF00u;  // hit ids kSpherePrim + i for sphere light i
 constexpr uint32_t kMaxSphereLights = 64;
+constexpr uint32_t kSphereBit = 0x80000000u;   // hit ids kSphereBit | i for sphere i
+constexpr uint32_t kMaxSpheres = 0x7FFFFF00u;
+
+__host__ __device__ __forceinline__ bool isSphereHit(uint32_t prim) { return prim >= kSphereBit && prim < kSpherePrim; }
 
 }  // namespace cr
 
@@ -197,6 +225,15 @@ struct cr_scene {
     float4* texels = nullptr;
     uint4* texDescs = nullptr;
     uint32_t nTex = 0;
+    // spheres and their BVH
+    uint32_t nSph = 0;
+    float4* sphGeom = nullptr;
+    uint32_t* sphMat = nullptr;
+    cr::NodePair* sphPairs = nullptr;
+    uint2* sphLeaves = nullptr;
+    cr::SphereBlock* sphBlocks = nullptr;
+    uint32_t sphRootRef = 0, sphRootFlags = 0, sphHasRoot = 0;
+    float3 sphRootMin{0, 0, 0}, sphRootMax{0, 0, 0};
 
     cr::SceneView view() const {
         cr::SceneView v;
@@ -224,6 +261,16 @@ struct cr_scene {
         v.sphereEm = sphereEm;
         v.texels = texels;
         v.texDescs = texDescs;
+        v.sph.pairs = sphPairs;
+        v.sph.leaves = sphLeaves;
+        v.sph.rootRef = sphRootRef;
+        v.sph.rootFlags = sphRootFlags;
+        v.sph.rootMin = sphRootMin;
+        v.sph.rootMax = sphRootMax;
+        v.sph.hasRoot = sphHasRoot;
+        v.sphBlocks = sphBlocks;
+        v.sphGeom = sphGeom;
+        v.sphMat = sphMat;
         return v;
     }
 };
@@ -232,6 +279,7 @@ namespace cr {
 
 // implemented in cr_bvh.cu
 int buildBvh(cr_scene* s);
+int buildSphereBvh(cr_scene* s);
 int exportBvh(const cr_scene* s, cr_bvh_node* nodes, uint32_t* primMap);
 // implemented in cr_trace.cu
 int traceClosestDevice(cr_scene* s, const cr_ray* rays, uint64_t n, cr_hit* hits, cudaStream_t st);

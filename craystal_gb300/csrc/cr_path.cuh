@@ -40,7 +40,9 @@ __device__ __forceinline__ void initBsdf(const PathCtx& c, Bsdf& b, const Materi
                                          uint32_t prim, float u, float v) {
     b.init(m, f);
     if (m.tex != CR_NO_TEXTURE) {
-        const float4 t = texSample(c.sc, m.tex, texCoordAt(c.sc, prim, u, v));
+        // a sphere's texture coordinates are its hit's (u, v), Scene/Scene.cu:41
+        const float2 tc = isSphereHit(prim) ? make_float2(u, v) : texCoordAt(c.sc, prim, u, v);
+        const float4 t = texSample(c.sc, m.tex, tc);
         b.kd = sp(t.x, t.y, t.z);
         if (m.type == CR_MATERIAL_PHONG) phongLobeProbs(b.kd, b.ks, kEps, b.dProb, b.sProb);
     }
@@ -73,7 +75,10 @@ __device__ __forceinline__ bool closest(PathCtx& c, float3 o, float3 d, THit& h)
     h.t = INFINITY;
     h.prim = CR_MISS;
     h.u = h.v = 0.0f;
-    bool hit = traverse<false>(c.sc, makeTRay(o, 0.0f, d, INFINITY), h);
+    const TRay r = makeTRay(o, 0.0f, d, INFINITY);
+    bool hit = false;
+    if (c.sc.sph.hasRoot) hit = traverseSpheres<false>(c.sc, r, h);
+    hit |= traverse<false>(c.sc, r, h);
     for (uint32_t i = 0; i < c.sc.nSpheres; i++) {
         const float t = raySphere(o, d, __ldg(c.sc.spheres + i), 0.0f, h.t);
         if (t < h.t) {
@@ -92,7 +97,9 @@ __device__ __forceinline__ bool occluded(PathCtx& c, float3 o, float3 d, float t
         if (raySphere(o, d, __ldg(c.sc.spheres + i), 0.0f, tMax) < INFINITY) return true;
     THit h;
     h.t = INFINITY;
-    return traverse<true>(c.sc, makeTRay(o, 0.0f, d, tMax), h);
+    const TRay r = makeTRay(o, 0.0f, d, tMax);
+    if (c.sc.sph.hasRoot && traverseSpheres<true>(c.sc, r, h)) return true;
+    return traverse<true>(c.sc, r, h);
 }
 
 struct LightSample {
@@ -222,8 +229,10 @@ __device__ __forceinline__ Spec tracePath(PathCtx& c, const CameraGpu& cam, cons
                 radiance = add(radiance, mul(toPathSpec(c.spec, e.x, e.y, e.z), beta));
                 break;
             }
-            const Isect it = makeIsect(sc, ro, rd, h.t, h.u, h.v, h.prim);
-            const MaterialGpu& m = materialOf(sc, h.prim);
+            const bool sphere = isSphereHit(h.prim);
+            const Isect it = sphere ? makeIsectSphere(sc, ro, rd, h.t, h.prim & ~kSphereBit)
+                                    : makeIsect(sc, ro, rd, h.t, h.u, h.v, h.prim);
+            const MaterialGpu& m = sphere ? sc.mats[__ldg(sc.sphMat + (h.prim & ~kSphereBit))] : materialOf(sc, h.prim);
             if (hk.atVertex(depth, it, m, beta, radiance)) break;
             if (m.flags & CR_MATERIAL_EMISSIVE) {
                 radiance = add(radiance, mul(emissionOf(c, m), beta));

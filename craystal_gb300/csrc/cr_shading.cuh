@@ -122,6 +122,19 @@ __device__ __forceinline__ Isect makeIsect(const SceneView& sc, float3 o, float3
     return it;
 }
 
+// createIntersection of a sphere hit (Scene/Scene.cu:43-47): the face and
+// shading normal point from the centre to the hit point.
+__device__ __forceinline__ Isect makeIsectSphere(const SceneView& sc, float3 o, float3 d, float t, uint32_t id) {
+    Isect it;
+    it.posW = add(o, mul(t, d));
+    it.viewW = neg(normalize(d));
+    const float4 g = __ldg(sc.sphGeom + id);
+    it.faceN = normalize(sub(it.posW, mk3(g.x, g.y, g.z)));
+    it.front = dot(it.viewW, it.faceN) > 0.0f;
+    it.frame.build(it.front ? it.faceN : neg(it.faceN));
+    return it;
+}
+
 __device__ __forceinline__ const MaterialGpu& materialOf(const SceneView& sc, uint32_t prim) {
     return sc.mats[sc.meshes[sc.primToMesh[prim]].material_id];
 }

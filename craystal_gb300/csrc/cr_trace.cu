@@ -13,7 +13,11 @@ constexpr int kTraceThreads = 128;
 // One thread per ray.  (A persistent variant that refills the lanes of a
 // warp from a per-warp ray range measured slower on GB300 for this
 // incoherent workload: the lanes' rounds synchronise on the slowest lane.)
-template <bool kAnyHit>
+//
+// kSpheres: the scene has analytic spheres, tested first as
+// SceneView::intersect does (a separate instance keeps the triangle-only
+// kernel free of the sphere code).
+template <bool kAnyHit, bool kSpheres>
 __global__ void __launch_bounds__(kTraceThreads) kTrace(const SceneView sc, const cr_ray* __restrict__ rays,
                                                         uint64_t n, cr_hit* __restrict__ hits,
                                                         uint8_t* __restrict__ occ) {
@@ -26,7 +30,9 @@ __global__ void __launch_bounds__(kTraceThreads) kTrace(const SceneView sc, cons
     h.t = INFINITY;
     h.u = h.v = 0.0f;
     h.prim = CR_MISS;
-    const bool hit = traverse<kAnyHit>(sc, r, h);
+    bool hit = false;
+    if (kSpheres) hit = traverseSpheres<kAnyHit>(sc, r, h);
+    if (!(kAnyHit && hit)) hit |= traverse<kAnyHit>(sc, r, h);
     if (kAnyHit) {
         occ[i] = hit ? 1 : 0;
     } else {
@@ -42,8 +48,13 @@ int launchTrace(cr_scene* s, const cr_ray* rays, uint64_t n, cr_hit* hits, uint8
     const SceneView v = s->view();
     for (uint64_t off = 0; off < n; off += kMaxRaysPerLaunch) {
         const uint64_t m = std::min(n - off, kMaxRaysPerLaunch);
-        kTrace<kAnyHit><<<(unsigned)((m + kTraceThreads - 1) / kTraceThreads), kTraceThreads, 0, st>>>(
-            v, rays + off, m, hits ? hits + off : nullptr, occ ? occ + off : nullptr);
+        const unsigned blocks = (unsigned)((m + kTraceThreads - 1) / kTraceThreads);
+        if (s->sphHasRoot)
+            kTrace<kAnyHit, true><<<blocks, kTraceThreads, 0, st>>>(v, rays + off, m, hits ? hits + off : nullptr,
+                                                                    occ ? occ + off : nullptr);
+        else
+            kTrace<kAnyHit, false><<<blocks, kTraceThreads, 0, st>>>(v, rays + off, m, hits ? hits + off : nullptr,
+                                                                     occ ? occ + off : nullptr);
         CR_LAUNCH_CHECK();
     }
     return CR_OK;

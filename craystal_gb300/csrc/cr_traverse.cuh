@@ -131,48 +131,121 @@ __device__ __forceinline__ void loadTri(const TriBlock* tris, uint32_t slot, flo
 
 constexpr int kStackSize = 32;  // depth <= 20 bounds a near-first stack by 21
 
-// Tests the triangles of leaf `ref` with the closest-hit rule of
-// Scene/Shape.h:26-31.  Returns true when the any-hit query can stop.
+// Leaf tests.  Each returns true when an any-hit query can stop.
+//
+// Triangles: the closest-hit rule of Scene/Shape.h:26-31 on the leaf's
+// slots in order.
 template <bool kAnyHit>
-__device__ __forceinline__ bool leafTest(const SceneView& sc, const TRay& r, THit& h, bool& isHit, uint32_t ref) {
-    const uint2 leaf = __ldg(sc.leaves + (ref & ~kLeafBit));
-    for (uint32_t i = 0; i < leaf.y; ++i) {
-        float3 v0, e1, e2;
-        uint32_t prim;
-        loadTri(sc.tris, leaf.x + i, v0, e1, e2, prim);
-        float t, u, v;
-        if (triTest(v0, e1, e2, r, t, u, v)) {
-            if (t < r.tMin || t > r.tMax) continue;
-            isHit = true;
-            if (kAnyHit) return true;
-            if (t < h.t) {
-                h.t = t;
-                h.u = u;
-                h.v = v;
-                h.prim = prim;
+struct TriLeaf {
+    const uint2* leaves;
+    const TriBlock* tris;
+    __device__ __forceinline__ bool operator()(const TRay& r, THit& h, bool& isHit, uint32_t ref) const {
+        const uint2 leaf = __ldg(leaves + (ref & ~kLeafBit));
+        for (uint32_t i = 0; i < leaf.y; ++i) {
+            float3 v0, e1, e2;
+            uint32_t prim;
+            loadTri(tris, leaf.x + i, v0, e1, e2, prim);
+            float t, u, v;
+            if (triTest(v0, e1, e2, r, t, u, v)) {
+                if (t < r.tMin || t > r.tMax) continue;
+                isHit = true;
+                if (kAnyHit) return true;
+                if (t < h.t) {
+                    h.t = t;
+                    h.u = u;
+                    h.v = v;
+                    h.prim = prim;
+                }
             }
         }
+        return false;
     }
-    return false;
+};
+
+// SphereSOA::intersect (Scene/Sphere.cu:6-38): the nearer root of
+// |o + t d - c|^2 = r^2 inside [tMin, tMax], else the farther one.
+__device__ __forceinline__ bool sphereTest(float4 s, const TRay& r, float& t) {
+    const float3 oc = sub(r.o, mk3(s.x, s.y, s.z));
+    const float a = dot(r.d, r.d);
+    const float b = 2.0f * dot(oc, r.d);
+    const float c = dot(oc, oc) - s.w * s.w;
+    const float disc = b * b - 4.0f * a * c;
+    if (disc < 0.0f) return false;
+    const float sq = sqrtf(disc);
+    float t0 = (-b - sq) / (2.0f * a);
+    float t1 = (-b + sq) / (2.0f * a);
+    if (t0 > t1) {
+        const float x = t0;
+        t0 = t1;
+        t1 = x;
+    }
+    if (t0 < r.tMin || t0 > r.tMax) {
+        if (t1 < r.tMin || t1 > r.tMax) return false;
+        t0 = t1;
+    }
+    t = t0;
+    return true;
 }
 
-// BVHData::intersect (Core/BVH.cu:13-84) for one ray.  h.t must hold the
-// initial closest t (infinity for a fresh RayHit).  Returns whether any
-// triangle was hit inside [tMin, tMax] (not only closer ones), as the
-// reference does.
+// The spherical coordinates a sphere hit reports as its (u, v)
+// (Scene/Sphere.cu:39-49).
+__device__ __forceinline__ float2 sphereUV(float4 s, const TRay& r, float t) {
+    const float3 p = add(r.o, mul(r.d, t));
+    const float3 n = normalize(sub(p, mk3(s.x, s.y, s.z)));
+    const float theta = acosf(-n.y);
+    const float phi = atan2f(-n.z, n.x) + kPi;
+    return make_float2(phi * (0.5f * kInvPi), theta * kInvPi);
+}
+
+// Spheres, tested before the triangles as SceneView::intersect does
+// (Scene/Scene.cu:5-14).  The reference loops over the spheres in index
+// order with the strict closest-hit rule, so of spheres hit at the same t
+// the lowest index wins; the BVH visits them in another order and breaks
+// such ties by index explicitly.
+template <bool kAnyHit>
+struct SphereLeaf {
+    const uint2* leaves;
+    const SphereBlock* blocks;
+    __device__ __forceinline__ bool operator()(const TRay& r, THit& h, bool& isHit, uint32_t ref) const {
+        const uint2 leaf = __ldg(leaves + (ref & ~kLeafBit));
+        for (uint32_t i = 0; i < leaf.y; ++i) {
+            const float4* p = reinterpret_cast<const float4*>(blocks + leaf.x + i);
+            const float4 g = __ldg(p);
+            float t;
+            if (!sphereTest(g, r, t)) continue;
+            isHit = true;
+            if (kAnyHit) return true;
+            const uint32_t id = kSphereBit | __ldg(reinterpret_cast<const uint32_t*>(p + 1));
+            if (t < h.t || (t == h.t && id < h.prim)) {
+                const float2 uv = sphereUV(g, r, t);
+                h.t = t;
+                h.u = uv.x;
+                h.v = uv.y;
+                h.prim = id;
+            }
+        }
+        return false;
+    }
+};
+
+// BVHData::intersect (Core/BVH.cu:13-84) for one ray over one BVH.  h.t
+// must hold the initial closest t (infinity for a fresh RayHit).  Returns
+// whether any primitive was hit inside [tMin, tMax] (not only closer ones),
+// as the reference does.
 //
 // One loop; the entry e being visited lives in registers.  When both
 // children pass, the far one is pushed and the near one becomes e (the
 // reference pushes both and pops the near one at once); an entry taken from
 // the stack is culled at the top of the loop when its distance is beyond
 // the closest hit, as at Core/BVH.cu:34-36.
-template <bool kAnyHit>
-__device__ __forceinline__ bool traverse(const SceneView& sc, const TRay& r, THit& h) {
+template <bool kAnyHit, class Leaf>
+__device__ __forceinline__ bool traverseBvh(const BvhView& bv, uint32_t* errFlags, const Leaf& leaf, const TRay& r,
+                                            THit& h) {
     float tr;
-    if (!sc.hasRoot || !boxTest(sc.rootMin, sc.rootMax, sc.rootFlags, r, tr)) return false;
+    if (!bv.hasRoot || !boxTest(bv.rootMin, bv.rootMax, bv.rootFlags, r, tr)) return false;
     uint2 stack[kStackSize];
     int sp = 0;
-    uint2 e = make_uint2(sc.rootRef, __float_as_uint(0.0f));
+    uint2 e = make_uint2(bv.rootRef, __float_as_uint(0.0f));
     bool have = true, isHit = false;
     while (have) {
         if (__uint_as_float(e.y) > h.t) {
@@ -181,12 +254,12 @@ __device__ __forceinline__ bool traverse(const SceneView& sc, const TRay& r, THi
             continue;
         }
         if (e.x & kLeafBit) {
-            if (leafTest<kAnyHit>(sc, r, h, isHit, e.x)) return true;
+            if (leaf(r, h, isHit, e.x)) return true;
             have = sp > 0;
             if (have) e = stack[--sp];
             continue;
         }
-        const float4* np = reinterpret_cast<const float4*>(sc.pairs + e.x);
+        const float4* np = reinterpret_cast<const float4*>(bv.pairs + e.x);
         const float4 p0 = __ldg(np), p1 = __ldg(np + 1), p2 = __ldg(np + 2);
         const uint4 ref = __ldg(reinterpret_cast<const uint4*>(np + 3));
         float lt = INFINITY, rt = INFINITY;
@@ -198,7 +271,7 @@ __device__ __forceinline__ bool traverse(const SceneView& sc, const TRay& r, THi
             // near = the child the reference pushes last: right when lt > rt
             const bool rightNear = lt > rt;
             if (sp >= kStackSize) {  // unreachable for depth <= 20; never overrun
-                atomicOr(sc.errFlags, kErrStackOverflow);
+                atomicOr(errFlags, kErrStackOverflow);
                 break;
             }
             stack[sp++] = rightNear ? make_uint2(ref.x, __float_as_uint(lt)) : make_uint2(ref.y, __float_as_uint(rt));
@@ -213,6 +286,21 @@ __device__ __forceinline__ bool traverse(const SceneView& sc, const TRay& r, THi
         }
     }
     return isHit;
+}
+
+// The triangle BVH of the scene.
+template <bool kAnyHit>
+__device__ __forceinline__ bool traverse(const SceneView& sc, const TRay& r, THit& h) {
+    const BvhView bv{sc.pairs, sc.leaves, sc.rootRef, sc.rootFlags, sc.rootMin, sc.rootMax, sc.hasRoot};
+    const TriLeaf<kAnyHit> leaf{sc.leaves, sc.tris};
+    return traverseBvh<kAnyHit>(bv, sc.errFlags, leaf, r, h);
+}
+
+// The sphere BVH of the scene (no spheres: no work).
+template <bool kAnyHit>
+__device__ __forceinline__ bool traverseSpheres(const SceneView& sc, const TRay& r, THit& h) {
+    const SphereLeaf<kAnyHit> leaf{sc.sph.leaves, sc.sphBlocks};
+    return traverseBvh<kAnyHit>(sc.sph, sc.errFlags, leaf, r, h);
 }
 
 }  // namespace cr

@@ -192,6 +192,27 @@ int cr_scene_set_environment(cr_scene* scene, const float radiance[3]);
 int cr_scene_set_sphere_lights(cr_scene* scene, const cr_sphere_light* lights,
                                uint32_t n);
 
+/* ---- analytic spheres ----
+ * SceneData::spheres (Scene/Scene.h:41, Scene/Sphere.h:9-12) with a
+ * material each (the reference's spheres have none and are shaded through
+ * the triangle-mesh tables).  Intersection is SphereSOA::intersect
+ * (Scene/Sphere.cu:6-52): the nearer root inside [tMin, tMax], else the
+ * farther one; (u, v) = (phi / 2pi, theta / pi) of the hit normal, which
+ * is also the texture coordinate.  Spheres are tested before the triangles
+ * (SceneView::intersect, Scene/Scene.cu:5-14), through a BVH of their own
+ * built on the GPU; a sphere hit reports prim = CR_SPHERE_BIT | index.
+ * Emissive spheres are reached by BSDF sampling only (next-event estimation
+ * samples the emissive triangles).  A new call replaces all spheres. */
+#define CR_SPHERE_BIT 0x80000000u
+typedef struct {
+    float center[3];
+    float radius;
+    uint32_t material;
+    uint32_t pad[3];
+} cr_sphere;
+int cr_scene_set_spheres(cr_scene* scene, const cr_sphere* spheres,
+                         uint32_t n);
+
 /* ---- diffuse textures ----
  * SceneData::textureImages + MaterialData::diffuseHandle and the
  * hasDiffuseTexture flag (Scene/Scene.h:45, Core/Material.h:29-36): a

@@ -68,6 +68,7 @@ def lib():
             "orc_scene_destroy": (None, [_P]),
             "orc_scene_set_lights": (None, [_P, _P, _P, U32]),
             "orc_scene_set_textures": (None, [_P, _P, _P, U32, _P, U32]),
+            "orc_scene_set_spheres": (None, [_P, _P, _P, U32]),
             "orc_texture_sample": (None, [_P, U32, _P, U64, _P]),
             "orc_scene_bvh_stats": (None, [_P, ctypes.POINTER(OrcStats)]),
             "orc_scene_bvh_export": (None, [_P, _P, _P]),
@@ -167,6 +168,15 @@ class OracleScene:
                                     _p(flat["emissive"]), len(flat["emissive"]))
         if flat.get("textures"):
             self.set_textures(flat["textures"], flat["mat_tex"])
+        if len(flat.get("sph_mat", ())):
+            self.set_spheres(flat["sph_geom"], flat["sph_mat"])
+
+    def set_spheres(self, geom, mats):
+        """Spheres: geom n x 4 (centre, radius), mats n material ids."""
+        g = np.ascontiguousarray(geom, np.float32).reshape(-1, 4)
+        m = np.ascontiguousarray(mats, np.uint32)
+        self._sph = (g, m)
+        lib().orc_scene_set_spheres(self.h, _p(g), _p(m), len(m))
 
     def set_textures(self, textures, material_texture):
         """RGBA texel arrays (HxWx4) and the texture of each material (0xFFFFFFFF = none)."""

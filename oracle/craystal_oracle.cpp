@@ -361,6 +361,9 @@ struct orc_scene {
     std::vector<float> texels;         // RGBA per texel, all textures
     std::vector<uint32_t> texDescs;    // first texel, width, height per texture
     std::vector<uint32_t> matTex;      // texture per material or 0xFFFFFFFF
+    // analytic spheres (Scene/Sphere.h:9-12) with a material each
+    std::vector<float> sph;            // centre xyz, radius per sphere
+    std::vector<uint32_t> sphMat;
     uint32_t maxDepth = 0, maxLeaf = 0, maxLeafDepth = 0;
 };
 
@@ -550,6 +553,59 @@ static inline bool intersectShape(const orc_scene& s, uint32_t prim, const Ray& 
     return true;
 }
 
+// SphereSOA::intersect, Scene/Sphere.cu:6-52
+constexpr uint32_t kSphereBit = 0x80000000u;
+
+static bool sphereIntersect(const float* g, const Ray& ray, float& hitT, float& u, float& v) {
+    const V3 center{g[0], g[1], g[2]};
+    const float radius = g[3];
+    const V3 oc = ray.o - center;
+    const float a = dot(ray.d, ray.d);
+    const float b = 2.0f * dot(oc, ray.d);
+    const float c = dot(oc, oc) - radius * radius;
+    const float disc = b * b - 4.0f * a * c;
+    if (disc < 0) return false;
+    const float sq = std::sqrt(disc);
+    float t0 = (-b - sq) / (2.0f * a);
+    float t1 = (-b + sq) / (2.0f * a);
+    if (t0 > t1) std::swap(t0, t1);
+    if (t0 < ray.tMin || t0 > ray.tMax) {
+        if (t1 < ray.tMin || t1 > ray.tMax) return false;
+        t0 = t1;
+    }
+    hitT = t0;
+    const V3 p = ray.o + ray.d * hitT;
+    const V3 n = normalize(p - center);
+    const float theta = std::acos(-n.y);
+    const float phi = std::atan2(-n.z, n.x) + kPi;
+    u = phi * (0.5f * kInvPi);
+    v = theta * kInvPi;
+    return true;
+}
+
+// The sphere loop of SceneView::intersect (Scene/Scene.cu:7-9) with the rule
+// of intersectShape (Scene/Shape.h:16-37).
+static bool spheresIntersect(const orc_scene& s, const Ray& ray, Hit& h) {
+    bool any = false;
+    for (size_t i = 0; i < s.sphMat.size(); i++) {
+        float t, u, v;
+        if (!sphereIntersect(&s.sph[4 * i], ray, t, u, v)) continue;
+        if (t < ray.tMin || t > ray.tMax) continue;
+        any = true;
+        const uint32_t prim = kSphereBit | (uint32_t)i;
+        if (t < h.t) {
+            h.t = t;
+            h.u = u;
+            h.v = v;
+            h.prim = prim;
+            h.tie = false;
+        } else if (t == h.t && prim != h.prim) {
+            h.tie = true;
+        }
+    }
+    return any;
+}
+
 // Core/BVH.cu:13-84
 static bool bvhIntersect(const orc_scene& s, const Ray& ray, Hit& h, Counters* c) {
     float unused;
@@ -713,6 +769,16 @@ static Intersection createIntersection(const orc_scene& s, const Ray& ray, const
     VertexData vd = tri.interpolate(w);
     V3 sn = normalize(vd.n);
     return Intersection(posW, fn, sn, viewW, vd.uv);
+}
+
+// createIntersection of a sphere hit (Scene/Scene.cu:43-47), with the
+// sphere's own material (the reference reads a mesh table here)
+static Intersection sphereIntersection(const orc_scene& s, const Ray& ray, const Hit& h) {
+    const float* g = &s.sph[4 * (size_t)(h.prim & ~kSphereBit)];
+    V3 posW = ray.o + h.t * ray.d;
+    V3 viewW = -normalize(ray.d);
+    V3 fn = normalize(posW - V3{g[0], g[1], g[2]});
+    return Intersection(posW, fn, fn, viewW, V2{h.u, h.v});
 }
 
 // ---------------------------------------------------------------------------
@@ -994,7 +1060,8 @@ struct Tracer {
     Spectral spec;
     bool intersect(const Ray& r, Hit& h) {
         rays++;
-        bool hit = bvhIntersect(s, r, h, nullptr);
+        bool hit = spheresIntersect(s, r, h);
+        hit |= bvhIntersect(s, r, h, nullptr);
         for (size_t i = 0; i < s.spheres.size() / 7; i++) {
             float t = raySphere(r, &s.spheres[7 * i], 0.0f, h.t);
             if (t < h.t) {
@@ -1010,6 +1077,7 @@ struct Tracer {
         for (size_t i = 0; i < s.spheres.size() / 7; i++)
             if (raySphere(r, &s.spheres[7 * i], 0.0f, r.tMax) < kFltInf) return true;
         Hit h;
+        if (spheresIntersect(s, r, h)) return true;
         return bvhIntersect(s, r, h, nullptr);
     }
 };
@@ -1152,8 +1220,9 @@ static S3 tracePath(Tracer& tr, const CameraData& cam, const orc_integrator_conf
                 radiance = radiance + toPathSpec(tr.spec, sl + 4) * beta;
                 break;
             }
-            Intersection it = createIntersection(s, ray, h);
-            const orc_material& m = materialOf(s, h.prim);
+            const bool sphere = h.prim >= kSphereBit && h.prim < kSpherePrim;
+            Intersection it = sphere ? sphereIntersection(s, ray, h) : createIntersection(s, ray, h);
+            const orc_material& m = sphere ? s.mats[s.sphMat[h.prim & ~kSphereBit]] : materialOf(s, h.prim);
             if (m.flags & 1u) {
                 radiance = radiance + toPathSpec(tr.spec, m.emission) * beta;
                 break;
@@ -1162,7 +1231,8 @@ static S3 tracePath(Tracer& tr, const CameraData& cam, const orc_integrator_conf
             // reflectance is the texture sampled at the hit
             const float* diffuse = m.diffuse;
             float texRgb[3];
-            const uint32_t mid = s.meshes[s.primToMesh[h.prim]].material_id;
+            const uint32_t mid =
+                sphere ? s.sphMat[h.prim & ~kSphereBit] : s.meshes[s.primToMesh[h.prim]].material_id;
             if (mid < s.matTex.size() && s.matTex[mid] != 0xFFFFFFFFu) {
                 const RGBA t = texSample(s, s.matTex[mid], it.uv);
                 texRgb[0] = t.v[0];
@@ -1330,6 +1400,11 @@ void orc_scene_set_lights(orc_scene* s, const float* env3, const float* spheres7
     s->spheres.assign(spheres7, spheres7 + 7 * (size_t)n_spheres);
 }
 
+void orc_scene_set_spheres(orc_scene* s, const float* geom4, const uint32_t* mats, uint32_t n) {
+    s->sph.assign(geom4, geom4 + 4 * (size_t)n);
+    s->sphMat.assign(mats, mats + n);
+}
+
 void orc_scene_set_textures(orc_scene* s, const float* texels, const uint32_t* descs, uint32_t n_tex,
                             const uint32_t* mat_tex, uint32_t n_mats) {
     size_t total = 0;
@@ -1384,7 +1459,9 @@ void orc_trace_closest(const orc_scene* s, const orc_ray* rays, uint64_t n, orc_
         uint64_t tc = 0;
         for (uint64_t i = b; i < e; i++) {
             Hit h;
-            bool hit = bvhIntersect(*s, toRay(rays[i]), h, counters ? &c : nullptr);
+            const Ray r = toRay(rays[i]);
+            bool hit = spheresIntersect(*s, r, h);  // SceneView::intersect: spheres, then the BVH
+            hit |= bvhIntersect(*s, r, h, counters ? &c : nullptr);
             if (hit) hits[i] = {h.prim, h.t, h.u, h.v};
             else hits[i] = {0xFFFFFFFFu, kFltInf, 0.0f, 0.0f};
             if (ties) ties[i] = (hit && h.tie) ? 1 : 0;
@@ -1407,7 +1484,8 @@ void orc_trace_occluded(const orc_scene* s, const orc_ray* rays, uint64_t n, uin
     parallelFor(n, threads, [&](uint64_t b, uint64_t e) {
         for (uint64_t i = b; i < e; i++) {
             Hit h;
-            occ[i] = bvhIntersect(*s, toRay(rays[i]), h, nullptr) ? 1 : 0;
+            const Ray r = toRay(rays[i]);
+            occ[i] = (spheresIntersect(*s, r, h) || bvhIntersect(*s, r, h, nullptr)) ? 1 : 0;
         }
     });
 }
@@ -1419,6 +1497,7 @@ void orc_trace_brute(const orc_scene* s, const orc_ray* rays, uint64_t n, orc_hi
             Ray r = toRay(rays[i]);
             Hit h;
             bool any = false;
+            any |= spheresIntersect(*s, r, h);
             for (uint32_t p = 0; p < nt; p++) any |= intersectShape(*s, p, r, h);
             if (any) hits[i] = {h.prim, h.t, h.u, h.v};
             else hits[i] = {0xFFFFFFFFu, kFltInf, 0.0f, 0.0f};

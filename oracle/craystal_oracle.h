@@ -144,6 +144,11 @@ void orc_scene_destroy(orc_scene* s);
  * and sphere lights (center xyz, radius, emission rgb per light). */
 void orc_scene_set_lights(orc_scene* s, const float* env3,
                           const float* spheres7, uint32_t n_spheres);
+/* Analytic spheres (centre xyz, radius per sphere; a material each),
+ * intersected before the triangles (Scene/Scene.cu:5-14); hits report
+ * prim = 0x80000000 | index. */
+void orc_scene_set_spheres(orc_scene* s, const float* geom4,
+                           const uint32_t* mats, uint32_t n);
 /* Diffuse textures: texels = RGBA floats of all textures, descs = (first
  * texel, width, height) per texture, mat_tex = texture per material or
  * 0xFFFFFFFF (Core/Texture.cu, Core/Material.h:29-36). */
