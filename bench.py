@@ -193,6 +193,39 @@ def cornell_extra(torch):
             "rays_per_path": round(rays / paths, 3)}
 
 
+def wavefront_extra(torch):
+    """The two schedules of the plain path tracer on the same paths: the
+    megakernel (one thread per pixel, all bounces in registers) and the
+    wavefront variant (extend, sort by material, shade per bounce).  Scenes:
+    the Cornell box 256x256 and a 500k-triangle box-clutter scene 512x512,
+    16 spp, max depth 10, NEE + MIS."""
+    from craystal_gb300 import scenes
+    from craystal_gb300.api import PathTraceIntegrator, Scene
+    out = {}
+    for name, (data, cam) in (("cornell_256", scenes.cornell_box(seed=0, width=256, height=256)),
+                              ("box_clutter_500k_512", scenes.box_clutter(3, 500000, 512, 512))):
+        sc = Scene(data)
+        sc.setCamera(cam)
+        cfg = PathTraceIntegrator.Configs(maxDepth=10, rrThreshold=0.05, useMIS=True)
+        row = {}
+        for label, wf in (("megakernel", False), ("wavefront", True)):
+            integ = PathTraceIntegrator(cfg, compat=False, wavefront=wf)
+            integ.dispatch(sc, 4, readback=False)
+            torch.cuda.synchronize()
+            sc.film_clear()
+            t = time.perf_counter()
+            integ.dispatch(sc, 16, readback=False)
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t
+            paths = cam.sensor.size[0] * cam.sensor.size[1] * 16
+            row[label] = {"ms": round(dt * 1e3, 2), "Mpaths_s": round(paths / dt / 1e6, 2),
+                          "Mrays_s": round(sc.render_ray_count() / dt / 1e6, 1)}
+        row["wavefront_over_megakernel_time"] = round(row["wavefront"]["ms"] / row["megakernel"]["ms"], 3)
+        out[name] = row
+        sc.close()
+    return out
+
+
 def cache_extra(torch, res=512):
     """Equal-time relMSE of the radiance-cache integrator against the plain
     path tracer on the Cornell box (res x res, max depth 8, NEE + MIS).  The
@@ -399,6 +432,7 @@ def run_ours(args):
         extra["restated_reference_kernel"] = restated_reference_extra(torch, sc, flatten_scene(data), d_rays, N_RAYS,
                                                                       d_hits)
         extra["path_tracer"] = cornell_extra(torch)
+        extra["wavefront_vs_megakernel"] = wavefront_extra(torch)
         extra["radiance_cache_equal_time"] = cache_extra(torch, args.cache_res)
         extra["batched_scenes"] = batch_extra(torch, args.batch_scenes)
 
@@ -443,6 +477,8 @@ def run_only(args):
     cg.load().cr_set_device(0)
     if args.only == "path_tracer":
         r = cornell_extra(torch)
+    elif args.only == "wavefront":
+        r = wavefront_extra(torch)
     elif args.only == "radiance_cache":
         r = cache_extra(torch, args.cache_res)
     else:
@@ -460,7 +496,7 @@ def main():
     ap.add_argument("--skip-extra", action="store_true", help="omit the path-tracer figures")
     ap.add_argument("--rays", type=int, default=N_RAYS, help="rays per step (profiling a smaller case)")
     ap.add_argument("--tris", type=int, default=N_TRIS, help="triangles (profiling a smaller case)")
-    ap.add_argument("--only", choices=["path_tracer", "radiance_cache", "batched_scenes"],
+    ap.add_argument("--only", choices=["path_tracer", "wavefront", "radiance_cache", "batched_scenes"],
                     help="run one secondary workload alone and print its figures (profiling)")
     ap.add_argument("--cache-res", type=int, default=512, help="radiance-cache workload resolution")
     ap.add_argument("--batch-scenes", type=int, default=64, help="scenes in the batched workload")

@@ -360,10 +360,12 @@ class PathTraceIntegrator:
             self.rrThreshold = rrThreshold
             self.useMIS = useMIS
 
-    def __init__(self, configs: "PathTraceIntegrator.Configs" = None, compat: bool = True, spectral: bool = False):
+    def __init__(self, configs: "PathTraceIntegrator.Configs" = None, compat: bool = True, spectral: bool = False,
+                 wavefront: bool = False):
         self.configs = configs or PathTraceIntegrator.Configs()
         self.compat = compat
         self.spectral = spectral  # hero-wavelength spectral rendering (an extension)
+        self.wavefront = wavefront  # the wavefront schedule with a material sort per bounce
 
     def device_config(self) -> CrIntegratorConfig:
         c = CrIntegratorConfig()
@@ -372,7 +374,7 @@ class PathTraceIntegrator:
         else:
             c.max_depth, c.rr_threshold = self.configs.maxDepth, self.configs.rrThreshold
         c.use_mis = 1 if self.configs.useMIS else 0
-        c.flags = 1 if self.spectral else 0
+        c.flags = (1 if self.spectral else 0) | (2 if self.wavefront else 0)
         return c
 
     def dispatch(self, scene: Scene, spp: int, first_sample: int = 0, stream: int = 0, readback: bool = True):

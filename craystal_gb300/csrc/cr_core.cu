@@ -413,7 +413,11 @@ int cr_render(cr_scene* scene, const cr_integrator_config* cfg, uint32_t spp, ui
     if (!scene || !cfg) return fail(CR_ERR_INVALID_ARGUMENT, "NULL argument");
     if (!scene->hasCamera) return fail(CR_ERR_INVALID_ARGUMENT, "scene has no camera; call cr_scene_set_camera");
     if (cfg->max_depth > 1024) return fail(CR_ERR_INVALID_ARGUMENT, "max_depth %u", cfg->max_depth);
+    if (cfg->flags & ~(CR_RENDER_SPECTRAL | CR_RENDER_WAVEFRONT))
+        return fail(CR_ERR_INVALID_ARGUMENT, "unknown render flags 0x%x", cfg->flags);
     CR_CUDA(cudaSetDevice(scene->device));
+    if (cfg->flags & CR_RENDER_WAVEFRONT)
+        return renderWavefront(scene, cfg, spp, first_sample, static_cast<cudaStream_t>(stream));
     return renderDevice(scene, cfg, spp, first_sample, static_cast<cudaStream_t>(stream));
 }
 

@@ -285,6 +285,8 @@ int exportBvh(const cr_scene* s, cr_bvh_node* nodes, uint32_t* primMap);
 int traceClosestDevice(cr_scene* s, const cr_ray* rays, uint64_t n, cr_hit* hits, cudaStream_t st);
 int traceOccludedDevice(cr_scene* s, const cr_ray* rays, uint64_t n, uint8_t* occ, cudaStream_t st);
 // implemented in cr_render.cu
+int renderWavefront(cr_scene* s, const cr_integrator_config* cfg, uint32_t spp, uint32_t first,
+                    cudaStream_t stream);
 int renderDevice(cr_scene* s, const cr_integrator_config* cfg, uint32_t spp, uint32_t first,
                  cudaStream_t st);
 int resolveFilm(cr_scene* s, float* rgbHost);

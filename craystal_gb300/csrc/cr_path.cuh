@@ -208,69 +208,89 @@ struct NoHooks {
     }
 };
 
+// One bounce of pathTraceKernel<useMIS> after its closest-hit query
+// (Core/Integrator.cu:170-225): h is the query's hit (h.prim == CR_MISS for
+// a miss).  Updates the ray, throughput and radiance; returns false when the
+// path ends.  Shared by the megakernel (tracePath) and the wavefront shade
+// stage (cr_wavefront.cu), so both consume the sampler identically.
+template <class Hooks>
+__device__ __forceinline__ bool shadeBounce(PathCtx& c, const Params& p, Sampler& smp, uint32_t depth, const THit& h,
+                                            float3& ro, float3& rd, Spec& beta, Spec& radiance, Hooks& hk) {
+    const SceneView& sc = c.sc;
+    bool terminate = false;
+    if (h.prim != CR_MISS) {
+        if (h.prim >= kSpherePrim) {  // a sphere light (extension)
+            const float4 e = __ldg(sc.sphereEm + (h.prim - kSpherePrim));
+            radiance = add(radiance, mul(toPathSpec(c.spec, e.x, e.y, e.z), beta));
+            return false;
+        }
+        const bool sphere = isSphereHit(h.prim);
+        const Isect it = sphere ? makeIsectSphere(sc, ro, rd, h.t, h.prim & ~kSphereBit)
+                                : makeIsect(sc, ro, rd, h.t, h.u, h.v, h.prim);
+        const MaterialGpu& m = sphere ? sc.mats[__ldg(sc.sphMat + (h.prim & ~kSphereBit))] : materialOf(sc, h.prim);
+        if (hk.atVertex(depth, it, m, beta, radiance)) return false;
+        if (m.flags & CR_MATERIAL_EMISSIVE) {
+            radiance = add(radiance, mul(emissionOf(c, m), beta));
+            return false;
+        }
+        Bsdf bsdf;
+        initBsdf(c, bsdf, m, it.frame, h.prim, h.u, h.v);
+        if (p.useMIS) {
+            radiance = add(radiance, mul(evalMIS(c, it, bsdf, smp), beta));
+        } else {
+            const LightSample ls = sampleLight(c, it, bsdf, smp);
+            if (ls.pdf > 0.0f) radiance = add(radiance, divs(divs(mul(ls.weight, beta), ls.pdf), ls.selectPdf));
+        }
+        float3 wi;
+        float pdf = 0.0f;
+        const Spec f = bsdf.sampleEvaluate(smp.next2D(), it.viewW, wi, pdf);
+        if (pdf <= 0.0f) return false;
+        beta = mul(beta, divs(f, pdf));
+        ro = offsetRayOrigin(it.posW, it.orientedFaceNormal());
+        rd = wi;
+    } else {
+        // a miss ends the path (Core/Integrator.cu:205-207), after
+        // collecting the constant environment when there is one (extension)
+        if (sc.env.x > 0.0f || sc.env.y > 0.0f || sc.env.z > 0.0f)
+            radiance = add(radiance, mul(toPathSpec(c.spec, sc.env.x, sc.env.y, sc.env.z), beta));
+        terminate = true;
+    }
+    if (smp.next1D() < p.rrThreshold) terminate = true;
+    if (terminate) return false;
+    if (depth > 5) {
+        float q = smax(p.rrThreshold, 1.0f - maxValue(beta));
+        q = q < 0.0f ? 0.0f : (1.0f < q ? 1.0f : q);
+        if (smp.next1D() < q) return false;
+        beta = divs(beta, 1.0f - q);
+    }
+    return true;
+}
+
+// The camera ray of a (pixel, sample index): the sampler's first 2D draw
+// jitters the film position (Core/Integrator.cu:150-156).
+__device__ __forceinline__ void cameraRay(const CameraGpu& cam, Sampler& smp, uint32_t x, uint32_t y, float2& pixel,
+                                          float3& ro, float3& rd) {
+    const float2 j = smp.next2D();
+    pixel = make_float2((float)x + j.x, (float)y + j.y);
+    ro = cam.pos;
+    rd = cameraDir(cam, pixel);
+}
+
 // pathTraceKernel body for one (pixel, sample index).
 template <class Hooks>
 __device__ __forceinline__ Spec tracePath(PathCtx& c, const CameraGpu& cam, const Params& p, uint32_t x, uint32_t y,
                                           uint32_t si, float2& pixel, Hooks& hk) {
-    const SceneView& sc = c.sc;
     c.spec = makeSpectralPath(p.spectral != 0, x, y, si);
     Sampler smp(x, y, si);
-    const float2 j = smp.next2D();
-    pixel = make_float2((float)x + j.x, (float)y + j.y);
-    float3 ro = cam.pos;
-    float3 rd = cameraDir(cam, pixel);
+    float3 ro, rd;
+    cameraRay(cam, smp, x, y, pixel, ro, rd);
     Spec radiance = sp(0.0f), beta = sp(1.0f);
     for (uint32_t depth = 0; depth < p.maxDepth; depth++) {
-        bool terminate = false;
         THit h;
-        if (closest(c, ro, rd, h)) {
-            if (h.prim >= kSpherePrim) {  // a sphere light (extension)
-                const float4 e = __ldg(sc.sphereEm + (h.prim - kSpherePrim));
-                radiance = add(radiance, mul(toPathSpec(c.spec, e.x, e.y, e.z), beta));
-                break;
-            }
-            const bool sphere = isSphereHit(h.prim);
-            const Isect it = sphere ? makeIsectSphere(sc, ro, rd, h.t, h.prim & ~kSphereBit)
-                                    : makeIsect(sc, ro, rd, h.t, h.u, h.v, h.prim);
-            const MaterialGpu& m = sphere ? sc.mats[__ldg(sc.sphMat + (h.prim & ~kSphereBit))] : materialOf(sc, h.prim);
-            if (hk.atVertex(depth, it, m, beta, radiance)) break;
-            if (m.flags & CR_MATERIAL_EMISSIVE) {
-                radiance = add(radiance, mul(emissionOf(c, m), beta));
-                break;
-            }
-            Bsdf bsdf;
-            initBsdf(c, bsdf, m, it.frame, h.prim, h.u, h.v);
-            if (p.useMIS) {
-                radiance = add(radiance, mul(evalMIS(c, it, bsdf, smp), beta));
-            } else {
-                const LightSample ls = sampleLight(c, it, bsdf, smp);
-                if (ls.pdf > 0.0f) radiance = add(radiance, divs(divs(mul(ls.weight, beta), ls.pdf), ls.selectPdf));
-            }
-            float3 wi;
-            float pdf = 0.0f;
-            const Spec f = bsdf.sampleEvaluate(smp.next2D(), it.viewW, wi, pdf);
-            if (pdf <= 0.0f) break;
-            beta = mul(beta, divs(f, pdf));
-            ro = offsetRayOrigin(it.posW, it.orientedFaceNormal());
-            rd = wi;
-        } else {
-            // a miss ends the path (Core/Integrator.cu:205-207), after
-            // collecting the constant environment when there is one (extension)
-            if (sc.env.x > 0.0f || sc.env.y > 0.0f || sc.env.z > 0.0f)
-                radiance = add(radiance, mul(toPathSpec(c.spec, sc.env.x, sc.env.y, sc.env.z), beta));
-            terminate = true;
-        }
-        if (smp.next1D() < p.rrThreshold) terminate = true;
-        if (terminate) break;
-        if (depth > 5) {
-            float q = smax(p.rrThreshold, 1.0f - maxValue(beta));
-            q = q < 0.0f ? 0.0f : (1.0f < q ? 1.0f : q);
-            if (smp.next1D() < q) break;
-            beta = divs(beta, 1.0f - q);
-        }
+        closest(c, ro, rd, h);
+        if (!shadeBounce(c, p, smp, depth, h, ro, rd, beta, radiance, hk)) break;
     }
     return radiance;
 }
-
 
 }  // namespace cr

@@ -20,6 +20,14 @@ namespace cr {
 // ---------------------------------------------------------------------------
 struct Sampler {
     uint32_t state, inc;
+    Sampler() = default;
+    // a sampler resumed from a saved (state, inc)
+    __device__ __forceinline__ static Sampler resume(uint32_t state, uint32_t inc) {
+        Sampler s;
+        s.state = state;
+        s.inc = inc;
+        return s;
+    }
     __device__ __forceinline__ Sampler(uint32_t px, uint32_t py, uint32_t sampleIndex) {
         state = px * 2654435761u + py * 1597334677u + sampleIndex;
         inc = px * 1234567891u + py * 987654321u + 1u;

@@ -11,6 +11,30 @@
 
 namespace cr {
 
+// SensorData::addSample (Core/Sensor.cu:19-43) straight into the global
+// film: the radius-1 triangle filter around the film position pix.
+__device__ __forceinline__ void splatGlobal(const CameraGpu& cam, float2 pix, const Spec& L, float* __restrict__ filmRgb,
+                                            float* __restrict__ filmW) {
+    if (isnan(L.r) || isnan(L.g) || isnan(L.b) || isinf(L.r) || isinf(L.g) || isinf(L.b)) return;
+    int xa = (int)floorf(pix.x - 1.0f), ya = (int)floorf(pix.y - 1.0f);
+    int xb = (int)ceilf(pix.x + 1.0f), yb = (int)ceilf(pix.y + 1.0f);
+    xa = max(xa, 0);
+    ya = max(ya, 0);
+    xb = min(xb, (int)cam.width - 1);
+    yb = min(yb, (int)cam.height - 1);
+    for (int yy = ya; yy <= yb; yy++)
+        for (int xx = xa; xx <= xb; xx++) {
+            const float dx = pix.x - ((float)xx + 0.5f), dy = pix.y - ((float)yy + 0.5f);
+            const float w = smax(0.0f, 1.0f - fabsf(dx)) * smax(0.0f, 1.0f - fabsf(dy));
+            if (w == 0.0f) continue;
+            const size_t pi = (size_t)yy * cam.width + xx;
+            atomicAdd(filmRgb + 3 * pi + 0, L.r * w);
+            atomicAdd(filmRgb + 3 * pi + 1, L.g * w);
+            atomicAdd(filmRgb + 3 * pi + 2, L.b * w);
+            atomicAdd(filmW + pi, w);
+        }
+}
+
 template <int TW>
 struct TileSmem {
     float film[(TW + 2) * (TW + 2) * 4];

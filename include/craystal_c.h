@@ -106,6 +106,12 @@ typedef struct {
  * is upsampled to spectra, the film receives linear sRGB white-balanced so
  * that a flat spectrum renders as in RGB. */
 #define CR_RENDER_SPECTRAL 1u
+/* The wavefront variant of the integrator (an alternative schedule of the
+ * same paths): live paths are kept in HBM between bounces; each bounce is a
+ * traversal launch, a sort of the hits by material and a shading launch.
+ * Per path the arithmetic and the sampler sequence are the megakernel's, so
+ * the film is the same up to the order of its float additions. */
+#define CR_RENDER_WAVEFRONT 2u
 
 /* Binary BVH node in the reference's layout (Core/BVH.h:17-30): nodes in
  * post-order with the root last; leaf: (a, b) = (first leaf slot, count),
