@@ -226,6 +226,33 @@ def wavefront_extra(torch):
     return out
 
 
+def cache_frames_extra(torch, res=512, frames=32):
+    """The cached integrator's frames alone (Cornell res x res, max depth 8,
+    NEE + MIS, training every frame) after 16 warm-up frames: ms per frame
+    and per plain sample of the same image, for profiling."""
+    from craystal_gb300 import scenes
+    from craystal_gb300.api import CachedPathTraceIntegrator, PathTraceIntegrator, Scene
+    data, cam = scenes.cornell_box(seed=0, width=res, height=res)
+    sc = Scene(data)
+    sc.setCamera(cam)
+    cfg = PathTraceIntegrator.Configs(maxDepth=8, rrThreshold=0.05, useMIS=True)
+    integ = CachedPathTraceIntegrator(cfg, train_every=16)
+    integ.dispatch(sc, 16, first_sample=5_000_000, readback=False)
+    plain = PathTraceIntegrator(cfg, compat=False)
+    plain.dispatch(sc, 4, readback=False)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    integ.dispatch(sc, frames, readback=False)
+    torch.cuda.synchronize()
+    tc = time.perf_counter() - t
+    t = time.perf_counter()
+    plain.dispatch(sc, frames, readback=False)
+    torch.cuda.synchronize()
+    tp = time.perf_counter() - t
+    return {"config": f"cornell {res}x{res}, max depth 8", "frames": frames,
+            "cache_ms_per_frame": round(1e3 * tc / frames, 3), "plain_ms_per_spp": round(1e3 * tp / frames, 3)}
+
+
 def cache_extra(torch, res=512):
     """Equal-time relMSE of the radiance-cache integrator against the plain
     path tracer on the Cornell box (res x res, max depth 8, NEE + MIS).  The
@@ -481,6 +508,8 @@ def run_only(args):
         r = wavefront_extra(torch)
     elif args.only == "radiance_cache":
         r = cache_extra(torch, args.cache_res)
+    elif args.only == "cache_frames":
+        r = cache_frames_extra(torch, args.cache_res)
     else:
         r = batch_extra(torch, args.batch_scenes)
     print(json.dumps({args.only: r}), flush=True)
@@ -496,7 +525,7 @@ def main():
     ap.add_argument("--skip-extra", action="store_true", help="omit the path-tracer figures")
     ap.add_argument("--rays", type=int, default=N_RAYS, help="rays per step (profiling a smaller case)")
     ap.add_argument("--tris", type=int, default=N_TRIS, help="triangles (profiling a smaller case)")
-    ap.add_argument("--only", choices=["path_tracer", "wavefront", "radiance_cache", "batched_scenes"],
+    ap.add_argument("--only", choices=["path_tracer", "wavefront", "radiance_cache", "cache_frames", "batched_scenes"],
                     help="run one secondary workload alone and print its figures (profiling)")
     ap.add_argument("--cache-res", type=int, default=512, help="radiance-cache workload resolution")
     ap.add_argument("--batch-scenes", type=int, default=64, help="scenes in the batched workload")

@@ -361,11 +361,12 @@ class PathTraceIntegrator:
             self.useMIS = useMIS
 
     def __init__(self, configs: "PathTraceIntegrator.Configs" = None, compat: bool = True, spectral: bool = False,
-                 wavefront: bool = False):
+                 wavefront: Optional[bool] = None):
         self.configs = configs or PathTraceIntegrator.Configs()
         self.compat = compat
         self.spectral = spectral  # hero-wavelength spectral rendering (an extension)
-        self.wavefront = wavefront  # the wavefront schedule with a material sort per bounce
+        # schedule: True = wavefront (material sort per bounce), False = megakernel, None = the library's choice
+        self.wavefront = wavefront
 
     def device_config(self) -> CrIntegratorConfig:
         c = CrIntegratorConfig()
@@ -374,7 +375,7 @@ class PathTraceIntegrator:
         else:
             c.max_depth, c.rr_threshold = self.configs.maxDepth, self.configs.rrThreshold
         c.use_mis = 1 if self.configs.useMIS else 0
-        c.flags = (1 if self.spectral else 0) | (2 if self.wavefront else 0)
+        c.flags = (1 if self.spectral else 0) | {None: 0, True: 2, False: 4}[self.wavefront]
         return c
 
     def dispatch(self, scene: Scene, spp: int, first_sample: int = 0, stream: int = 0, readback: bool = True):
@@ -449,8 +450,9 @@ class CachedPathTraceIntegrator(PathTraceIntegrator):
     (cr_render_cached)."""
 
     def __init__(self, configs=None, compat=False, query_vertex=1, train_every=16, train_samples=65536,
-                 train_steps=1, cache: "RadianceCache" = None):
-        super().__init__(configs or PathTraceIntegrator.Configs(), compat)
+                 train_steps=1, cache: "RadianceCache" = None, wavefront: Optional[bool] = None):
+        # schedule: the wavefront unless wavefront=False (the megakernel form)
+        super().__init__(configs or PathTraceIntegrator.Configs(), compat, wavefront=wavefront)
         from ._lib import CrCacheConfig, CrCacheStats
         self.cache = cache or RadianceCache()
         self.cc = CrCacheConfig(query_vertex, train_every, train_samples, train_steps, 0)

@@ -27,6 +27,7 @@
 #include "cr_internal.cuh"
 #include "cr_mlp.cuh"
 #include "cr_path.cuh"
+#include "cr_wavefront.cuh"
 
 namespace cr {
 namespace {
@@ -197,6 +198,107 @@ __global__ void kSplatCached(const SampleRec* __restrict__ samples, const float*
     }
 }
 
+// The cached integrator on the wavefront schedule (cr_wavefront.cuh).  The
+// megakernel form above keeps a warp busy until its slowest path ends, and
+// one training path in `train_every` runs to full depth, so nearly every
+// warp of rendering paths (which stop at the query vertex) waits for one;
+// here the short paths leave the queue after their query and only the
+// training paths keep bouncing.  Per path the estimator, the sampler
+// sequence, the queries and the training records are the megakernel's.
+struct CachedMode;
+
+struct WfCacheHooks {
+    const CachedMode* m;
+    bool train;
+    uint32_t q, slot, nRec;
+    __device__ __forceinline__ bool atVertex(uint32_t depth, const Isect& it, const MaterialGpu& mat, const Spec& b,
+                                             const Spec& radiance);
+};
+
+struct CachedMode {
+    using Hooks = WfCacheHooks;
+    CacheParams cp;
+    uint32_t width;
+    float* qIn;
+    float* qBeta;
+    uint32_t* qCount;
+    float* recIn;      // per training path slot: kMaxRecords x 7 inputs
+    float* recBeta;    // kMaxRecords x 3
+    float* recBefore;  // kMaxRecords x 3
+    uint32_t* slotCount;
+    uint32_t slotCap;
+    float* tIn;
+    float* tTarget;
+    uint32_t* tCount;
+    SampleRec* samples;
+
+    __device__ __forceinline__ Hooks hooks(const WfState& st, uint32_t k, const uint4& meta) const {
+        const uint4 a = st.aux[k];
+        return Hooks{this, cp.trainEvery > 0 && hash3(meta.x, meta.y, meta.z) % cp.trainEvery == 0, a.x, a.y, a.z};
+    }
+    __device__ __forceinline__ void keep(const WfState& st, uint32_t k, const Hooks& h) const {
+        st.aux[k] = make_uint4(h.q, h.slot, h.nRec, 0u);
+    }
+    __device__ __forceinline__ void end(const WfState&, uint32_t, const uint4& meta, const PathCtx&, const Spec& L,
+                                        float2 pix, const Hooks& h) const {
+        SampleRec rec;
+        rec.a = make_float4(L.r, L.g, L.b, pix.x);
+        rec.b = make_float4(pix.y, __uint_as_float(h.q), 0.0f, 0.0f);
+        samples[(size_t)meta.y * width + meta.x] = rec;
+        if (!h.train || h.slot >= slotCap) return;
+        const size_t r0 = (size_t)h.slot * kMaxRecords;
+        for (uint32_t r = 0; r < h.nRec; r++) {
+            const size_t ri = r0 + r;
+            const Spec be = sp(recBeta[ri * 3 + 0], recBeta[ri * 3 + 1], recBeta[ri * 3 + 2]);
+            const Spec d = sub(L, sp(recBefore[ri * 3 + 0], recBefore[ri * 3 + 1], recBefore[ri * 3 + 2]));
+            const Spec t = Spec{be.r > 0.0f ? d.r / be.r : 0.0f, be.g > 0.0f ? d.g / be.g : 0.0f,
+                                be.b > 0.0f ? d.b / be.b : 0.0f};
+            if (!finite3(t) || maxValue(be) <= 0.0f || maxValue(t) > kMaxTarget) continue;
+            const uint32_t idx = atomicAdd(tCount, 1u);
+            if (idx >= cp.trainCap) break;
+            for (int j = 0; j < 7; j++) tIn[(size_t)idx * 7 + j] = recIn[ri * 7 + j];
+            tTarget[(size_t)idx * 3 + 0] = t.r;
+            tTarget[(size_t)idx * 3 + 1] = t.g;
+            tTarget[(size_t)idx * 3 + 2] = t.b;
+        }
+    }
+};
+
+// TrainHooks / QueryHooks with their state in the path's aux record.
+__device__ __forceinline__ bool WfCacheHooks::atVertex(uint32_t depth, const Isect& it, const MaterialGpu& mat,
+                                                       const Spec& b, const Spec& radiance) {
+    if (train) {
+        if (depth >= 1 && nRec < kMaxRecords) {
+            if (slot == CR_MISS) slot = atomicAdd(m->slotCount, 1u);
+            if (slot < m->slotCap) {
+                const size_t ri = (size_t)slot * kMaxRecords + nRec;
+                float f[7];
+                features(m->cp, it, mat, f);
+                for (int j = 0; j < 7; j++) m->recIn[ri * 7 + j] = f[j];
+                m->recBeta[ri * 3 + 0] = b.r;
+                m->recBeta[ri * 3 + 1] = b.g;
+                m->recBeta[ri * 3 + 2] = b.b;
+                m->recBefore[ri * 3 + 0] = radiance.r;
+                m->recBefore[ri * 3 + 1] = radiance.g;
+                m->recBefore[ri * 3 + 2] = radiance.b;
+                nRec++;
+            }
+        }
+        return false;
+    }
+    if (depth != m->cp.queryVertex) return false;
+    if (finite3(b) && maxValue(b) > 0.0f) {
+        float f[7];
+        features(m->cp, it, mat, f);
+        q = atomicAdd(m->qCount, 1u);
+        for (int j = 0; j < 7; j++) m->qIn[(size_t)q * 7 + j] = f[j];
+        m->qBeta[(size_t)q * 3 + 0] = b.r;
+        m->qBeta[(size_t)q * 3 + 1] = b.g;
+        m->qBeta[(size_t)q * 3 + 2] = b.b;
+    }
+    return true;
+}
+
 }  // namespace
 
 // Per-scene buffers of the cached integrator (sized for the film).
@@ -209,13 +311,18 @@ struct CacheBuffers {
     float* qOut = nullptr;
     float* tIn = nullptr;
     float* tTarget = nullptr;
-    uint32_t* counters = nullptr;  // [0] queries, [1] training records
+    uint32_t* counters = nullptr;  // [0] queries, [1] training records, [2] training path slots
+    uint32_t slotCap = 0;          // training paths with records (wavefront form)
+    float* recIn = nullptr;
+    float* recBeta = nullptr;
+    float* recBefore = nullptr;
 };
 
 void freeCacheBuffers(void* p) {
     CacheBuffers* b = static_cast<CacheBuffers*>(p);
     if (!b) return;
-    void* ptrs[] = {b->samples, b->qIn, b->qBeta, b->qOut, b->tIn, b->tTarget, b->counters};
+    void* ptrs[] = {b->samples, b->qIn, b->qBeta, b->qOut, b->tIn, b->tTarget, b->counters, b->recIn, b->recBeta,
+                    b->recBefore};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     delete b;
@@ -223,10 +330,10 @@ void freeCacheBuffers(void* p) {
 
 namespace {
 
-int ensureCacheBuffers(cr_scene* s, uint32_t trainCap, CacheBuffers** out) {
+int ensureCacheBuffers(cr_scene* s, uint32_t trainCap, uint32_t slotCap, CacheBuffers** out) {
     const uint64_t px = (uint64_t)s->cam.width * s->cam.height;
     CacheBuffers* b = static_cast<CacheBuffers*>(s->cacheBuffers);
-    if (b && b->pixels == px && b->trainCap >= trainCap) {
+    if (b && b->pixels == px && b->trainCap >= trainCap && b->slotCap >= slotCap) {
         *out = b;
         return CR_OK;
     }
@@ -242,7 +349,13 @@ int ensureCacheBuffers(cr_scene* s, uint32_t trainCap, CacheBuffers** out) {
     CR_CUDA(cudaMalloc(&b->qOut, px * 3 * sizeof(float)));
     CR_CUDA(cudaMalloc(&b->tIn, (size_t)trainCap * kMlpInputs * sizeof(float)));
     CR_CUDA(cudaMalloc(&b->tTarget, (size_t)trainCap * 3 * sizeof(float)));
-    CR_CUDA(cudaMalloc(&b->counters, 2 * sizeof(uint32_t)));
+    CR_CUDA(cudaMalloc(&b->counters, 3 * sizeof(uint32_t)));
+    b->slotCap = slotCap;
+    if (slotCap) {
+        CR_CUDA(cudaMalloc(&b->recIn, (size_t)slotCap * kMaxRecords * kMlpInputs * sizeof(float)));
+        CR_CUDA(cudaMalloc(&b->recBeta, (size_t)slotCap * kMaxRecords * 3 * sizeof(float)));
+        CR_CUDA(cudaMalloc(&b->recBefore, (size_t)slotCap * kMaxRecords * 3 * sizeof(float)));
+    }
     *out = b;
     return CR_OK;
 }
@@ -252,9 +365,7 @@ int ensureCacheBuffers(cr_scene* s, uint32_t trainCap, CacheBuffers** out) {
 int renderCached(cr_scene* s, const cr_integrator_config* cfg, const cr_cache_config* cc, MlpState* mlp,
                  uint32_t frames, uint32_t first, cudaStream_t st, cr_cache_stats* stats) {
     const uint32_t trainCap = cc->train_samples ? cc->train_samples : 65536u;
-    CacheBuffers* b = nullptr;
-    int rc = ensureCacheBuffers(s, trainCap, &b);
-    if (rc) return rc;
+    const bool wavefront = !(cfg->flags & CR_RENDER_MEGAKERNEL);
     CacheParams cp;
     float3 mn = s->rootMin, mx = s->rootMax;
     if (cc->scene_max[0] > cc->scene_min[0]) {
@@ -272,6 +383,19 @@ int renderCached(cr_scene* s, const cr_integrator_config* cfg, const cr_cache_co
     cp.trainEvery = cc->train_every ? cc->train_every
                                     : (uint32_t)std::max<uint64_t>(1, (px * 3 + trainCap / 2) / trainCap);
     cp.trainCap = trainCap;
+    // training paths of a frame: px / trainEvery on average (the hash picks
+    // them); room for four times that, beyond which a path keeps no records
+    const uint32_t slotCap =
+        wavefront ? (uint32_t)std::min<uint64_t>(px, 4 * (px / cp.trainEvery) + 4096) : 0u;
+    CacheBuffers* b = nullptr;
+    int rc = ensureCacheBuffers(s, trainCap, slotCap, &b);
+    if (rc) return rc;
+    WfBuffers* wb = nullptr;
+    const uint32_t waveCap = (uint32_t)std::min<uint64_t>(px, kWaveCap);
+    if (wavefront) {
+        rc = ensureWavefrontBuffers(s, waveCap, s->nMats + 2, wb);
+        if (rc) return rc;
+    }
     Params p;
     p.maxDepth = cfg->max_depth;
     p.rrThreshold = cfg->rr_threshold;
@@ -286,10 +410,20 @@ int renderCached(cr_scene* s, const cr_integrator_config* cfg, const cr_cache_co
     uint32_t lastTrain = 0;
     for (uint32_t f = 0; f < frames; f++) {
         p.first = first + f;
-        CR_CUDA(cudaMemsetAsync(b->counters, 0, 2 * sizeof(uint32_t), st));
-        kRenderCached<<<grid, block, 0, st>>>(s->view(), s->cam, p, cp, b->samples, b->qIn, b->qBeta, b->counters,
-                                              b->tIn, b->tTarget, b->counters + 1, s->rayCounter);
-        CR_LAUNCH_CHECK();
+        CR_CUDA(cudaMemsetAsync(b->counters, 0, 3 * sizeof(uint32_t), st));
+        if (wavefront) {
+            const CachedMode mode{cp,         W,         b->qIn,    b->qBeta,     b->counters, b->recIn,
+                                  b->recBeta, b->recBefore, b->counters + 2, slotCap, b->tIn, b->tTarget,
+                                  b->counters + 1, b->samples};
+            for (uint64_t base = 0; base < px; base += waveCap) {
+                rc = runWave(s, p, mode, wb, base, (uint32_t)std::min<uint64_t>(waveCap, px - base), st);
+                if (rc) return rc;
+            }
+        } else {
+            kRenderCached<<<grid, block, 0, st>>>(s->view(), s->cam, p, cp, b->samples, b->qIn, b->qBeta,
+                                                  b->counters, b->tIn, b->tTarget, b->counters + 1, s->rayCounter);
+            CR_LAUNCH_CHECK();
+        }
         uint32_t cnt[2];
         CR_CUDA(cudaMemcpyAsync(cnt, b->counters, sizeof(cnt), cudaMemcpyDeviceToHost, st));
         CR_CUDA(cudaStreamSynchronize(st));

@@ -95,6 +95,7 @@ void freeScene(cr_scene* s) {
     for (void* p : ptrs)
         if (p) cudaFree(p);
     freeCacheBuffers(s->cacheBuffers);
+    freeWavefrontBuffers(s->wfBuffers);
     for (int k = 0; k < 2; k++) {
         if (s->stageRays[k]) cudaFree(s->stageRays[k]);
         if (s->stageHits[k]) cudaFree(s->stageHits[k]);
@@ -413,11 +414,15 @@ int cr_render(cr_scene* scene, const cr_integrator_config* cfg, uint32_t spp, ui
     if (!scene || !cfg) return fail(CR_ERR_INVALID_ARGUMENT, "NULL argument");
     if (!scene->hasCamera) return fail(CR_ERR_INVALID_ARGUMENT, "scene has no camera; call cr_scene_set_camera");
     if (cfg->max_depth > 1024) return fail(CR_ERR_INVALID_ARGUMENT, "max_depth %u", cfg->max_depth);
-    if (cfg->flags & ~(CR_RENDER_SPECTRAL | CR_RENDER_WAVEFRONT))
+    if (cfg->flags & ~(CR_RENDER_SPECTRAL | CR_RENDER_WAVEFRONT | CR_RENDER_MEGAKERNEL))
         return fail(CR_ERR_INVALID_ARGUMENT, "unknown render flags 0x%x", cfg->flags);
+    if ((cfg->flags & CR_RENDER_WAVEFRONT) && (cfg->flags & CR_RENDER_MEGAKERNEL))
+        return fail(CR_ERR_INVALID_ARGUMENT, "CR_RENDER_WAVEFRONT and CR_RENDER_MEGAKERNEL exclude each other");
     CR_CUDA(cudaSetDevice(scene->device));
-    if (cfg->flags & CR_RENDER_WAVEFRONT)
-        return renderWavefront(scene, cfg, spp, first_sample, static_cast<cudaStream_t>(stream));
+    const uint64_t paths = (uint64_t)scene->cam.width * scene->cam.height * spp;
+    const bool wavefront =
+        (cfg->flags & CR_RENDER_WAVEFRONT) || (!(cfg->flags & CR_RENDER_MEGAKERNEL) && paths >= (1u << 16));
+    if (wavefront) return renderWavefront(scene, cfg, spp, first_sample, static_cast<cudaStream_t>(stream));
     return renderDevice(scene, cfg, spp, first_sample, static_cast<cudaStream_t>(stream));
 }
 

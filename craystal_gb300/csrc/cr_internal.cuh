@@ -216,6 +216,8 @@ struct cr_scene {
     uint64_t stageCap = 0;
     // buffers of the radiance-cache integrator (cr_cache.cu), created on first use
     void* cacheBuffers = nullptr;
+    // path state of the wavefront integrator (cr_wavefront.cu), created on first use
+    void* wfBuffers = nullptr;
     // lights beyond the reference
     float3 env{0, 0, 0};
     uint32_t nSpheres = 0;
@@ -287,6 +289,7 @@ int traceOccludedDevice(cr_scene* s, const cr_ray* rays, uint64_t n, uint8_t* oc
 // implemented in cr_render.cu
 int renderWavefront(cr_scene* s, const cr_integrator_config* cfg, uint32_t spp, uint32_t first,
                     cudaStream_t stream);
+void freeWavefrontBuffers(void* p);
 int renderDevice(cr_scene* s, const cr_integrator_config* cfg, uint32_t spp, uint32_t first,
                  cudaStream_t st);
 int resolveFilm(cr_scene* s, float* rgbHost);

@@ -68,6 +68,7 @@ __device__ __forceinline__ float raySphere(float3 o, float3 d, float4 s, float t
     return INFINITY;
 }
 
+
 // SceneView::intersect (Scene/Scene.cu:5-14): the BVH, then the sphere
 // lights (an extension) under the closest-hit rule.
 __device__ __forceinline__ bool closest(PathCtx& c, float3 o, float3 d, THit& h) {

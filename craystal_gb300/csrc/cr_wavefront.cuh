@@ -1,0 +1,373 @@
+// cr_wavefront.cuh -- the wavefront variant of pathTraceKernel<useMIS>
+// (Core/Integrator.cu:142-227): paths live in HBM between bounces and each
+// bounce is three launches over the live paths,
+//   extend   the closest-hit query of every live path (a pure traversal
+//            kernel), with the hit's material as a sort key;
+//   sort     the live paths by material (a counting sort: block-aggregated
+//            histogram, scan, block-aggregated scatter), so that the warps of
+//            the shade stage run one BSDF and touch one material's data;
+//   shade    the bounce after the query (shadeBounce, the megakernel's own
+//            code: next-event estimation and MIS with their shadow and BSDF
+//            rays, continuation sampling, Russian roulette); surviving paths
+//            are appended to the next bounce's queue, ending paths go to the
+//            integrator's Mode (the plain tracer splats them into the film,
+//            cr_wavefront.cu; the cached one records them, cr_cache.cu).
+// Per path the arithmetic and the sampler's sequence are the megakernel's,
+// so the plain film equals cr_render's up to the order of its float adds.
+//
+// Path state (structure of arrays, 16-byte records):
+//   ro    (origin, film x)        rd    (direction, film y)
+//   beta  (throughput, depth)     rad   (radiance, 0)
+//   meta  (x, y, sample index, sampler state)   inc (sampler increment)
+//   hit   (prim, t, u, v) of the extend stage
+//   aux   per-path state of the Mode's hooks
+// Paths run in waves of at most kWaveCap (the whole image x spp when it
+// fits), 128 bytes each.  Every stage reads the live-path count from device
+// memory, so a render is a fixed sequence of launches on one stream: no
+// host synchronisation, and it can be captured into a CUDA graph.
+
+#pragma once
+
+#include "cr_internal.cuh"
+#include "cr_math.cuh"
+#include "cr_path.cuh"
+#include "cr_shading.cuh"
+#include "cr_tile.cuh"
+#include "cr_traverse.cuh"
+
+namespace cr {
+
+// Path state and queues, kept with the scene and grown on demand.
+struct WfBuffers {
+    uint32_t cap = 0, keyCap = 0;
+    float4 *ro = nullptr, *rd = nullptr, *beta = nullptr, *rad = nullptr, *hit = nullptr;
+    uint4 *meta = nullptr, *aux = nullptr;
+    uint32_t *inc = nullptr, *qa = nullptr, *qb = nullptr, *keys = nullptr, *sorted = nullptr, *counts = nullptr,
+             *hist = nullptr;
+    void release() {
+        void* ptrs[] = {ro, rd, beta, rad, hit, meta, aux, inc, qa, qb, keys, sorted, counts, hist};
+        for (void* q : ptrs)
+            if (q) cudaFree(q);
+        *this = WfBuffers{};
+    }
+};
+
+template <class T>
+inline cudaError_t wfAlloc(T*& p, size_t n) {
+    return cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T));
+}
+
+inline int ensureWavefrontBuffers(cr_scene* s, uint32_t cap, uint32_t nKeys, WfBuffers*& out) {
+    WfBuffers* b = static_cast<WfBuffers*>(s->wfBuffers);
+    if (!b) {
+        b = new WfBuffers;
+        s->wfBuffers = b;
+    }
+    if (b->cap < cap || b->keyCap < nKeys) {
+        CR_CUDA(cudaDeviceSynchronize());  // earlier renders may still use the old buffers
+        b->release();
+        CR_CUDA(wfAlloc(b->ro, cap));
+        CR_CUDA(wfAlloc(b->rd, cap));
+        CR_CUDA(wfAlloc(b->beta, cap));
+        CR_CUDA(wfAlloc(b->rad, cap));
+        CR_CUDA(wfAlloc(b->hit, cap));
+        CR_CUDA(wfAlloc(b->meta, cap));
+        CR_CUDA(wfAlloc(b->aux, cap));
+        CR_CUDA(wfAlloc(b->inc, cap));
+        CR_CUDA(wfAlloc(b->qa, cap));
+        CR_CUDA(wfAlloc(b->qb, cap));
+        CR_CUDA(wfAlloc(b->keys, cap));
+        CR_CUDA(wfAlloc(b->sorted, cap));
+        CR_CUDA(wfAlloc(b->counts, 2));
+        CR_CUDA(wfAlloc(b->hist, nKeys));
+        b->cap = cap;
+        b->keyCap = nKeys;
+    }
+    out = b;
+    return CR_OK;
+}
+
+namespace {
+
+
+constexpr uint32_t kWaveCap = 1u << 21;
+constexpr int kWfThreads = 128;
+
+struct WfState {
+    float4* ro;
+    float4* rd;
+    float4* beta;
+    float4* rad;
+    uint4* meta;
+    uint32_t* inc;
+    float4* hit;
+    uint4* aux;  // per-path state of the integrator's hooks
+};
+
+__device__ __forceinline__ void addRays(unsigned long long* counter, uint32_t rays) {
+    for (int o = 16; o > 0; o >>= 1) rays += __shfl_xor_sync(0xffffffffu, rays, o);
+    if ((threadIdx.x & 31) == 0 && rays) atomicAdd(counter, (unsigned long long)rays);
+}
+
+// Camera rays of paths [base, base + n) of the wave sequence: path k is
+// pixel k mod (w h) at sample p.first + k / (w h).
+__global__ void __launch_bounds__(kWfThreads) kWfInit(const CameraGpu cam, const Params p, WfState st, uint64_t base,
+                                                      uint32_t n, uint32_t* __restrict__ queue) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint64_t k = base + i;
+    const uint64_t area = (uint64_t)cam.width * cam.height;
+    const uint32_t px = (uint32_t)(k % area);
+    const uint32_t x = px % cam.width, y = px / cam.width;
+    const uint32_t si = p.first + (uint32_t)(k / area);
+    Sampler smp(x, y, si);
+    float2 pix;
+    float3 ro, rd;
+    cameraRay(cam, smp, x, y, pix, ro, rd);
+    st.ro[i] = make_float4(ro.x, ro.y, ro.z, pix.x);
+    st.rd[i] = make_float4(rd.x, rd.y, rd.z, pix.y);
+    st.beta[i] = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(0u));
+    st.rad[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    st.meta[i] = make_uint4(x, y, si, smp.state);
+    st.inc[i] = smp.inc;
+    st.aux[i] = make_uint4(CR_MISS, CR_MISS, 0u, 0u);
+    queue[i] = i;
+}
+
+// The closest-hit query of every live path; key = the material to shade
+// (nMats for a miss, nMats + 1 for a sphere light).
+__global__ void __launch_bounds__(kWfThreads) kWfExtend(const SceneView sc, WfState st,
+                                                        const uint32_t* __restrict__ queue,
+                                                        const uint32_t* __restrict__ count, uint32_t nMats,
+                                                        uint32_t* __restrict__ keys,
+                                                        unsigned long long* __restrict__ rayCounter) {
+    const uint32_t n = *count;
+    if (blockIdx.x * blockDim.x >= n) return;  // the whole block is past the live paths
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    PathCtx c{sc, 0u, SpectralPath{}};
+    if (i < n) {
+        const uint32_t k = queue[i];
+        const float4 o = st.ro[k], d = st.rd[k];
+        THit h;
+        closest(c, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), h);
+        st.hit[k] = make_float4(__uint_as_float(h.prim), h.t, h.u, h.v);
+        uint32_t key;
+        if (h.prim == CR_MISS) key = nMats;
+        else if (h.prim >= kSpherePrim) key = nMats + 1;
+        else if (isSphereHit(h.prim)) key = __ldg(sc.sphMat + (h.prim & ~kSphereBit));
+        else key = sc.meshes[sc.primToMesh[h.prim]].material_id;
+        keys[i] = key;
+    }
+    addRays(rayCounter, c.rays);
+}
+
+// Counting sort of the live paths by key.  Keys beyond kSmemKeys bins fall
+// back to global atomics per path.
+constexpr uint32_t kSmemKeys = 2048;
+
+__global__ void __launch_bounds__(kWfThreads) kWfHistogram(const uint32_t* __restrict__ keys,
+                                                           const uint32_t* __restrict__ count, uint32_t nKeys,
+                                                           uint32_t* __restrict__ hist) {
+    __shared__ uint32_t local[kSmemKeys];
+    const uint32_t n = *count;
+    if (blockIdx.x * blockDim.x >= n) return;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool smem = nKeys <= kSmemKeys;
+    if (smem) {
+        for (uint32_t k = threadIdx.x; k < nKeys; k += blockDim.x) local[k] = 0;
+        __syncthreads();
+        if (i < n) atomicAdd(&local[keys[i]], 1u);
+        __syncthreads();
+        for (uint32_t k = threadIdx.x; k < nKeys; k += blockDim.x)
+            if (local[k]) atomicAdd(&hist[k], local[k]);
+    } else if (i < n) {
+        atomicAdd(&hist[keys[i]], 1u);
+    }
+}
+
+// Exclusive scan of the histogram into bin offsets (one block).
+__global__ void __launch_bounds__(1024) kWfScan(uint32_t* __restrict__ hist, uint32_t nKeys) {
+    __shared__ uint32_t partial[1024];
+    const uint32_t per = (nKeys + blockDim.x - 1) / blockDim.x;
+    const uint32_t b = threadIdx.x * per, e = min(nKeys, b + per);
+    uint32_t sum = 0;
+    for (uint32_t k = b; k < e; k++) sum += hist[k];
+    partial[threadIdx.x] = sum;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t run = 0;
+        for (uint32_t t = 0; t < blockDim.x; t++) {
+            const uint32_t v = partial[t];
+            partial[t] = run;
+            run += v;
+        }
+    }
+    __syncthreads();
+    uint32_t run = partial[threadIdx.x];
+    for (uint32_t k = b; k < e; k++) {
+        const uint32_t v = hist[k];
+        hist[k] = run;
+        run += v;
+    }
+}
+
+// Scatter: each block reserves its range in every bin once, then places its
+// paths with shared-memory counters.
+__global__ void __launch_bounds__(kWfThreads) kWfScatter(const uint32_t* __restrict__ keys,
+                                                         const uint32_t* __restrict__ queue,
+                                                         const uint32_t* __restrict__ count, uint32_t nKeys,
+                                                         uint32_t* __restrict__ offsets,
+                                                         uint32_t* __restrict__ sorted) {
+    __shared__ uint32_t local[kSmemKeys];
+    const uint32_t n = *count;
+    if (blockIdx.x * blockDim.x >= n) return;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (nKeys <= kSmemKeys) {
+        for (uint32_t k = threadIdx.x; k < nKeys; k += blockDim.x) local[k] = 0;
+        __syncthreads();
+        uint32_t key = 0, rank = 0;
+        if (i < n) {
+            key = keys[i];
+            rank = atomicAdd(&local[key], 1u);
+        }
+        __syncthreads();
+        for (uint32_t k = threadIdx.x; k < nKeys; k += blockDim.x)
+            if (local[k]) local[k] = atomicAdd(&offsets[k], local[k]);
+        __syncthreads();
+        if (i < n) sorted[local[key] + rank] = queue[i];
+    } else if (i < n) {
+        sorted[atomicAdd(&offsets[keys[i]], 1u)] = queue[i];
+    }
+}
+
+// Between bounces: the next queue's count becomes the live count, and the
+// counters the next bounce accumulates into are cleared.
+__global__ void kWfAdvance(uint32_t* __restrict__ counts, uint32_t* __restrict__ hist, uint32_t nKeys) {
+    for (uint32_t k = threadIdx.x; k < nKeys; k += blockDim.x) hist[k] = 0;
+    if (threadIdx.x == 0) {
+        counts[0] = counts[1];
+        counts[1] = 0;
+    }
+}
+
+// The bounce after the query, for the live paths in material order.  Mode
+// supplies the hooks of shadeBounce (with their per-path state in st.aux)
+// and what happens to a path that ends.
+template <class Mode>
+__global__ void __launch_bounds__(kWfThreads) kWfShade(const SceneView sc, const Params p, WfState st,
+                                                       const __grid_constant__ Mode mode,
+                                                       const uint32_t* __restrict__ order,
+                                                       const uint32_t* __restrict__ count, uint32_t depth,
+                                                       uint32_t* __restrict__ next, uint32_t* __restrict__ nextCount,
+                                                       unsigned long long* __restrict__ rayCounter) {
+    const uint32_t n = *count;
+    if (blockIdx.x * blockDim.x >= n) return;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    PathCtx c{sc, 0u, SpectralPath{}};
+    bool push = false;
+    uint32_t k = 0;
+    if (i < n) {
+        k = order[i];
+        const uint4 meta = st.meta[k];
+        c.spec = makeSpectralPath(p.spectral != 0, meta.x, meta.y, meta.z);
+        Sampler smp = Sampler::resume(meta.w, st.inc[k]);
+        const float4 o = st.ro[k], d = st.rd[k], b = st.beta[k], r = st.rad[k], hv = st.hit[k];
+        float3 ro = mk3(o.x, o.y, o.z), rd = mk3(d.x, d.y, d.z);
+        Spec beta = sp(b.x, b.y, b.z), radiance = sp(r.x, r.y, r.z);
+        THit h;
+        h.prim = __float_as_uint(hv.x);
+        h.t = hv.y;
+        h.u = hv.z;
+        h.v = hv.w;
+        typename Mode::Hooks hk = mode.hooks(st, k, meta);
+        const bool alive = shadeBounce(c, p, smp, depth, h, ro, rd, beta, radiance, hk);
+        if (alive && depth + 1 < p.maxDepth) {
+            push = true;
+            st.ro[k] = make_float4(ro.x, ro.y, ro.z, o.w);
+            st.rd[k] = make_float4(rd.x, rd.y, rd.z, d.w);
+            st.beta[k] = make_float4(beta.r, beta.g, beta.b, __uint_as_float(depth + 1));
+            st.rad[k] = make_float4(radiance.r, radiance.g, radiance.b, 0.0f);
+            st.meta[k] = make_uint4(meta.x, meta.y, meta.z, smp.state);
+            mode.keep(st, k, hk);
+        } else {
+            mode.end(st, k, meta, c, radiance, make_float2(o.w, d.w), hk);
+        }
+    }
+    // warp-aggregated append to the next queue
+    const unsigned act = __activemask();
+    const unsigned m = __ballot_sync(act, push);
+    if (m) {
+        const int lane = threadIdx.x & 31;
+        const int leader = __ffs(m) - 1;
+        uint32_t base = 0;
+        if (lane == leader) base = atomicAdd(nextCount, (uint32_t)__popc(m));
+        base = __shfl_sync(act, base, leader);
+        if (push) next[base + __popc(m & ((1u << lane) - 1u))] = k;
+    }
+    addRays(rayCounter, c.rays);
+}
+
+// Paths never traced (max depth 0) end with zero radiance.
+template <class Mode>
+__global__ void kWfEndAll(const SceneView sc, const Params p, WfState st, const __grid_constant__ Mode mode,
+                          uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint4 meta = st.meta[i];
+    PathCtx c{sc, 0u, SpectralPath{}};
+    c.spec = makeSpectralPath(p.spectral != 0, meta.x, meta.y, meta.z);
+    typename Mode::Hooks hk = mode.hooks(st, i, meta);
+    mode.end(st, i, meta, c, sp(0.0f), make_float2(st.ro[i].w, st.rd[i].w), hk);
+}
+
+__global__ void kWfStart(uint32_t* __restrict__ counts, uint32_t n, uint32_t* __restrict__ hist, uint32_t nKeys) {
+    for (uint32_t k = threadIdx.x; k < nKeys; k += blockDim.x) hist[k] = 0;
+    if (threadIdx.x == 0) {
+        counts[0] = n;
+        counts[1] = 0;
+    }
+}
+
+inline unsigned blocks(uint64_t n) { return (unsigned)((n + kWfThreads - 1) / kWfThreads); }
+
+// One wave of n paths (path k of the wave is path base + k of the render):
+// camera rays, then per bounce extend, histogram, scan, scatter, shade and
+// advance, on `stream` without waiting on the host.
+template <class Mode>
+int runWave(cr_scene* s, const Params& p, const Mode& mode, WfBuffers* b, uint64_t base, uint32_t n,
+            cudaStream_t stream) {
+    const uint32_t nKeys = s->nMats + 2;
+    const WfState st{b->ro, b->rd, b->beta, b->rad, b->meta, b->inc, b->hit, b->aux};
+    const SceneView v = s->view();
+    kWfInit<<<blocks(n), kWfThreads, 0, stream>>>(s->cam, p, st, base, n, b->qa);
+    CR_LAUNCH_CHECK();
+    if (p.maxDepth == 0) {
+        kWfEndAll<Mode><<<blocks(n), kWfThreads, 0, stream>>>(v, p, st, mode, n);
+        CR_LAUNCH_CHECK();
+        return CR_OK;
+    }
+    kWfStart<<<1, 256, 0, stream>>>(b->counts, n, b->hist, nKeys);
+    CR_LAUNCH_CHECK();
+    uint32_t* live = b->qa;
+    uint32_t* nextQ = b->qb;
+    for (uint32_t depth = 0; depth < p.maxDepth; depth++) {
+        kWfExtend<<<blocks(n), kWfThreads, 0, stream>>>(v, st, live, b->counts, s->nMats, b->keys, s->rayCounter);
+        CR_LAUNCH_CHECK();
+        kWfHistogram<<<blocks(n), kWfThreads, 0, stream>>>(b->keys, b->counts, nKeys, b->hist);
+        CR_LAUNCH_CHECK();
+        kWfScan<<<1, 1024, 0, stream>>>(b->hist, nKeys);
+        CR_LAUNCH_CHECK();
+        kWfScatter<<<blocks(n), kWfThreads, 0, stream>>>(b->keys, live, b->counts, nKeys, b->hist, b->sorted);
+        CR_LAUNCH_CHECK();
+        kWfShade<Mode><<<blocks(n), kWfThreads, 0, stream>>>(v, p, st, mode, b->sorted, b->counts, depth, nextQ,
+                                                              b->counts + 1, s->rayCounter);
+        CR_LAUNCH_CHECK();
+        kWfAdvance<<<1, 256, 0, stream>>>(b->counts, b->hist, nKeys);
+        CR_LAUNCH_CHECK();
+        std::swap(live, nextQ);
+    }
+    return CR_OK;
+}
+
+}  // namespace
+}  // namespace cr

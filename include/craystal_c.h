@@ -106,12 +106,18 @@ typedef struct {
  * is upsampled to spectra, the film receives linear sRGB white-balanced so
  * that a flat spectrum renders as in RGB. */
 #define CR_RENDER_SPECTRAL 1u
-/* The wavefront variant of the integrator (an alternative schedule of the
- * same paths): live paths are kept in HBM between bounces; each bounce is a
- * traversal launch, a sort of the hits by material and a shading launch.
- * Per path the arithmetic and the sampler sequence are the megakernel's, so
- * the film is the same up to the order of its float additions. */
+/* Schedules of the same paths.  The megakernel keeps each path in one
+ * thread's registers for all its bounces (the reference's structure); the
+ * wavefront keeps live paths in HBM between bounces and runs each bounce as
+ * a traversal launch, a counting sort of the hits by material and a shading
+ * launch.  Per path the arithmetic and the sampler sequence are the same,
+ * so the film is the same up to the order of its float additions.  Without
+ * either flag cr_render takes the wavefront for 65,536 paths (pixels x spp)
+ * or more and the megakernel below.  Neither waits on the host; the
+ * wavefront's path state is allocated with the scene on first use (render
+ * once before capturing cr_render into a CUDA graph). */
 #define CR_RENDER_WAVEFRONT 2u
+#define CR_RENDER_MEGAKERNEL 4u
 
 /* Binary BVH node in the reference's layout (Core/BVH.h:17-30): nodes in
  * post-order with the root last; leaf: (a, b) = (first leaf slot, count),

@@ -47,6 +47,26 @@ def test_all_training_paths_equal_plain(gpu_lib):
     assert integ.stats.queries == 0 and integ.stats.train_records > 0
 
 
+@pytest.mark.parametrize("train_every", [1, 4])
+def test_wavefront_form_equals_megakernel_form(gpu_lib, train_every):
+    """The two schedules of the cached integrator with the same frozen network:
+    the same queries, training records, rays and film."""
+    from craystal_gb300.api import RadianceCache
+    sc, cam = cornell(64)
+    cache = RadianceCache()
+    out = []
+    for wf in (False, True):
+        integ = CachedPathTraceIntegrator(CFG, train_every=train_every, cache=cache, wavefront=wf)
+        sc.film_clear()
+        integ.dispatch(sc, 4, first_sample=11, freeze=True)
+        out.append((cam.sensor.data.copy(), cam.sensor.weight.copy(), integ.stats.queries,
+                    integ.stats.train_records, sc.render_ray_count()))
+    (r0, w0, q0, t0, n0), (r1, w1, q1, t1, n1) = out
+    assert (q0, t0, n0) == (q1, t1, n1)
+    np.testing.assert_allclose(w1, w0, rtol=1e-5)
+    np.testing.assert_allclose(r1, r0, rtol=1e-4, atol=1e-5)
+
+
 def test_cache_bookkeeping_and_finite(gpu_lib):
     sc, cam = cornell(128)
     integ = CachedPathTraceIntegrator(CFG, train_every=8)

@@ -1,9 +1,10 @@
-"""The wavefront integrator (CR_RENDER_WAVEFRONT: extend, sort by material,
-shade per bounce) traces the same paths as the megakernel with the same
-arithmetic and sampler sequence: films equal up to the order of the float
-atomics, ray counts exactly equal.  Covered: MIS on and off, spectral mode,
-spheres + textures + an environment, several waves (more paths than one
-wave holds), and max depth 0."""
+"""The wavefront integrator (CR_RENDER_WAVEFRONT: extend, counting sort by
+material, shade per bounce) traces the same paths as the megakernel
+(CR_RENDER_MEGAKERNEL) with the same arithmetic and sampler sequence: films
+equal up to the order of the float atomics, ray counts exactly equal.
+Covered: MIS on and off, spectral mode, spheres + textures + an
+environment, several waves (more paths than one wave holds), max depth 0,
+the automatic choice, and a wavefront render captured in a CUDA graph."""
 import numpy as np
 import pytest
 
@@ -22,7 +23,7 @@ def film_of(sc, integ, spp, first=0):
 
 def compare(sc, depth=8, mis=True, spectral=False, spp=16, first=3):
     cfg = PathTraceIntegrator.Configs(maxDepth=depth, rrThreshold=0.05, useMIS=mis)
-    mega = film_of(sc, PathTraceIntegrator(cfg, compat=False, spectral=spectral), spp, first)
+    mega = film_of(sc, PathTraceIntegrator(cfg, compat=False, spectral=spectral, wavefront=False), spp, first)
     wave = film_of(sc, PathTraceIntegrator(cfg, compat=False, spectral=spectral, wavefront=True), spp, first)
     np.testing.assert_allclose(wave[1], mega[1], rtol=1e-5, atol=1e-5)
     np.testing.assert_allclose(wave[0], mega[0], rtol=2e-4, atol=2e-4)
@@ -57,3 +58,36 @@ def test_wavefront_several_waves_and_depth_zero(gpu_lib):
     compare(sc, spp=9)  # 2.36 M paths: two waves
     rgb, w, rays = compare(sc, depth=0, spp=2)
     assert rays == 0 and w.sum() > 0 and not rgb.any()
+
+
+def test_auto_schedule_and_graph_capture(gpu_lib):
+    import ctypes
+
+    import torch
+
+    from craystal_gb300._lib import CrIntegratorConfig, check, load
+    data, cam = scenes.cornell_box(seed=8, width=128, height=128)
+    sc = Scene(data)
+    sc.setCamera(cam)
+    cfg = PathTraceIntegrator.Configs(maxDepth=8, rrThreshold=0.05)
+    ref = film_of(sc, PathTraceIntegrator(cfg, compat=False, wavefront=False), 8)
+    auto = film_of(sc, PathTraceIntegrator(cfg, compat=False), 8)  # 131,072 paths: the wavefront
+    np.testing.assert_allclose(auto[0], ref[0], rtol=2e-4, atol=2e-4)
+    # the wavefront schedule records into a CUDA graph and replays the same samples
+    lib = load()
+    c = CrIntegratorConfig(8, 0.05, 1, 2)
+    s = torch.cuda.Stream()
+    sc.film_clear()
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        check(lib.cr_render(sc.handle, ctypes.byref(c), 8, 0, ctypes.c_void_p(s.cuda_stream)))
+    sc.film_clear()
+    torch.cuda.synchronize()
+    g.replay()
+    torch.cuda.synchronize()
+    rgb, w = sc.film_read()
+    np.testing.assert_allclose(w, ref[1], rtol=1e-5, atol=1e-5)
+    np.testing.assert_allclose(rgb, ref[0], rtol=2e-4, atol=2e-4)
+    with pytest.raises(Exception):
+        check(lib.cr_render(sc.handle, ctypes.byref(CrIntegratorConfig(8, 0.05, 1, 6)), 1, 0, None))
