@@ -226,6 +226,52 @@ def wavefront_extra(torch):
     return out
 
 
+def large_scene_extra(torch, spp=32):
+    """The large workload: a 4096 x 4096 fBm heightfield (33.5M triangles)
+    plus 10k boxes, Principled materials, a sun sphere light and a constant
+    sky, rendered at 3840 x 2160, 32 spp, max depth 12, NEE + MIS, on the
+    wavefront schedule; with the host generation time, the GPU BVH build
+    time and the device memory the scene and its render hold."""
+    from craystal_gb300 import scenes
+    from craystal_gb300.api import PathTraceIntegrator, Scene
+    t = time.perf_counter()
+    data, cam, env, sun = scenes.large_terrain_scene()
+    gen_s = time.perf_counter() - t
+    torch.cuda.synchronize()
+    free0, total = torch.cuda.mem_get_info()
+    t = time.perf_counter()
+    sc = Scene(data)
+    sc.setCamera(cam)
+    sc.set_environment(env)
+    sc.set_sphere_lights(sun)
+    torch.cuda.synchronize()
+    create_s = time.perf_counter() - t
+    st = sc.bvh_stats()
+    n_tris = sc.n_tris
+    del data
+    integ = PathTraceIntegrator(PathTraceIntegrator.Configs(maxDepth=12, rrThreshold=0.05, useMIS=True), compat=False)
+    integ.dispatch(sc, 1, readback=False)  # allocates the path state
+    torch.cuda.synchronize()
+    sc.film_clear()
+    t = time.perf_counter()
+    integ.dispatch(sc, spp, readback=False)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t
+    free1, _ = torch.cuda.mem_get_info()
+    rays = sc.render_ray_count()
+    rgb, w = sc.film_read()
+    paths = 3840 * 2160 * spp
+    out = {"config": "terrain 4096^2 (fBm, 6 octaves) + 10k boxes, 3840x2160, 32 spp, depth 12, sun + sky",
+           "triangles": int(n_tris), "host_generation_s": round(gen_s, 2), "scene_create_s": round(create_s, 2),
+           "gpu_bvh_build_ms": round(st["build_ms"], 1), "bvh_device_mib": round(st["device_bytes"] / 2 ** 20, 1),
+           "device_gib_held": round((free0 - free1) / 2 ** 30, 2), "render_s": round(dt, 3),
+           "Mpaths_s": round(paths / dt / 1e6, 1), "Mrays_s": round(rays / dt / 1e6, 1),
+           "rays_per_path": round(rays / paths, 3),
+           "mean_rgb": [round(float(x), 4) for x in np.nanmean(rgb / w[..., None], axis=(0, 1))]}
+    sc.close()
+    return out
+
+
 def cache_frames_extra(torch, res=512, frames=32):
     """The cached integrator's frames alone (Cornell res x res, max depth 8,
     NEE + MIS, training every frame) after 16 warm-up frames: ms per frame
@@ -309,9 +355,10 @@ def cache_extra(torch, res=512):
 def batch_extra(torch, n_scenes=64):
     """The batched workload: 64 random-box-clutter scenes (triangles
     log-uniform 10k-500k, resolution from {128..1024}^2, spp log-uniform 4-256,
-    depth 8-16) in one persistent launch replayed from a CUDA graph, tuned by
-    the autotuner on a 1/16-spp probe of the same batch; compared with the same
-    renders dispatched scene by scene."""
+    depth 8-16) replayed from captured CUDA graphs on the schedule the
+    autotuner picks on a 1/16-spp probe of the same batch (persistent
+    megakernel or many-scene wavefront); compared with the same renders
+    dispatched scene by scene."""
     from craystal_gb300 import scenes
     from craystal_gb300.api import BatchRenderer, PathTraceIntegrator, Scene
     params = scenes.batch_workload(n_scenes)
@@ -327,7 +374,7 @@ def batch_extra(torch, n_scenes=64):
     tune = probe.autotune()
     probe.close()
     b = BatchRenderer(scs, integs, [p["spp"] for p in params])
-    b.set_tuning(tune["best"]["tile"], tune["best"]["spp_per_item"])
+    b.set_tuning(tune["best"]["tile"], tune["best"]["spp_per_item"], wave_log2=tune["best"]["wave_log2"])
 
     def timed(fn):
         torch.cuda.synchronize()
@@ -345,7 +392,7 @@ def batch_extra(torch, n_scenes=64):
         sc.film_clear()
     t_seq = timed(lambda: [integ.dispatch(sc, p["spp"], readback=False) for sc, integ, p in zip(scs, integs, params)])
     paths = sum(p["res"] ** 2 * p["spp"] for p in params)
-    return {"config": f"{n_scenes} box-clutter scenes, one persistent launch from a CUDA graph",
+    return {"config": f"{n_scenes} box-clutter scenes from captured CUDA graphs",
             "triangles": int(sum(sc.n_tris for sc in scs)), "paths": int(paths), "rays": int(rays),
             "batched_s": round(t_batch, 3), "batched_Mpaths_s": round(paths / t_batch / 1e6, 1),
             "batched_Mrays_s": round(rays / t_batch / 1e6, 1), "per_scene_dispatch_s": round(t_seq, 3),
@@ -462,6 +509,7 @@ def run_ours(args):
         extra["wavefront_vs_megakernel"] = wavefront_extra(torch)
         extra["radiance_cache_equal_time"] = cache_extra(torch, args.cache_res)
         extra["batched_scenes"] = batch_extra(torch, args.batch_scenes)
+        extra["large_scene"] = large_scene_extra(torch)
 
     out = {"metric": METRIC, "value": round(value, 2), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
@@ -510,6 +558,8 @@ def run_only(args):
         r = cache_extra(torch, args.cache_res)
     elif args.only == "cache_frames":
         r = cache_frames_extra(torch, args.cache_res)
+    elif args.only == "large_scene":
+        r = large_scene_extra(torch)
     else:
         r = batch_extra(torch, args.batch_scenes)
     print(json.dumps({args.only: r}), flush=True)
@@ -525,7 +575,8 @@ def main():
     ap.add_argument("--skip-extra", action="store_true", help="omit the path-tracer figures")
     ap.add_argument("--rays", type=int, default=N_RAYS, help="rays per step (profiling a smaller case)")
     ap.add_argument("--tris", type=int, default=N_TRIS, help="triangles (profiling a smaller case)")
-    ap.add_argument("--only", choices=["path_tracer", "wavefront", "radiance_cache", "cache_frames", "batched_scenes"],
+    ap.add_argument("--only", choices=["path_tracer", "wavefront", "radiance_cache", "cache_frames", "batched_scenes",
+                                       "large_scene"],
                     help="run one secondary workload alone and print its figures (profiling)")
     ap.add_argument("--cache-res", type=int, default=512, help="radiance-cache workload resolution")
     ap.add_argument("--batch-scenes", type=int, default=64, help="scenes in the batched workload")

@@ -96,7 +96,8 @@ class CrBatchItem(ctypes.Structure):
 
 
 class CrBatchTuning(ctypes.Structure):
-    _fields_ = [("tile", ctypes.c_uint32), ("spp_per_item", ctypes.c_uint32), ("blocks_per_sm", ctypes.c_uint32)]
+    _fields_ = [("tile", ctypes.c_uint32), ("spp_per_item", ctypes.c_uint32), ("blocks_per_sm", ctypes.c_uint32),
+                ("wave_log2", ctypes.c_uint32)]
 
 
 class CrBatchTuningResult(ctypes.Structure):

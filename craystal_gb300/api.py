@@ -509,16 +509,19 @@ class BatchRenderer:
     def render(self, stream: int = 0):
         check(load().cr_batch_render(self._h, stream or None))
 
-    def set_tuning(self, tile=16, spp_per_item=4, blocks_per_sm=0):
+    def set_tuning(self, tile=16, spp_per_item=4, blocks_per_sm=0, wave_log2=0):
+        """wave_log2 = 0: the persistent megakernel with (tile, spp_per_item,
+        blocks_per_sm); 16..23: the wavefront in waves of 2^wave_log2 paths."""
         from ._lib import CrBatchTuning
-        t = CrBatchTuning(tile, spp_per_item, blocks_per_sm)
+        t = CrBatchTuning(tile, spp_per_item, blocks_per_sm, wave_log2)
         check(load().cr_batch_set_tuning(self._h, ctypes.byref(t)))
 
     def tuning(self) -> dict:
         from ._lib import CrBatchTuning
         t = CrBatchTuning()
         check(load().cr_batch_get_tuning(self._h, ctypes.byref(t)))
-        return {"tile": t.tile, "spp_per_item": t.spp_per_item, "blocks_per_sm": t.blocks_per_sm}
+        return {"tile": t.tile, "spp_per_item": t.spp_per_item, "blocks_per_sm": t.blocks_per_sm,
+                "wave_log2": t.wave_log2}
 
     def autotune(self, json_path: str = None) -> dict:
         """Times every tuning on this batch, keeps the fastest (films are
@@ -528,9 +531,10 @@ class BatchRenderer:
         res = (CrBatchTuningResult * 32)()
         n = ctypes.c_uint32()
         check(load().cr_batch_autotune(self._h, ctypes.byref(best), res, 32, ctypes.byref(n)))
-        out = {"best": {"tile": best.tile, "spp_per_item": best.spp_per_item},
+        out = {"best": {"tile": best.tile, "spp_per_item": best.spp_per_item, "wave_log2": best.wave_log2},
                "timings_ms": [{"tile": res[i].tuning.tile, "spp_per_item": res[i].tuning.spp_per_item,
-                               "ms": round(res[i].ms, 4)} for i in range(n.value)]}
+                               "wave_log2": res[i].tuning.wave_log2, "ms": round(res[i].ms, 4)}
+                              for i in range(n.value)]}
         if json_path:
             import json
             with open(json_path, "w") as f:

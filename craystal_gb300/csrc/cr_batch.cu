@@ -18,6 +18,7 @@
 
 #include "cr_internal.cuh"
 #include "cr_tile.cuh"
+#include "cr_wavefront.cuh"
 
 namespace cr {
 namespace {
@@ -70,8 +71,14 @@ struct cr_batch {
     int device = 0;
     std::vector<cr_scene*> scenes;
     std::vector<cr_batch_item> items;
-    cr_batch_tuning tuning{16, 4, 0};
+    cr_batch_tuning tuning{16, 4, 0, 0};
     BatchScene* dScenes = nullptr;
+    // wavefront schedule
+    WfScene* dWf = nullptr;
+    void* wfBuffers = nullptr;
+    uint64_t* dWaveBase = nullptr;
+    uint64_t wfTotal = 0;
+    uint32_t wfKeys = 0, wfMaxDepth = 0, wfWaves = 0;
     BatchItem* dItems = nullptr;
     uint32_t nItems = 0;
     uint32_t* dQueue = nullptr;
@@ -126,6 +133,62 @@ int uploadDescriptors(cr_batch* b, cudaStream_t st) {
         d[i].tilesX = (s->cam.width + tw - 1) / tw;
     }
     CR_CUDA(cudaMemcpyAsync(b->dScenes, d.data(), d.size() * sizeof(BatchScene), cudaMemcpyHostToDevice, st));
+    if (b->tuning.wave_log2) {
+        // the wavefront's scene table: the same descriptors plus each scene's
+        // range of the path sequence and of the sort keys
+        std::vector<WfScene> w(b->scenes.size());
+        uint64_t path = 0;
+        uint32_t key = 0;
+        for (size_t i = 0; i < w.size(); i++) {
+            cr_scene* s = b->scenes[i];
+            std::memset(&w[i], 0, sizeof(WfScene));
+            w[i].view = d[i].view;
+            w[i].cam = d[i].cam;
+            w[i].p = d[i].p;
+            w[i].p.sppPerBlock = 1;
+            w[i].filmRgb = d[i].filmRgb;
+            w[i].filmW = d[i].filmW;
+            w[i].rayCounter = d[i].rayCounter;
+            w[i].pathBase = path;
+            w[i].keyBase = key;
+            w[i].nMats = s->nMats;
+            path += (uint64_t)s->cam.width * s->cam.height * b->items[i].spp;
+            key += s->nMats + 2;
+        }
+        CR_CUDA(cudaMemcpyAsync(b->dWf, w.data(), w.size() * sizeof(WfScene), cudaMemcpyHostToDevice, st));
+    }
+    return CR_OK;
+}
+
+// The wavefront schedule: one wave of the batch's path sequence captured as
+// a graph; renderOnce replays it until the sequence is done.
+int buildWavefront(cr_batch* b, cudaStream_t st) {
+    uint64_t total = 0;
+    uint32_t keys = 0, maxDepth = 0;
+    for (size_t i = 0; i < b->scenes.size(); i++) {
+        const cr_scene* s = b->scenes[i];
+        total += (uint64_t)s->cam.width * s->cam.height * b->items[i].spp;
+        keys += s->nMats + 2;
+        maxDepth = std::max(maxDepth, b->items[i].config.max_depth);
+    }
+    const uint32_t cap = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(total, 1), 1ull << b->tuning.wave_log2);
+    WfBuffers* wb = nullptr;
+    int rc = ensureWavefrontBuffers(b->wfBuffers, cap, keys, wb);
+    if (rc) return rc;
+    if (!b->dWf) CR_CUDA(cudaMalloc(&b->dWf, b->scenes.size() * sizeof(WfScene)));
+    if (!b->dWaveBase) CR_CUDA(cudaMalloc(&b->dWaveBase, sizeof(uint64_t)));
+    b->wfTotal = total;
+    b->wfKeys = keys;
+    b->wfMaxDepth = maxDepth;
+    b->wfWaves = (uint32_t)((total + cap - 1) / cap);
+    const ManyScenes src{b->dWf, (uint32_t)b->scenes.size()};
+    CR_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    rc = runWave(src, PlainMode{}, wb, 0, cap, maxDepth, keys, st, b->dWaveBase, total);
+    cudaError_t e = cudaStreamEndCapture(st, &b->graph);
+    if (rc) return rc;
+    if (e != cudaSuccess) return fail(CR_ERR_CUDA, "cudaStreamEndCapture: %s", cudaGetErrorString(e));
+    CR_CUDA(cudaGraphInstantiate(&b->exec, b->graph, 0));
+    b->built = true;
     return CR_OK;
 }
 
@@ -133,6 +196,7 @@ int buildWork(cr_batch* b, cudaStream_t st) {
     releaseGraph(b);
     if (b->dItems) cudaFree(b->dItems);
     b->dItems = nullptr;
+    if (b->tuning.wave_log2) return buildWavefront(b, st);
     const int tw = b->tuning.tile;
     const uint32_t run = std::max(1u, b->tuning.spp_per_item);
     // scenes by estimated cost (pixels * spp * depth), largest first
@@ -181,8 +245,14 @@ int renderOnce(cr_batch* b, cudaStream_t st) {
     }
     int rc = uploadDescriptors(b, st);
     if (rc) return rc;
-    CR_CUDA(cudaGraphLaunch(b->exec, st));
-    countLaunch();
+    if (b->tuning.wave_log2) {
+        CR_CUDA(cudaMemsetAsync(b->dWaveBase, 0, sizeof(uint64_t), st));
+        for (uint32_t w = 0; w < b->wfWaves; w++) CR_CUDA(cudaGraphLaunch(b->exec, st));
+        countLaunch(b->wfWaves);
+    } else {
+        CR_CUDA(cudaGraphLaunch(b->exec, st));
+        countLaunch();
+    }
     b->replays++;
     return CR_OK;
 }
@@ -223,6 +293,9 @@ int cr_batch_destroy(cr_batch* b) {
     if (b->dItems) cudaFree(b->dItems);
     if (b->dScenes) cudaFree(b->dScenes);
     if (b->dQueue) cudaFree(b->dQueue);
+    if (b->dWf) cudaFree(b->dWf);
+    if (b->dWaveBase) cudaFree(b->dWaveBase);
+    freeWavefrontBuffers(b->wfBuffers);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
     return CR_OK;
@@ -231,8 +304,10 @@ int cr_batch_destroy(cr_batch* b) {
 int cr_batch_set_tuning(cr_batch* b, const cr_batch_tuning* t) {
     clearError();
     if (!b || !t) return fail(CR_ERR_INVALID_ARGUMENT, "NULL argument");
-    if (t->tile != 8 && t->tile != 16) return fail(CR_ERR_INVALID_ARGUMENT, "tile must be 8 or 16");
-    if (t->spp_per_item == 0) return fail(CR_ERR_INVALID_ARGUMENT, "spp_per_item must be positive");
+    if (t->wave_log2 && (t->wave_log2 < 16 || t->wave_log2 > 23))
+        return fail(CR_ERR_INVALID_ARGUMENT, "wave_log2 must be 0 or 16..23");
+    if (!t->wave_log2 && t->tile != 8 && t->tile != 16) return fail(CR_ERR_INVALID_ARGUMENT, "tile must be 8 or 16");
+    if (!t->wave_log2 && t->spp_per_item == 0) return fail(CR_ERR_INVALID_ARGUMENT, "spp_per_item must be positive");
     b->tuning = *t;
     b->built = false;
     return CR_OK;
@@ -261,17 +336,18 @@ int cr_batch_autotune(cr_batch* b, cr_batch_tuning* best, cr_batch_tuning_result
     clearError();
     if (!b) return fail(CR_ERR_INVALID_ARGUMENT, "NULL argument");
     CR_CUDA(cudaSetDevice(b->device));
-    const uint32_t tiles[] = {8, 16};
-    const uint32_t runs[] = {1, 2, 4, 8, 16};
+    std::vector<cr_batch_tuning> cands;
+    for (uint32_t tw : {8u, 16u})
+        for (uint32_t r : {1u, 2u, 4u, 8u, 16u}) cands.push_back(cr_batch_tuning{tw, r, 0, 0});
+    for (uint32_t w : {19u, 20u, 21u, 22u}) cands.push_back(cr_batch_tuning{16, 4, 0, w});
     cudaEvent_t e0, e1;
     CR_CUDA(cudaEventCreate(&e0));
     CR_CUDA(cudaEventCreate(&e1));
     float bestMs = INFINITY;
     cr_batch_tuning bestT = b->tuning;
     uint32_t k = 0;
-    for (uint32_t tw : tiles) {
-        for (uint32_t r : runs) {
-            cr_batch_tuning t{tw, r, 0};
+    {
+        for (const cr_batch_tuning& t : cands) {
             b->tuning = t;
             b->built = false;
             int rc = buildWork(b, b->stream);

@@ -239,8 +239,9 @@ struct CachedMode {
     __device__ __forceinline__ void keep(const WfState& st, uint32_t k, const Hooks& h) const {
         st.aux[k] = make_uint4(h.q, h.slot, h.nRec, 0u);
     }
-    __device__ __forceinline__ void end(const WfState&, uint32_t, const uint4& meta, const PathCtx&, const Spec& L,
-                                        float2 pix, const Hooks& h) const {
+    template <class Src>
+    __device__ __forceinline__ void end(const Src&, uint32_t, const WfState&, uint32_t, const uint4& meta,
+                                        const PathCtx&, const Spec& L, float2 pix, const Hooks& h) const {
         SampleRec rec;
         rec.a = make_float4(L.r, L.g, L.b, pix.x);
         rec.b = make_float4(pix.y, __uint_as_float(h.q), 0.0f, 0.0f);
@@ -393,7 +394,7 @@ int renderCached(cr_scene* s, const cr_integrator_config* cfg, const cr_cache_co
     WfBuffers* wb = nullptr;
     const uint32_t waveCap = (uint32_t)std::min<uint64_t>(px, kWaveCap);
     if (wavefront) {
-        rc = ensureWavefrontBuffers(s, waveCap, s->nMats + 2, wb);
+        rc = ensureWavefrontBuffers(s->wfBuffers, waveCap, s->nMats + 2, wb);
         if (rc) return rc;
     }
     Params p;
@@ -416,7 +417,8 @@ int renderCached(cr_scene* s, const cr_integrator_config* cfg, const cr_cache_co
                                   b->recBeta, b->recBefore, b->counters + 2, slotCap, b->tIn, b->tTarget,
                                   b->counters + 1, b->samples};
             for (uint64_t base = 0; base < px; base += waveCap) {
-                rc = runWave(s, p, mode, wb, base, (uint32_t)std::min<uint64_t>(waveCap, px - base), st);
+                rc = runWave(oneScene(s, p), mode, wb, base, (uint32_t)std::min<uint64_t>(waveCap, px - base),
+                             p.maxDepth, s->nMats + 2, st);
                 if (rc) return rc;
             }
         } else {

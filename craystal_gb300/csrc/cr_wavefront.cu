@@ -5,23 +5,6 @@
 #include "cr_wavefront.cuh"
 
 namespace cr {
-namespace {
-
-struct PlainMode {
-    using Hooks = NoHooks;
-    CameraGpu cam;
-    float3 wb;
-    float* filmRgb;
-    float* filmW;
-    __device__ __forceinline__ Hooks hooks(const WfState&, uint32_t, const uint4&) const { return NoHooks{}; }
-    __device__ __forceinline__ void keep(const WfState&, uint32_t, const Hooks&) const {}
-    __device__ __forceinline__ void end(const WfState&, uint32_t, const uint4&, const PathCtx& c, const Spec& L,
-                                        float2 pix, const Hooks&) const {
-        splatGlobal(cam, pix, pathSpecToRgb(c.spec, L, wb), filmRgb, filmW);
-    }
-};
-
-}  // namespace
 
 void freeWavefrontBuffers(void* p) {
     if (!p) return;
@@ -45,11 +28,12 @@ int renderWavefront(cr_scene* s, const cr_integrator_config* cfg, uint32_t spp, 
     const uint64_t total = (uint64_t)s->cam.width * s->cam.height * spp;
     const uint32_t cap = (uint32_t)std::min<uint64_t>(total, kWaveCap);
     WfBuffers* b = nullptr;
-    int rc = ensureWavefrontBuffers(s, cap, s->nMats + 2, b);
+    int rc = ensureWavefrontBuffers(s->wfBuffers, cap, s->nMats + 2, b);
     if (rc) return rc;
-    const PlainMode mode{s->cam, p.wb, s->filmRgb, s->filmW};
+    const OneScene src = oneScene(s, p);
     for (uint64_t base = 0; base < total; base += cap) {
-        rc = runWave(s, p, mode, b, base, (uint32_t)std::min<uint64_t>(cap, total - base), stream);
+        rc = runWave(src, PlainMode{}, b, base, (uint32_t)std::min<uint64_t>(cap, total - base), p.maxDepth,
+                     s->nMats + 2, stream);
         if (rc) return rc;
     }
     return CR_OK;

@@ -42,10 +42,10 @@ struct WfBuffers {
     uint32_t cap = 0, keyCap = 0;
     float4 *ro = nullptr, *rd = nullptr, *beta = nullptr, *rad = nullptr, *hit = nullptr;
     uint4 *meta = nullptr, *aux = nullptr;
-    uint32_t *inc = nullptr, *qa = nullptr, *qb = nullptr, *keys = nullptr, *sorted = nullptr, *counts = nullptr,
-             *hist = nullptr;
+    uint32_t *inc = nullptr, *item = nullptr, *qa = nullptr, *qb = nullptr, *keys = nullptr, *sorted = nullptr,
+             *counts = nullptr, *hist = nullptr;
     void release() {
-        void* ptrs[] = {ro, rd, beta, rad, hit, meta, aux, inc, qa, qb, keys, sorted, counts, hist};
+        void* ptrs[] = {ro, rd, beta, rad, hit, meta, aux, inc, item, qa, qb, keys, sorted, counts, hist};
         for (void* q : ptrs)
             if (q) cudaFree(q);
         *this = WfBuffers{};
@@ -57,11 +57,11 @@ inline cudaError_t wfAlloc(T*& p, size_t n) {
     return cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T));
 }
 
-inline int ensureWavefrontBuffers(cr_scene* s, uint32_t cap, uint32_t nKeys, WfBuffers*& out) {
-    WfBuffers* b = static_cast<WfBuffers*>(s->wfBuffers);
+inline int ensureWavefrontBuffers(void*& slot, uint32_t cap, uint32_t nKeys, WfBuffers*& out) {
+    WfBuffers* b = static_cast<WfBuffers*>(slot);
     if (!b) {
         b = new WfBuffers;
-        s->wfBuffers = b;
+        slot = b;
     }
     if (b->cap < cap || b->keyCap < nKeys) {
         CR_CUDA(cudaDeviceSynchronize());  // earlier renders may still use the old buffers
@@ -74,6 +74,7 @@ inline int ensureWavefrontBuffers(cr_scene* s, uint32_t cap, uint32_t nKeys, WfB
         CR_CUDA(wfAlloc(b->meta, cap));
         CR_CUDA(wfAlloc(b->aux, cap));
         CR_CUDA(wfAlloc(b->inc, cap));
+        CR_CUDA(wfAlloc(b->item, cap));
         CR_CUDA(wfAlloc(b->qa, cap));
         CR_CUDA(wfAlloc(b->qb, cap));
         CR_CUDA(wfAlloc(b->keys, cap));
@@ -101,29 +102,120 @@ struct WfState {
     uint4* meta;
     uint32_t* inc;
     float4* hit;
-    uint4* aux;  // per-path state of the integrator's hooks
+    uint4* aux;       // per-path state of the integrator's hooks
+    uint32_t* item;   // the path's scene (many-scene sources)
 };
 
+// Rays traced by each lane, added to its scene's counter: one atomic per
+// group of lanes with the same counter.
 __device__ __forceinline__ void addRays(unsigned long long* counter, uint32_t rays) {
-    for (int o = 16; o > 0; o >>= 1) rays += __shfl_xor_sync(0xffffffffu, rays, o);
-    if ((threadIdx.x & 31) == 0 && rays) atomicAdd(counter, (unsigned long long)rays);
+    const unsigned act = __activemask();
+    const unsigned grp = __match_any_sync(act, (unsigned long long)counter);
+    const uint32_t sum = __reduce_add_sync(grp, rays);
+    if ((int)(threadIdx.x & 31) == __ffs(grp) - 1 && sum) atomicAdd(counter, (unsigned long long)sum);
 }
 
-// Camera rays of paths [base, base + n) of the wave sequence: path k is
-// pixel k mod (w h) at sample p.first + k / (w h).
-__global__ void __launch_bounds__(kWfThreads) kWfInit(const CameraGpu cam, const Params p, WfState st, uint64_t base,
-                                                      uint32_t n, uint32_t* __restrict__ queue) {
+// What a wave renders.  A source maps path g of its sequence to a scene
+// (item), a pixel and a sample index, and gives each item's scene, camera,
+// integrator parameters, film and key range of the material sort.
+//
+// One scene: path g is pixel g mod (w h) at sample p.first + g / (w h).
+struct OneScene {
+    SceneView view;
+    CameraGpu cam;
+    Params p;
+    float* filmRgb;
+    float* filmW;
+    unsigned long long* rayCounter;
+    uint32_t nMats;
+    __device__ __forceinline__ const SceneView& sceneOf(uint32_t) const { return view; }
+    __device__ __forceinline__ const CameraGpu& camOf(uint32_t) const { return cam; }
+    __device__ __forceinline__ const Params& paramsOf(uint32_t) const { return p; }
+    __device__ __forceinline__ float* filmRgbOf(uint32_t) const { return filmRgb; }
+    __device__ __forceinline__ float* filmWOf(uint32_t) const { return filmW; }
+    __device__ __forceinline__ unsigned long long* raysOf(uint32_t) const { return rayCounter; }
+    __device__ __forceinline__ uint32_t keyBase(uint32_t) const { return 0u; }
+    __device__ __forceinline__ uint32_t nMatsOf(uint32_t) const { return nMats; }
+    __device__ __forceinline__ void locate(uint64_t g, uint32_t& item, uint32_t& x, uint32_t& y,
+                                           uint32_t& si) const {
+        const uint64_t area = (uint64_t)cam.width * cam.height;
+        const uint32_t px = (uint32_t)(g % area);
+        item = 0;
+        x = px % cam.width;
+        y = px / cam.width;
+        si = p.first + (uint32_t)(g / area);
+    }
+};
+
+// One scene of a many-scene source; its paths are [pathBase, pathBase +
+// width * height * p.spp) of the source's sequence, its sort keys
+// [keyBase, keyBase + nMats + 2).
+struct __align__(16) WfScene {
+    SceneView view;
+    CameraGpu cam;
+    Params p;
+    float* filmRgb;
+    float* filmW;
+    unsigned long long* rayCounter;
+    uint64_t pathBase;
+    uint32_t keyBase, nMats;
+};
+
+struct ManyScenes {
+    const WfScene* scenes;
+    uint32_t n;
+    __device__ __forceinline__ const SceneView& sceneOf(uint32_t i) const { return scenes[i].view; }
+    __device__ __forceinline__ const CameraGpu& camOf(uint32_t i) const { return scenes[i].cam; }
+    __device__ __forceinline__ const Params& paramsOf(uint32_t i) const { return scenes[i].p; }
+    __device__ __forceinline__ float* filmRgbOf(uint32_t i) const { return scenes[i].filmRgb; }
+    __device__ __forceinline__ float* filmWOf(uint32_t i) const { return scenes[i].filmW; }
+    __device__ __forceinline__ unsigned long long* raysOf(uint32_t i) const { return scenes[i].rayCounter; }
+    __device__ __forceinline__ uint32_t keyBase(uint32_t i) const { return scenes[i].keyBase; }
+    __device__ __forceinline__ uint32_t nMatsOf(uint32_t i) const { return scenes[i].nMats; }
+    __device__ __forceinline__ void locate(uint64_t g, uint32_t& item, uint32_t& x, uint32_t& y,
+                                           uint32_t& si) const {
+        uint32_t lo = 0, hi = n - 1;  // the last scene whose pathBase <= g
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi + 1) / 2;
+            if (scenes[mid].pathBase <= g) lo = mid;
+            else hi = mid - 1;
+        }
+        item = lo;
+        const WfScene& s = scenes[lo];
+        const uint64_t k = g - s.pathBase;
+        const uint64_t area = (uint64_t)s.cam.width * s.cam.height;
+        const uint32_t px = (uint32_t)(k % area);
+        x = px % s.cam.width;
+        y = px / s.cam.width;
+        si = s.p.first + (uint32_t)(k / area);
+    }
+};
+
+// Camera rays of paths [base, base + n) of the source's sequence.
+//
+// With waveBase set, the wave starts at *waveBase and holds min(n, total -
+// *waveBase) paths (a wave graph replayed over a long sequence).
+__device__ __forceinline__ uint32_t waveSize(uint64_t& base, uint32_t n, const uint64_t* waveBase, uint64_t total) {
+    if (!waveBase) return n;
+    base = *waveBase;
+    if (base >= total) return 0u;
+    const uint64_t left = total - base;
+    return left < (uint64_t)n ? (uint32_t)left : n;
+}
+
+template <class Src>
+__global__ void __launch_bounds__(kWfThreads) kWfInit(const __grid_constant__ Src src, WfState st, uint64_t base,
+                                                      uint32_t n, const uint64_t* __restrict__ waveBase,
+                                                      uint64_t total) {
+    n = waveSize(base, n, waveBase, total);
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const uint64_t k = base + i;
-    const uint64_t area = (uint64_t)cam.width * cam.height;
-    const uint32_t px = (uint32_t)(k % area);
-    const uint32_t x = px % cam.width, y = px / cam.width;
-    const uint32_t si = p.first + (uint32_t)(k / area);
+    uint32_t item, x, y, si;
+    src.locate(base + i, item, x, y, si);
     Sampler smp(x, y, si);
     float2 pix;
     float3 ro, rd;
-    cameraRay(cam, smp, x, y, pix, ro, rd);
+    cameraRay(src.camOf(item), smp, x, y, pix, ro, rd);
     st.ro[i] = make_float4(ro.x, ro.y, ro.z, pix.x);
     st.rd[i] = make_float4(rd.x, rd.y, rd.z, pix.y);
     st.beta[i] = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(0u));
@@ -131,34 +223,39 @@ __global__ void __launch_bounds__(kWfThreads) kWfInit(const CameraGpu cam, const
     st.meta[i] = make_uint4(x, y, si, smp.state);
     st.inc[i] = smp.inc;
     st.aux[i] = make_uint4(CR_MISS, CR_MISS, 0u, 0u);
-    queue[i] = i;
+    st.item[i] = item;
 }
 
-// The closest-hit query of every live path; key = the material to shade
-// (nMats for a miss, nMats + 1 for a sphere light).
-__global__ void __launch_bounds__(kWfThreads) kWfExtend(const SceneView sc, WfState st,
+// The closest-hit query of every live path; key = the scene's key base plus
+// the material to shade (nMats for a miss, nMats + 1 for a sphere light).
+template <class Src>
+__global__ void __launch_bounds__(kWfThreads) kWfExtend(const __grid_constant__ Src src, WfState st,
                                                         const uint32_t* __restrict__ queue,
-                                                        const uint32_t* __restrict__ count, uint32_t nMats,
-                                                        uint32_t* __restrict__ keys,
-                                                        unsigned long long* __restrict__ rayCounter) {
+                                                        const uint32_t* __restrict__ count,
+                                                        uint32_t* __restrict__ keys) {
     const uint32_t n = *count;
     if (blockIdx.x * blockDim.x >= n) return;  // the whole block is past the live paths
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    PathCtx c{sc, 0u, SpectralPath{}};
+    uint32_t item = 0, rays = 0;
     if (i < n) {
         const uint32_t k = queue[i];
+        item = st.item[k];
+        const SceneView& sc = src.sceneOf(item);
+        PathCtx c{sc, 0u, SpectralPath{}};
         const float4 o = st.ro[k], d = st.rd[k];
         THit h;
         closest(c, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), h);
         st.hit[k] = make_float4(__uint_as_float(h.prim), h.t, h.u, h.v);
+        const uint32_t nMats = src.nMatsOf(item);
         uint32_t key;
         if (h.prim == CR_MISS) key = nMats;
         else if (h.prim >= kSpherePrim) key = nMats + 1;
         else if (isSphereHit(h.prim)) key = __ldg(sc.sphMat + (h.prim & ~kSphereBit));
         else key = sc.meshes[sc.primToMesh[h.prim]].material_id;
-        keys[i] = key;
+        keys[i] = src.keyBase(item) + key;
+        rays = c.rays;
     }
-    addRays(rayCounter, c.rays);
+    addRays(src.raysOf(item), rays);
 }
 
 // Counting sort of the live paths by key.  Keys beyond kSmemKeys bins fall
@@ -253,21 +350,23 @@ __global__ void kWfAdvance(uint32_t* __restrict__ counts, uint32_t* __restrict__
 // The bounce after the query, for the live paths in material order.  Mode
 // supplies the hooks of shadeBounce (with their per-path state in st.aux)
 // and what happens to a path that ends.
-template <class Mode>
-__global__ void __launch_bounds__(kWfThreads) kWfShade(const SceneView sc, const Params p, WfState st,
+template <class Src, class Mode>
+__global__ void __launch_bounds__(kWfThreads) kWfShade(const __grid_constant__ Src src, WfState st,
                                                        const __grid_constant__ Mode mode,
                                                        const uint32_t* __restrict__ order,
                                                        const uint32_t* __restrict__ count, uint32_t depth,
-                                                       uint32_t* __restrict__ next, uint32_t* __restrict__ nextCount,
-                                                       unsigned long long* __restrict__ rayCounter) {
+                                                       uint32_t* __restrict__ next,
+                                                       uint32_t* __restrict__ nextCount) {
     const uint32_t n = *count;
     if (blockIdx.x * blockDim.x >= n) return;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    PathCtx c{sc, 0u, SpectralPath{}};
     bool push = false;
-    uint32_t k = 0;
+    uint32_t k = 0, item = 0, rays = 0;
     if (i < n) {
         k = order[i];
+        item = st.item[k];
+        const Params& p = src.paramsOf(item);
+        PathCtx c{src.sceneOf(item), 0u, SpectralPath{}};
         const uint4 meta = st.meta[k];
         c.spec = makeSpectralPath(p.spectral != 0, meta.x, meta.y, meta.z);
         Sampler smp = Sampler::resume(meta.w, st.inc[k]);
@@ -290,8 +389,9 @@ __global__ void __launch_bounds__(kWfThreads) kWfShade(const SceneView sc, const
             st.meta[k] = make_uint4(meta.x, meta.y, meta.z, smp.state);
             mode.keep(st, k, hk);
         } else {
-            mode.end(st, k, meta, c, radiance, make_float2(o.w, d.w), hk);
+            mode.end(src, item, st, k, meta, c, radiance, make_float2(o.w, d.w), hk);
         }
+        rays = c.rays;
     }
     // warp-aggregated append to the next queue
     const unsigned act = __activemask();
@@ -304,54 +404,81 @@ __global__ void __launch_bounds__(kWfThreads) kWfShade(const SceneView sc, const
         base = __shfl_sync(act, base, leader);
         if (push) next[base + __popc(m & ((1u << lane) - 1u))] = k;
     }
-    addRays(rayCounter, c.rays);
+    addRays(src.raysOf(item), rays);
 }
 
-// Paths never traced (max depth 0) end with zero radiance.
-template <class Mode>
-__global__ void kWfEndAll(const SceneView sc, const Params p, WfState st, const __grid_constant__ Mode mode,
-                          uint32_t n) {
+// Paths whose scene allows no bounce (max depth 0) end with zero radiance.
+template <class Src, class Mode>
+__global__ void __launch_bounds__(kWfThreads) kWfEndUntraced(const __grid_constant__ Src src, WfState st,
+                                                             const __grid_constant__ Mode mode, uint32_t n,
+                                                             const uint64_t* __restrict__ waveBase, uint64_t total,
+                                                             uint32_t* __restrict__ queue,
+                                                             uint32_t* __restrict__ liveCount) {
+    uint64_t base = 0;
+    n = waveSize(base, n, waveBase, total);
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const uint4 meta = st.meta[i];
-    PathCtx c{sc, 0u, SpectralPath{}};
-    c.spec = makeSpectralPath(p.spectral != 0, meta.x, meta.y, meta.z);
-    typename Mode::Hooks hk = mode.hooks(st, i, meta);
-    mode.end(st, i, meta, c, sp(0.0f), make_float2(st.ro[i].w, st.rd[i].w), hk);
+    bool push = false;
+    if (i < n) {
+        const uint32_t item = st.item[i];
+        const Params& p = src.paramsOf(item);
+        if (p.maxDepth > 0) {
+            push = true;
+        } else {
+            const uint4 meta = st.meta[i];
+            PathCtx c{src.sceneOf(item), 0u, SpectralPath{}};
+            c.spec = makeSpectralPath(p.spectral != 0, meta.x, meta.y, meta.z);
+            typename Mode::Hooks hk = mode.hooks(st, i, meta);
+            mode.end(src, item, st, i, meta, c, sp(0.0f), make_float2(st.ro[i].w, st.rd[i].w), hk);
+        }
+    }
+    const unsigned act = __activemask();
+    const unsigned m = __ballot_sync(act, push);
+    if (m) {
+        const int lane = threadIdx.x & 31;
+        const int leader = __ffs(m) - 1;
+        uint32_t base = 0;
+        if (lane == leader) base = atomicAdd(liveCount, (uint32_t)__popc(m));
+        base = __shfl_sync(act, base, leader);
+        if (push) queue[base + __popc(m & ((1u << lane) - 1u))] = i;
+    }
 }
 
-__global__ void kWfStart(uint32_t* __restrict__ counts, uint32_t n, uint32_t* __restrict__ hist, uint32_t nKeys) {
+__global__ void kWfNextWave(uint64_t* __restrict__ waveBase, uint32_t cap) { *waveBase += cap; }
+
+__global__ void kWfStart(uint32_t* __restrict__ counts, uint32_t* __restrict__ hist, uint32_t nKeys) {
     for (uint32_t k = threadIdx.x; k < nKeys; k += blockDim.x) hist[k] = 0;
     if (threadIdx.x == 0) {
-        counts[0] = n;
+        counts[0] = 0;
         counts[1] = 0;
     }
 }
 
 inline unsigned blocks(uint64_t n) { return (unsigned)((n + kWfThreads - 1) / kWfThreads); }
 
-// One wave of n paths (path k of the wave is path base + k of the render):
+// One wave of n paths (path k of the wave is path base + k of the source):
 // camera rays, then per bounce extend, histogram, scan, scatter, shade and
-// advance, on `stream` without waiting on the host.
-template <class Mode>
-int runWave(cr_scene* s, const Params& p, const Mode& mode, WfBuffers* b, uint64_t base, uint32_t n,
-            cudaStream_t stream) {
-    const uint32_t nKeys = s->nMats + 2;
-    const WfState st{b->ro, b->rd, b->beta, b->rad, b->meta, b->inc, b->hit, b->aux};
-    const SceneView v = s->view();
-    kWfInit<<<blocks(n), kWfThreads, 0, stream>>>(s->cam, p, st, base, n, b->qa);
+// advance, on `stream` without waiting on the host.  maxDepth bounds every
+// scene's max depth, nKeys the sort keys of all scenes.
+//
+// With waveBase set (device memory), the wave starts at *waveBase, holds
+// min(n, total - *waveBase) paths and advances *waveBase by n at its end, so
+// that the same launch sequence (a captured graph) replays wave after wave.
+template <class Src, class Mode>
+int runWave(const Src& src, const Mode& mode, WfBuffers* b, uint64_t base, uint32_t n, uint32_t maxDepth,
+            uint32_t nKeys, cudaStream_t stream, uint64_t* waveBase = nullptr, uint64_t total = 0) {
+    const WfState st{b->ro, b->rd, b->beta, b->rad, b->meta, b->inc, b->hit, b->aux, b->item};
+    kWfInit<Src><<<blocks(n), kWfThreads, 0, stream>>>(src, st, base, n, waveBase, total);
     CR_LAUNCH_CHECK();
-    if (p.maxDepth == 0) {
-        kWfEndAll<Mode><<<blocks(n), kWfThreads, 0, stream>>>(v, p, st, mode, n);
-        CR_LAUNCH_CHECK();
-        return CR_OK;
-    }
-    kWfStart<<<1, 256, 0, stream>>>(b->counts, n, b->hist, nKeys);
+    kWfStart<<<1, 256, 0, stream>>>(b->counts, b->hist, nKeys);
+    CR_LAUNCH_CHECK();
+    // the paths of scenes with max depth 0 end here; the others form the first queue
+    kWfEndUntraced<Src, Mode><<<blocks(n), kWfThreads, 0, stream>>>(src, st, mode, n, waveBase, total, b->qa,
+                                                                     b->counts);
     CR_LAUNCH_CHECK();
     uint32_t* live = b->qa;
     uint32_t* nextQ = b->qb;
-    for (uint32_t depth = 0; depth < p.maxDepth; depth++) {
-        kWfExtend<<<blocks(n), kWfThreads, 0, stream>>>(v, st, live, b->counts, s->nMats, b->keys, s->rayCounter);
+    for (uint32_t depth = 0; depth < maxDepth; depth++) {
+        kWfExtend<Src><<<blocks(n), kWfThreads, 0, stream>>>(src, st, live, b->counts, b->keys);
         CR_LAUNCH_CHECK();
         kWfHistogram<<<blocks(n), kWfThreads, 0, stream>>>(b->keys, b->counts, nKeys, b->hist);
         CR_LAUNCH_CHECK();
@@ -359,14 +486,37 @@ int runWave(cr_scene* s, const Params& p, const Mode& mode, WfBuffers* b, uint64
         CR_LAUNCH_CHECK();
         kWfScatter<<<blocks(n), kWfThreads, 0, stream>>>(b->keys, live, b->counts, nKeys, b->hist, b->sorted);
         CR_LAUNCH_CHECK();
-        kWfShade<Mode><<<blocks(n), kWfThreads, 0, stream>>>(v, p, st, mode, b->sorted, b->counts, depth, nextQ,
-                                                              b->counts + 1, s->rayCounter);
+        kWfShade<Src, Mode><<<blocks(n), kWfThreads, 0, stream>>>(src, st, mode, b->sorted, b->counts, depth, nextQ,
+                                                                   b->counts + 1);
         CR_LAUNCH_CHECK();
         kWfAdvance<<<1, 256, 0, stream>>>(b->counts, b->hist, nKeys);
         CR_LAUNCH_CHECK();
         std::swap(live, nextQ);
     }
+    if (waveBase) {
+        kWfNextWave<<<1, 1, 0, stream>>>(waveBase, n);
+        CR_LAUNCH_CHECK();
+    }
     return CR_OK;
+}
+
+// The plain path tracer: an ending path splats its radiance into its
+// scene's film (SensorData::addSample, Core/Sensor.cu:19-43).
+struct PlainMode {
+    using Hooks = NoHooks;
+    __device__ __forceinline__ Hooks hooks(const WfState&, uint32_t, const uint4&) const { return NoHooks{}; }
+    __device__ __forceinline__ void keep(const WfState&, uint32_t, const Hooks&) const {}
+    template <class Src>
+    __device__ __forceinline__ void end(const Src& src, uint32_t item, const WfState&, uint32_t, const uint4&,
+                                        const PathCtx& c, const Spec& L, float2 pix, const Hooks&) const {
+        splatGlobal(src.camOf(item), pix, pathSpecToRgb(c.spec, L, src.paramsOf(item).wb), src.filmRgbOf(item),
+                    src.filmWOf(item));
+    }
+};
+
+// The single-scene source of a scene and its integrator parameters.
+inline OneScene oneScene(cr_scene* s, const Params& p) {
+    return OneScene{s->view(), s->cam, p, s->filmRgb, s->filmW, s->rayCounter, s->nMats};
 }
 
 }  // namespace

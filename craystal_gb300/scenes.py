@@ -463,3 +463,111 @@ def export_obj_scene(data: SceneData, cam: Camera, xml_path: str) -> str:
                 f.write(f'<light mtlname="mat{k}" radiance="{m.emission[0]:.9g},{m.emission[1]:.9g},'
                         f'{m.emission[2]:.9g}"/>\n')
     return base + ".xml"
+
+
+def _fbm_grid(n: int, octaves: int, seed: int, base_res: int = 8) -> np.ndarray:
+    """fBm of 2D value noise sampled on an n x n grid over the unit square:
+    octave o has a (base_res 2^o + 1)^2 lattice of uniform values, smoothstep-
+    bilinear interpolation, amplitude 2^-o; result normalised to [0, 1]."""
+    rng = np.random.default_rng(seed)
+    t = np.linspace(0.0, 1.0, n, dtype=np.float64)
+    h = np.zeros((n, n), np.float32)
+    for o in range(octaves):
+        res = base_res << o
+        lat = rng.random((res + 1, res + 1)).astype(np.float32)
+        x = t * res
+        i0 = np.minimum(np.floor(x).astype(np.int64), res - 1)
+        f = (x - i0).astype(np.float32)
+        w1 = f * f * (3.0 - 2.0 * f)
+        w0 = 1.0 - w1
+        amp = np.float32(0.5 ** o)
+        h += amp * (lat[np.ix_(i0, i0)] * (w0[:, None] * w0[None, :]) +
+                    lat[np.ix_(i0 + 1, i0)] * (w1[:, None] * w0[None, :]) +
+                    lat[np.ix_(i0, i0 + 1)] * (w0[:, None] * w1[None, :]) +
+                    lat[np.ix_(i0 + 1, i0 + 1)] * (w1[:, None] * w1[None, :]))
+    h -= h.min()
+    h /= max(float(h.max()), 1e-6)
+    return h
+
+
+def _box_soup(centers, halves, angles):
+    """Vectorised boxes: 12 outward-facing triangles per box with flat normals
+    (positions, normals: (36 n) x 3; indices 0 .. 36 n - 1)."""
+    corners = np.array([[sx, sy, sz] for sx in (-1, 1) for sy in (-1, 1) for sz in (-1, 1)], np.float64)
+    quads = [(0, 1, 3, 2), (4, 6, 7, 5), (0, 4, 5, 1), (2, 3, 7, 6), (0, 2, 6, 4), (1, 5, 7, 3)]
+    tri = []
+    for a, b, c, d in quads:
+        tri += [(a, b, c), (a, c, d)]
+    tri = np.array(tri)
+    local = corners[tri]                                    # 12 x 3 x 3 (unit cube corners)
+    n0 = np.cross(local[:, 1] - local[:, 0], local[:, 2] - local[:, 0])
+    flip = (n0 * local.mean(1)).sum(1) < 0                  # orient outward
+    local[flip] = local[flip][:, [0, 2, 1]]
+    p = local[None] * halves[:, None, None, :]              # n x 12 x 3 x 3
+    ca, sa = np.cos(angles)[:, None, None], np.sin(angles)[:, None, None]
+    x, z = p[..., 0].copy(), p[..., 2].copy()
+    p[..., 0] = ca * x + sa * z
+    p[..., 2] = -sa * x + ca * z
+    p += centers[:, None, None, :]
+    nrm = np.cross(p[:, :, 1] - p[:, :, 0], p[:, :, 2] - p[:, :, 0])
+    nrm /= np.linalg.norm(nrm, axis=-1, keepdims=True)
+    pos = p.reshape(-1, 3).astype(np.float32)
+    nrm = np.repeat(nrm[:, :, None, :], 3, axis=2).reshape(-1, 3).astype(np.float32)
+    return pos, nrm, np.arange(len(pos), dtype=np.uint32)
+
+
+def large_terrain_scene(width: int = 3840, height: int = 2160, grid: int = 4096, n_boxes: int = 10000,
+                        seed: int = 7, extent: float = 200.0, relief: float = 25.0):
+    """Returns (SceneData, Camera, environment, sphere_lights) of the large
+    workload: a grid x grid heightfield (2 (grid - 1)^2 triangles; 33.5M for
+    4096) of 6-octave fBm heights over [-extent/2, extent/2]^2, 10k boxes of
+    scale log-uniform 0.5-20 standing on it, Principled materials, a sun
+    sphere light and a constant sky."""
+    rng = np.random.default_rng(seed)
+    h = _fbm_grid(grid, 6, seed) * np.float32(relief)
+    t = np.linspace(-extent / 2, extent / 2, grid, dtype=np.float32)
+    xx, zz = np.meshgrid(t, t, indexing="ij")
+    pos = np.stack([xx, h, zz], -1).reshape(-1, 3)
+    dh_x = np.gradient(h, t, axis=0)
+    dh_z = np.gradient(h, t, axis=1)
+    nrm = np.stack([-dh_x, np.ones_like(h), -dh_z], -1).reshape(-1, 3)
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    i = np.arange(grid - 1, dtype=np.uint32)
+    v00 = (i[:, None] * grid + i[None, :]).reshape(-1)
+    v10, v01, v11 = v00 + grid, v00 + 1, v00 + grid + 1
+    idx = np.empty((len(v00), 2, 3), np.uint32)
+    idx[:, 0] = np.stack([v00, v01, v11], -1)  # normals point up (+y)
+    idx[:, 1] = np.stack([v00, v11, v10], -1)
+    mats = [MaterialData(diffuseRefl=(0.42, 0.38, 0.30), specularRefl=(0.04, 0.04, 0.04), shininess=3.0,
+                         type=MaterialType.Principled)]
+    meshes = [MeshData(position=pos.astype(np.float32), normal=nrm.astype(np.float32), index=idx.reshape(-1),
+                       materialID=0)]
+    # boxes on the terrain, in 4 material groups
+    cx = rng.uniform(-extent * 0.45, extent * 0.45, n_boxes)
+    cz = rng.uniform(-extent * 0.45, extent * 0.45, n_boxes)
+    scale = np.exp(rng.uniform(np.log(0.5), np.log(20.0), n_boxes))
+    halves = scale[:, None] * rng.uniform(0.3, 1.0, (n_boxes, 3)) * 0.5
+    gi = np.clip(((cx + extent / 2) / extent * (grid - 1)).astype(np.int64), 0, grid - 1)
+    gj = np.clip(((cz + extent / 2) / extent * (grid - 1)).astype(np.int64), 0, grid - 1)
+    centers = np.stack([cx, h[gi, gj] + halves[:, 1] * 0.9, cz], -1)
+    angles = rng.uniform(0.0, np.pi / 2, n_boxes)
+    group = rng.integers(0, 4, n_boxes)
+    for g in range(4):
+        base = rng.uniform(0.2, 0.9, 3)
+        metal = g == 3
+        mats.append(MaterialData(diffuseRefl=tuple(base), specularRefl=(0.9, 0.9, 0.9) if metal else (0.04,) * 3,
+                                 shininess=float(rng.uniform(5, 200)), type=MaterialType.Principled))
+        sel = group == g
+        p, n, ix = _box_soup(centers[sel], halves[sel], angles[sel])
+        meshes.append(MeshData(position=p, normal=n, index=ix, materialID=len(mats) - 1))
+    for m in mats:
+        m.finalize()
+    cam = Camera()
+    cam.setWorldPosition((-extent * 0.42, relief * 2.2, -extent * 0.42))
+    cam.setTarget((0.0, relief * 0.3, 0.0))
+    cam.setUp((0.0, 1.0, 0.0))
+    cam.setFovY(50.0)
+    cam.setSensor(Sensor((width, height)))
+    env = (0.35, 0.45, 0.65)
+    sun = [((extent * 2.0, extent * 3.0, extent * 1.0), extent * 0.12, (60.0, 55.0, 45.0))]
+    return SceneData(meshes=meshes, materials=mats, emissiveIndex=[]), cam, env, sun

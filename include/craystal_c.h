@@ -456,15 +456,22 @@ int cr_render_cached(cr_scene* scene, const cr_integrator_config* cfg,
                      uint32_t first_sample, void* stream, cr_cache_stats* stats);
 
 /* ---- batched rendering (no counterpart in the reference) ----
- * Many scenes (each with its camera and film set) rendered by one
- * persistent launch that replays a captured CUDA graph: work items (scene,
- * pixel tile, run of spp_per_item sample indices) are taken from one queue,
- * largest scenes first.  Each scene's film receives exactly the samples
- * cr_render(scene, config, spp, first_sample) would add; the k-th
- * cr_batch_render of a batch uses sample indices first_sample + k*spp.
- * cr_batch_autotune times every (tile 8|16) x (spp_per_item 1,2,4,8,16) on the
- * batch itself, keeps the fastest and clears the films it rendered into.
- * The scenes must outlive the batch and keep their camera size. */
+ * Many scenes (each with its camera and film set) rendered from captured
+ * CUDA graphs, on one of two schedules:
+ *   - persistent megakernel (wave_log2 = 0): one persistent launch whose
+ *     blocks take work items (scene, pixel tile, run of spp_per_item sample
+ *     indices) from one queue, largest scenes first;
+ *   - wavefront (wave_log2 = 16..23): the paths of all scenes form one
+ *     sequence, rendered in waves of 2^wave_log2 paths; every bounce sorts
+ *     the live paths by (scene, material), so a wave mixes scenes and the
+ *     small ones fill the GPU beside the large ones.  One captured graph of
+ *     a wave is replayed wave after wave.
+ * Each scene's film receives exactly the samples cr_render(scene, config,
+ * spp, first_sample) would add; the k-th cr_batch_render of a batch uses
+ * sample indices first_sample + k*spp.  cr_batch_autotune times every
+ * (tile 8|16) x (spp_per_item 1,2,4,8,16) and every wave size 2^19..2^22
+ * on the batch itself, keeps the fastest and clears the films it rendered
+ * into.  The scenes must outlive the batch and keep their camera size. */
 typedef struct cr_batch cr_batch;
 typedef struct {
     cr_integrator_config config;
@@ -472,9 +479,10 @@ typedef struct {
     uint32_t first_sample;
 } cr_batch_item;
 typedef struct {
-    uint32_t tile;          /* 8 or 16 pixels square */
-    uint32_t spp_per_item;  /* sample indices per work item */
-    uint32_t blocks_per_sm; /* 0 = as many as fit */
+    uint32_t tile;          /* persistent: 8 or 16 pixels square */
+    uint32_t spp_per_item;  /* persistent: sample indices per work item */
+    uint32_t blocks_per_sm; /* persistent: 0 = as many as fit */
+    uint32_t wave_log2;     /* 0 = persistent megakernel; 16..23 = wavefront waves of 2^wave_log2 paths */
 } cr_batch_tuning;
 typedef struct {
     cr_batch_tuning tuning;

@@ -1,8 +1,9 @@
-"""Batched rendering (cr_batch_*): many scenes of uneven size in one
-persistent launch replayed from a CUDA graph.  Each scene's film must equal
-what cr_render adds for the same sample indices (float-atomic summation
-order aside), successive replays must advance the sample indices, and the
-autotuner must time every tuning and leave the films cleared."""
+"""Batched rendering (cr_batch_*): many scenes of uneven size from captured
+CUDA graphs, on the persistent megakernel or the many-scene wavefront.
+Each scene's film must equal what cr_render adds for the same sample
+indices (float-atomic summation order aside), successive replays must
+advance the sample indices, and the autotuner must time every tuning and
+leave the films cleared."""
 import numpy as np
 import pytest
 
@@ -26,11 +27,11 @@ def make_batch(n=5):
     return params, scs, integs
 
 
-@pytest.mark.parametrize("tile,run", [(16, 4), (8, 1), (8, 16)])
-def test_batch_equals_per_scene_renders(gpu_lib, tile, run):
+@pytest.mark.parametrize("tile,run,wave", [(16, 4, 0), (8, 1, 0), (8, 16, 0), (16, 4, 16), (16, 4, 20)])
+def test_batch_equals_per_scene_renders(gpu_lib, tile, run, wave):
     params, scs, integs = make_batch()
     b = BatchRenderer(scs, integs, [p["spp"] for p in params], first_sample=[7] * len(params))
-    b.set_tuning(tile, run)
+    b.set_tuning(tile, run, wave_log2=wave)
     b.render()
     batch = [sc.film_read() for sc in scs]
     rays = [sc.render_ray_count() for sc in scs]
@@ -43,9 +44,11 @@ def test_batch_equals_per_scene_renders(gpu_lib, tile, run):
         assert sc.render_ray_count() == r
 
 
-def test_batch_replays_advance_samples(gpu_lib):
+@pytest.mark.parametrize("wave", [0, 17])
+def test_batch_replays_advance_samples(gpu_lib, wave):
     params, scs, integs = make_batch(3)
     b = BatchRenderer(scs, integs, [p["spp"] for p in params])
+    b.set_tuning(8, 2, wave_log2=wave)
     b.render()
     w1 = [sc.film_read()[1].copy() for sc in scs]
     b.render()  # sample indices spp .. 2*spp - 1
@@ -60,10 +63,10 @@ def test_autotune_times_every_tuning_and_clears(gpu_lib, tmp_path):
     params, scs, integs = make_batch(4)
     b = BatchRenderer(scs, integs, [p["spp"] for p in params])
     out = b.autotune(json_path=str(tmp_path / "tuning.json"))
-    assert len(out["timings_ms"]) == 10
+    assert len(out["timings_ms"]) == 14
     best = min(out["timings_ms"], key=lambda r: r["ms"])
-    assert out["best"] == {"tile": best["tile"], "spp_per_item": best["spp_per_item"]}
-    assert b.tuning()["tile"] == best["tile"]
+    assert out["best"] == {"tile": best["tile"], "spp_per_item": best["spp_per_item"], "wave_log2": best["wave_log2"]}
+    assert b.tuning()["wave_log2"] == best["wave_log2"]
     for sc in scs:
         rgb, w = sc.film_read()
         assert not w.any() and sc.render_ray_count() == 0
