@@ -188,9 +188,24 @@ def cornell_extra(torch):
     ms = e0.elapsed_time(e1)
     rays = sc.render_ray_count()
     paths = 256 * 256 * spp * reps
-    return {"config": "cornell 256x256, 16 spp, max depth 8, NEE+MIS", "Mpaths_s": round(paths / ms / 1e3, 2),
-            "Mrays_s": round(rays / ms / 1e3, 2), "ms_per_16spp": round(ms / reps, 3),
-            "rays_per_path": round(rays / paths, 3)}
+    out = {"config": "cornell 256x256, 16 spp, max depth 8, NEE+MIS (default schedule: wavefront)",
+           "Mpaths_s": round(paths / ms / 1e3, 2), "Mrays_s": round(rays / ms / 1e3, 2),
+           "ms_per_16spp": round(ms / reps, 3), "rays_per_path": round(rays / paths, 3)}
+    # the reference's own path tracer restated (W x H grid of 16 x 16 blocks, a launch and a
+    # device sync per sample, 36-byte nodes, closest-hit shadow rays, atomic film)
+    from baseline.restated import RestatedPathTracer
+    from craystal_gb300.api import flatten_scene
+    ref = RestatedPathTracer(sc, flatten_scene(data))
+    ref.render(cam, 2, max_depth=8, rr_threshold=0.05)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    _, ref_rays = ref.render(cam, spp, max_depth=8, rr_threshold=0.05)
+    ref_s = time.perf_counter() - t
+    out["restated_reference_path_tracer"] = {
+        "Mpaths_s": round(256 * 256 * spp / ref_s / 1e6, 2), "Mrays_s": round(ref_rays / ref_s / 1e6, 2),
+        "ms_per_16spp": round(ref_s * 1e3, 3)}
+    out["speedup_over_restated_reference"] = round(out["Mpaths_s"] / out["restated_reference_path_tracer"]["Mpaths_s"], 2)
+    return out
 
 
 def wavefront_extra(torch):

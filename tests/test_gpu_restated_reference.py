@@ -1,7 +1,10 @@
-"""The restated reference traversal (the comparator bench.py times) must do
-the reference's work: on the reference-layout tree the product exports, its
-closest hits equal the oracle's up to the last bits that FMA contraction
-changes (the reference's CUDA build contracts; the oracle does not)."""
+"""The restated reference kernels (the comparators bench.py times) must do
+the reference's work: on the reference-layout tree the product exports, the
+restated traversal's closest hits equal the oracle's up to the last bits
+that FMA contraction changes (the reference's CUDA build contracts; the
+oracle does not), and the restated path tracer renders the product's image
+(same estimator and sample indices; FMA contraction makes paths diverge
+now and then, so the films agree statistically) with about the same rays."""
 import numpy as np
 import pytest
 
@@ -33,3 +36,19 @@ def test_restated_reference_matches_oracle(gpu_lib, n_tris):
     both = (got["prim"] == want["prim"]) & (want["prim"] != 0xFFFFFFFF)
     np.testing.assert_allclose(got["t"][both], want["t"][both], rtol=1e-4)
     assert RAY_DTYPE.itemsize == 32
+
+
+def test_restated_path_tracer_renders_the_same_image(gpu_lib):
+    from baseline.restated import RestatedPathTracer
+    from craystal_gb300.api import PathTraceIntegrator
+    data, cam = scenes.cornell_box(seed=3, width=48, height=48)
+    sc = Scene(data)
+    sc.setCamera(cam)
+    (rgb, w), rays = RestatedPathTracer(sc, flatten_scene(data)).render(cam, 64, max_depth=8, rr_threshold=0.05)
+    sc.film_clear()
+    PathTraceIntegrator(PathTraceIntegrator.Configs(maxDepth=8, rrThreshold=0.05), compat=False).dispatch(sc, 64)
+    ours = cam.sensor.createImage()
+    ref = rgb / w[..., None]
+    err = float(np.mean((np.nan_to_num(ref) - np.nan_to_num(ours)) ** 2 / (np.nan_to_num(ours) ** 2 + 1e-2)))
+    assert err < 2e-3, err
+    assert abs(rays / sc.render_ray_count() - 1.0) < 0.02
