@@ -166,35 +166,38 @@ def run_reference(args):
 
 def cornell_extra(torch):
     """The plain path tracer on the procedural Cornell box, 256x256, 16 spp,
-    max depth 8, NEE + MIS: Mpaths/s and Mrays/s of the render."""
+    max depth 8, NEE + MIS, hero-wavelength spectral (the C1 config) and RGB,
+    on the default (wavefront) schedule: Mpaths/s and Mrays/s; beside it the
+    reference's own path tracer restated in CUDA and the CPU oracle's path
+    tracer on all host cores (RGB, a bounded number of samples)."""
     from craystal_gb300 import scenes
-    from craystal_gb300.api import PathTraceIntegrator, Scene
+    from craystal_gb300.api import PathTraceIntegrator, Scene, flatten_scene
     data, cam = scenes.cornell_box(seed=0, width=256, height=256)
     sc = Scene(data)
     sc.setCamera(cam)
-    integ = PathTraceIntegrator(PathTraceIntegrator.Configs(maxDepth=8, rrThreshold=0.05, useMIS=True), compat=False)
-    integ.dispatch(sc, 16, readback=False)
-    torch.cuda.synchronize()
-    sc.film_clear()
-    spp = 16
+    cfg = PathTraceIntegrator.Configs(maxDepth=8, rrThreshold=0.05, useMIS=True)
+    spp, reps = 16, 5
     s = torch.cuda.current_stream()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    reps = 5
-    e0.record(s)
-    for r in range(reps):
-        integ.dispatch(sc, spp, first_sample=r * spp, stream=s.cuda_stream, readback=False)
-    e1.record(s)
-    e1.synchronize()
-    ms = e0.elapsed_time(e1)
-    rays = sc.render_ray_count()
-    paths = 256 * 256 * spp * reps
-    out = {"config": "cornell 256x256, 16 spp, max depth 8, NEE+MIS (default schedule: wavefront)",
-           "Mpaths_s": round(paths / ms / 1e3, 2), "Mrays_s": round(rays / ms / 1e3, 2),
-           "ms_per_16spp": round(ms / reps, 3), "rays_per_path": round(rays / paths, 3)}
+    out = {"config": "cornell 256x256, 16 spp, max depth 8, NEE+MIS, default schedule (wavefront)"}
+    for label, spectral in (("spectral", True), ("rgb", False)):
+        integ = PathTraceIntegrator(cfg, compat=False, spectral=spectral)
+        integ.dispatch(sc, spp, readback=False)
+        torch.cuda.synchronize()
+        sc.film_clear()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for r in range(reps):
+            integ.dispatch(sc, spp, first_sample=r * spp, stream=s.cuda_stream, readback=False)
+        e1.record(s)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        rays = sc.render_ray_count()
+        paths = 256 * 256 * spp * reps
+        out[label] = {"Mpaths_s": round(paths / ms / 1e3, 2), "Mrays_s": round(rays / ms / 1e3, 2),
+                      "ms_per_16spp": round(ms / reps, 3), "rays_per_path": round(rays / paths, 3)}
     # the reference's own path tracer restated (W x H grid of 16 x 16 blocks, a launch and a
-    # device sync per sample, 36-byte nodes, closest-hit shadow rays, atomic film)
+    # device sync per sample, 36-byte nodes, closest-hit shadow rays, atomic film); RGB
     from baseline.restated import RestatedPathTracer
-    from craystal_gb300.api import flatten_scene
     ref = RestatedPathTracer(sc, flatten_scene(data))
     ref.render(cam, 2, max_depth=8, rr_threshold=0.05)
     torch.cuda.synchronize()
@@ -204,7 +207,79 @@ def cornell_extra(torch):
     out["restated_reference_path_tracer"] = {
         "Mpaths_s": round(256 * 256 * spp / ref_s / 1e6, 2), "Mrays_s": round(ref_rays / ref_s / 1e6, 2),
         "ms_per_16spp": round(ref_s * 1e3, 3)}
-    out["speedup_over_restated_reference"] = round(out["Mpaths_s"] / out["restated_reference_path_tracer"]["Mpaths_s"], 2)
+    out["speedup_over_restated_reference_rgb"] = round(out["rgb"]["Mpaths_s"] /
+                                                       out["restated_reference_path_tracer"]["Mpaths_s"], 2)
+    # the CPU oracle's path tracer, all host threads, a bounded sample of spp
+    import oracle
+    threads = oracle.hardware_threads()
+    osc = oracle.OracleScene(flatten_scene(data))
+    oc = oracle.make_camera(cam.posW, cam.target, cam.up, cam.fovY, 256, 256)
+    t = time.perf_counter()
+    _, orays = osc.render(oc, 8, 0.05, True, spp=1, threads=threads)
+    one = time.perf_counter() - t
+    cpu_spp = max(1, min(16, int(8.0 / max(one, 1e-3))))
+    t = time.perf_counter()
+    _, orays = osc.render(oc, 8, 0.05, True, spp=cpu_spp, first_sample=1, threads=threads)
+    cpu_s = time.perf_counter() - t
+    out["cpu_oracle"] = {"Mpaths_s": round(256 * 256 * cpu_spp / cpu_s / 1e6, 3),
+                         "Mrays_s": round(orays / cpu_s / 1e6, 3), "threads": threads, "spp": cpu_spp}
+    return out
+
+
+def c3_extra(torch, res=(480, 270), budgets=(16, 64, 256)):
+    """The radiance-cache config: 8 displaced icospheres (2.6M triangles),
+    Principled materials, constant environment 0.5 and one sphere light, max
+    depth 16.  Plain throughput at 1920x1080, 64 spp; the equal-time cache
+    comparison at res (reference: 4096 spp of the plain tracer, FP64 film
+    sum; the cache trained from scratch inside its time)."""
+    from craystal_gb300 import scenes
+    from craystal_gb300.api import CachedPathTraceIntegrator, PathTraceIntegrator, RadianceCache, Scene
+    cfg = PathTraceIntegrator.Configs(maxDepth=16, rrThreshold=0.05, useMIS=True)
+    plain = PathTraceIntegrator(cfg, compat=False)
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        fn()
+        torch.cuda.synchronize()
+        return time.perf_counter() - t
+
+    data, cam, env, sph = scenes.cache_scene(seed=0, width=1920, height=1080)
+    sc = Scene(data)
+    sc.setCamera(cam)
+    sc.set_environment(env)
+    sc.set_sphere_lights(sph)
+    plain.dispatch(sc, 1, readback=False)
+    sc.film_clear()
+    dt = timed(lambda: plain.dispatch(sc, 64, readback=False))
+    rays = sc.render_ray_count()
+    out = {"config": "8 displaced icospheres (2.6M tris), Principled, env 0.5 + sphere light, depth 16",
+           "plain_1080p_64spp": {"s": round(dt, 3), "Mpaths_s": round(1920 * 1080 * 64 / dt / 1e6, 1),
+                                 "Mrays_s": round(rays / dt / 1e6, 1), "triangles": int(sc.n_tris)}}
+    w, h = res
+    cam.setSensor(type(cam.sensor)((w, h)))
+    sc.setCamera(cam)
+    acc = np.zeros((h, w, 3))
+    accw = np.zeros((h, w))
+    for k in range(8):
+        sc.film_clear()
+        plain.dispatch(sc, 512, first_sample=1_000_000 + 512 * k, readback=False)
+        rgb, wt = sc.film_read()
+        acc += rgb
+        accw += wt
+    ref = acc / accw[..., None]
+
+    def rel_mse(rgb, wt):
+        img = np.nan_to_num((rgb / wt[..., None]).astype(np.float64))
+        return float(np.mean((img - ref) ** 2 / (ref ** 2 + 1e-2)))
+
+    probe = CachedPathTraceIntegrator(cfg, train_every=16, cache=RadianceCache(seed=1))
+    probe.dispatch(sc, 16, first_sample=2_000_000, readback=False)
+    t_frame = timed(lambda: probe.dispatch(sc, 32, first_sample=3_000_000, readback=False)) / 32
+    rows = equal_time_trials(sc, cfg, plain, rel_mse, timed, t_frame, budgets)
+    out["equal_time"] = {"resolution": [w, h], "reference_spp": 4096, "ms_per_cached_frame": round(t_frame * 1e3, 3),
+                         "budgets": rows}
+    sc.close()
     return out
 
 
@@ -314,15 +389,44 @@ def cache_frames_extra(torch, res=512, frames=32):
             "cache_ms_per_frame": round(1e3 * tc / frames, 3), "plain_ms_per_spp": round(1e3 * tp / frames, 3)}
 
 
-def cache_extra(torch, res=512):
+def equal_time_trials(sc, cfg, plain, rel_mse, timed, t_frame, budgets, trials=3):
+    """Per budget (plain spp): `trials` independent pairs of (plain render,
+    fresh cache trained and rendering inside the plain render's time) on
+    disjoint sample indices and network seeds; relMSE is heavy-tailed
+    (rare bright paths), so every trial and the median ratio are reported."""
+    from craystal_gb300.api import CachedPathTraceIntegrator, RadianceCache
+    rows = []
+    for spp in budgets:
+        trials_out = []
+        for k in range(trials):
+            sc.film_clear()
+            t_plain = timed(lambda: plain.dispatch(sc, spp, first_sample=10_000_000 * (k + 1), readback=False))
+            e_plain = rel_mse(*sc.film_read())
+            frames = max(1, int(t_plain / t_frame))
+            integ = CachedPathTraceIntegrator(cfg, train_every=16, cache=RadianceCache(seed=k))
+            sc.film_clear()
+            t_cache = timed(lambda: integ.dispatch(sc, frames, first_sample=50_000_000 + 10_000_000 * k,
+                                                   readback=False))
+            e_cache = rel_mse(*sc.film_read())
+            trials_out.append({"plain_s": round(t_plain, 4), "plain_relmse": round(e_plain, 5), "cache_frames": frames,
+                               "cache_s": round(t_cache, 4), "cache_relmse": round(e_cache, 5),
+                               "ratio": round(e_plain / e_cache, 3)})
+        ratios = sorted(t["ratio"] for t in trials_out)
+        rows.append({"plain_spp": spp, "median_ratio_plain_over_cache": ratios[len(ratios) // 2],
+                     "trials": trials_out})
+    return rows
+
+
+def cache_extra(torch, res=512, budgets=(64, 256, 1024)):
     """Equal-time relMSE of the radiance-cache integrator against the plain
-    path tracer on the Cornell box (res x res, max depth 8, NEE + MIS).  The
-    reference is the plain tracer at 4096 spp with its films of 512-spp
-    passes summed in FP64.  The plain arm renders 64 spp; the cache arm,
-    after 64 untimed training frames, renders as many frames (1 spp each,
-    training included) as fit in the plain arm's time."""
+    path tracer on the Cornell box (res x res, max depth 8, NEE + MIS), both
+    on the default (wavefront) schedule.  The reference is the plain tracer
+    at 16384 spp with its films of 512-spp passes summed in FP64.  For each
+    budget the plain tracer renders that many spp in time T; a fresh cache
+    (untrained network) then renders, trains and renders as many frames (1
+    spp each) as fit in T, its training included."""
     from craystal_gb300 import scenes
-    from craystal_gb300.api import CachedPathTraceIntegrator, PathTraceIntegrator, Scene
+    from craystal_gb300.api import CachedPathTraceIntegrator, PathTraceIntegrator, RadianceCache, Scene
     data, cam = scenes.cornell_box(seed=0, width=res, height=res)
     sc = Scene(data)
     sc.setCamera(cam)
@@ -330,7 +434,7 @@ def cache_extra(torch, res=512):
     plain = PathTraceIntegrator(cfg, compat=False)
     acc = np.zeros((res, res, 3))
     accw = np.zeros((res, res))
-    for k in range(8):
+    for k in range(32):
         sc.film_clear()
         plain.dispatch(sc, 512, first_sample=1_000_000 + 512 * k, readback=False)
         rgb, w = sc.film_read()
@@ -349,22 +453,14 @@ def cache_extra(torch, res=512):
         torch.cuda.synchronize()
         return time.perf_counter() - t
 
-    sc.film_clear()
-    t_plain = timed(lambda: plain.dispatch(sc, 64, readback=False))
-    e_plain = rel_mse(*sc.film_read())
-    integ = CachedPathTraceIntegrator(cfg, train_every=16)
-    integ.dispatch(sc, 64, first_sample=2_000_000, readback=False)
-    sc.film_clear()
-    t16 = timed(lambda: integ.dispatch(sc, 16, first_sample=3_000_000, readback=False))
-    frames = max(1, int(16 * t_plain / t16))
-    sc.film_clear()
-    t_cache = timed(lambda: integ.dispatch(sc, frames, readback=False))
-    e_cache = rel_mse(*sc.film_read())
-    return {"config": f"cornell {res}x{res}, max depth 8, NEE+MIS; reference 4096 spp plain, FP64 film sum",
-            "plain_spp": 64, "plain_s": round(t_plain, 4), "plain_relmse": round(e_plain, 5),
-            "cache_frames": frames, "cache_s": round(t_cache, 4), "cache_relmse": round(e_cache, 5),
-            "relmse_ratio_plain_over_cache": round(e_plain / e_cache, 3),
-            "train_every": 16, "query_vertex": 1, "last_loss": round(float(integ.stats.last_loss), 5)}
+    # cost of a cached frame, from a separate cache
+    probe = CachedPathTraceIntegrator(cfg, train_every=16, cache=RadianceCache(seed=1))
+    probe.dispatch(sc, 16, first_sample=2_000_000, readback=False)
+    t_frame = timed(lambda: probe.dispatch(sc, 32, first_sample=3_000_000, readback=False)) / 32
+    rows = equal_time_trials(sc, cfg, plain, rel_mse, timed, t_frame, budgets)
+    return {"config": f"cornell {res}x{res}, max depth 8, NEE+MIS; reference 16384 spp plain, FP64 film sum; "
+                      "cache trained from scratch inside its time; 3 independent trials per budget",
+            "ms_per_cached_frame": round(t_frame * 1e3, 3), "train_every": 16, "query_vertex": 1, "budgets": rows}
 
 
 def batch_extra(torch, n_scenes=64):
@@ -523,6 +619,7 @@ def run_ours(args):
         extra["path_tracer"] = cornell_extra(torch)
         extra["wavefront_vs_megakernel"] = wavefront_extra(torch)
         extra["radiance_cache_equal_time"] = cache_extra(torch, args.cache_res)
+        extra["radiance_cache_scene"] = c3_extra(torch)
         extra["batched_scenes"] = batch_extra(torch, args.batch_scenes)
         extra["large_scene"] = large_scene_extra(torch)
 
@@ -575,6 +672,8 @@ def run_only(args):
         r = cache_frames_extra(torch, args.cache_res)
     elif args.only == "large_scene":
         r = large_scene_extra(torch)
+    elif args.only == "radiance_cache_scene":
+        r = c3_extra(torch)
     else:
         r = batch_extra(torch, args.batch_scenes)
     print(json.dumps({args.only: r}), flush=True)
@@ -591,7 +690,7 @@ def main():
     ap.add_argument("--rays", type=int, default=N_RAYS, help="rays per step (profiling a smaller case)")
     ap.add_argument("--tris", type=int, default=N_TRIS, help="triangles (profiling a smaller case)")
     ap.add_argument("--only", choices=["path_tracer", "wavefront", "radiance_cache", "cache_frames", "batched_scenes",
-                                       "large_scene"],
+                                       "large_scene", "radiance_cache_scene"],
                     help="run one secondary workload alone and print its figures (profiling)")
     ap.add_argument("--cache-res", type=int, default=512, help="radiance-cache workload resolution")
     ap.add_argument("--batch-scenes", type=int, default=64, help="scenes in the batched workload")

@@ -103,6 +103,19 @@ __device__ __forceinline__ bool occluded(PathCtx& c, float3 o, float3 d, float t
     return traverse<true>(c.sc, r, h);
 }
 
+#if defined(CR_SECONDARY_NOINLINE)
+// experiment: the shadow and MIS rays' queries out of line
+static __device__ __noinline__ bool closestSecondary(PathCtx* c, float3 o, float3 d, THit* h) { return closest(*c, o, d, *h); }
+static __device__ __noinline__ bool occludedSecondary(PathCtx* c, float3 o, float3 d, float tMax) {
+    return occluded(*c, o, d, tMax);
+}
+#define CR_CLOSEST2(c, o, d, h) closestSecondary(&(c), o, d, &(h))
+#define CR_OCCLUDED2(c, o, d, t) occludedSecondary(&(c), o, d, t)
+#else
+#define CR_CLOSEST2(c, o, d, h) closest(c, o, d, h)
+#define CR_OCCLUDED2(c, o, d, t) occluded(c, o, d, t)
+#endif
+
 struct LightSample {
     Spec weight;
     float3 dirW;
@@ -138,7 +151,7 @@ __device__ __forceinline__ LightSample sampleLight(PathCtx& c, const Isect& it, 
     if (dot(ofn, dir) < 0.0f || dot(vn, dir) > 0.0f || dist < kEps) return ls;
     const float3 so = offsetRayOrigin(it.posW, ofn);
     const float tMax = length(sub(so, target)) - kEps;
-    if (occluded(c, so, dir, tMax)) return ls;
+    if (CR_OCCLUDED2(c, so, dir, tMax)) return ls;
     const MaterialGpu& m = materialOf(sc, id);
     ls.weight = mul(bsdf.evaluate(it.viewW, dir), emissionOf(c, m));
     ls.dirW = dir;
@@ -168,7 +181,7 @@ __device__ __forceinline__ Spec evalMIS(PathCtx& c, const Isect& it, const Bsdf&
         if (maxValue(w) > 0.0f && bsdfPdf > 0.0f) {
             const float3 o = offsetRayOrigin(it.posW, it.orientedFaceNormal());
             THit h;
-            if (closest(c, o, dir, h) && h.prim == ls.id) {
+            if (CR_CLOSEST2(c, o, dir, h) && h.prim == ls.id) {
                 // createIntersection of the light hit: only its position and
                 // face normal are read
                 const TriVerts tri = loadTriangle(sc, h.prim);

@@ -118,4 +118,6 @@ def test_equal_time_cache_beats_plain(gpu_lib):
     plain.dispatch(sc, spp, readback=False)
     rgb, w = sc.film_read()
     e_plain = rel_mse(rgb / w[..., None], ref)
+    print(f"equal time: cache {e_cache:.5f} (64 frames, {t_cache:.4f} s) plain {e_plain:.5f} ({spp} spp; "
+          f"64 spp {t64:.4f} s)")
     assert e_cache < e_plain, (e_cache, e_plain, spp, t_cache, t64)
