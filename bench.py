@@ -48,6 +48,18 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def slowest_rank_ms(ms, world, device):
+    """The timed region of the slowest rank (max over ranks), as every rank
+    times its own replica between barriers."""
+    if world <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -581,10 +593,7 @@ def run_ours(args):
     ms = e0.elapsed_time(e1)
     launches = cg.kernel_launch_count() - launches0
     clk = clocks.stop()
-    if world > 1:
-        t = torch.tensor([ms], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = slowest_rank_ms(ms, world, f"cuda:{local}")
     value = N_RAYS * args.steps * world / (ms * 1e-3) / 1e6
     kernel_ms = ms / args.steps  # one launch per step
 

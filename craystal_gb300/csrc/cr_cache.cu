@@ -472,6 +472,10 @@ extern "C" int cr_render_cached(cr_scene* scene, const cr_integrator_config* cfg
     if (cfg->max_depth > 1024) return fail(CR_ERR_INVALID_ARGUMENT, "max_depth %u", cfg->max_depth);
     if (cfg->flags & CR_RENDER_SPECTRAL)
         return fail(CR_ERR_UNSUPPORTED, "the radiance cache learns RGB radiance; spectral rendering is not cached");
+    if (cfg->flags & ~(CR_RENDER_WAVEFRONT | CR_RENDER_MEGAKERNEL))
+        return fail(CR_ERR_INVALID_ARGUMENT, "unknown render flags 0x%x", cfg->flags);
+    if ((cfg->flags & CR_RENDER_WAVEFRONT) && (cfg->flags & CR_RENDER_MEGAKERNEL))
+        return fail(CR_ERR_INVALID_ARGUMENT, "CR_RENDER_WAVEFRONT and CR_RENDER_MEGAKERNEL exclude each other");
     if (cc->query_vertex == 0 || cc->query_vertex >= cfg->max_depth)
         return fail(CR_ERR_INVALID_ARGUMENT, "query_vertex %u must be in [1, max_depth)", cc->query_vertex);
     CR_CUDA(cudaSetDevice(scene->device));
