@@ -238,12 +238,12 @@ def cornell_extra(torch):
     return out
 
 
-def c3_extra(torch, res=(480, 270), budgets=(16, 64, 256)):
+def c3_extra(torch, res=(1920, 1080), budgets=(16, 64)):
     """The radiance-cache config: 8 displaced icospheres (2.6M triangles),
     Principled materials, constant environment 0.5 and one sphere light, max
-    depth 16.  Plain throughput at 1920x1080, 64 spp; the equal-time cache
-    comparison at res (reference: 4096 spp of the plain tracer, FP64 film
-    sum; the cache trained from scratch inside its time)."""
+    depth 16, 1920x1080.  Plain throughput at 64 spp; the equal-time cache
+    comparison (reference: 4096 spp of the plain tracer, FP64 film sum; the
+    cache trained from scratch inside its time; 3 trials per budget)."""
     from craystal_gb300 import scenes
     from craystal_gb300.api import CachedPathTraceIntegrator, PathTraceIntegrator, RadianceCache, Scene
     cfg = PathTraceIntegrator.Configs(maxDepth=16, rrThreshold=0.05, useMIS=True)
