@@ -69,6 +69,63 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def tensor_peak():
+    """Dense bf16 tensor-core throughput (TFLOP/s), burst, and its source."""
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return float(json.load(f)["bf16_tflops"]), "measured"
+    return 1900.0, "fallback"
+
+
+def fp32_peak_tflops(torch):
+    """FP32 FMA throughput measured here: cuBLAS SGEMM 8192^3 with TF32 off,
+    best of 5 (CUDA events)."""
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    n = 8192
+    g = torch.Generator(device="cuda").manual_seed(0)
+    a = torch.randn(n, n, device="cuda", generator=g)
+    b = torch.randn(n, n, device="cuda", generator=g)
+    c = a @ b
+    torch.cuda.synchronize()
+    best = float("inf")
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b, out=c)
+        e1.record()
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    torch.backends.cuda.matmul.allow_tf32 = prev
+    del a, b, c
+    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+
+
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo) and core count."""
+    name = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                name = line.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    if name is None:
+        try:
+            with open("/proc/cpuinfo") as f:
+                for line in f:
+                    if line.lower().startswith("model name"):
+                        name = line.split(":", 1)[1].strip()
+                        break
+        except OSError:
+            pass
+    import platform
+    return {"model": name or platform.machine(), "nproc": os.cpu_count()}
+
+
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -171,7 +228,7 @@ def run_reference(args):
            "config": {"workload": WORKLOAD, "triangles": N_TRIS, "rays": N_RAYS,
                       "step_sample_rays": sample, "bvh": "binned SAH, 32 bins (reference CPU build)"},
            "cpu_baseline": {"value": round(v, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
-                            "sample": f"{sample} of the {N_RAYS} rays per step"},
+                            "sample": f"{sample} of the {N_RAYS} rays per step", "cpu": cpu_model()},
            "e2e": {"value": round(v, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 
@@ -179,7 +236,8 @@ def run_reference(args):
 def cornell_extra(torch):
     """The plain path tracer on the procedural Cornell box, 256x256, 16 spp,
     max depth 8, NEE + MIS, hero-wavelength spectral (the C1 config) and RGB,
-    on the default (wavefront) schedule: Mpaths/s and Mrays/s; beside it the
+    plus RGB at the reference's effective settings (max depth 10), on the
+    default (wavefront) schedule: Mpaths/s and Mrays/s; beside it the
     reference's own path tracer restated in CUDA and the CPU oracle's path
     tracer on all host cores (RGB, a bounded number of samples)."""
     from craystal_gb300 import scenes
@@ -191,8 +249,11 @@ def cornell_extra(torch):
     spp, reps = 16, 5
     s = torch.cuda.current_stream()
     out = {"config": "cornell 256x256, 16 spp, max depth 8, NEE+MIS, default schedule (wavefront)"}
-    for label, spectral in (("spectral", True), ("rgb", False)):
-        integ = PathTraceIntegrator(cfg, compat=False, spectral=spectral)
+    # compat: the reference's effective settings (its Configs never reach the
+    # kernel, so it always runs max depth 10, rr 0.05)
+    for label, spectral, compat in (("spectral", True, False), ("rgb", False, False),
+                                    ("rgb_compat_depth10", False, True)):
+        integ = PathTraceIntegrator(cfg, compat=compat, spectral=spectral)
         integ.dispatch(sc, spp, readback=False)
         torch.cuda.synchronize()
         sc.film_clear()
@@ -221,6 +282,15 @@ def cornell_extra(torch):
         "ms_per_16spp": round(ref_s * 1e3, 3)}
     out["speedup_over_restated_reference_rgb"] = round(out["rgb"]["Mpaths_s"] /
                                                        out["restated_reference_path_tracer"]["Mpaths_s"], 2)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    _, ref_rays = ref.render(cam, spp, max_depth=10, rr_threshold=0.05)
+    ref_s = time.perf_counter() - t
+    out["restated_reference_path_tracer_depth10"] = {
+        "Mpaths_s": round(256 * 256 * spp / ref_s / 1e6, 2), "Mrays_s": round(ref_rays / ref_s / 1e6, 2),
+        "ms_per_16spp": round(ref_s * 1e3, 3)}
+    out["speedup_over_restated_reference_compat"] = round(
+        out["rgb_compat_depth10"]["Mpaths_s"] / out["restated_reference_path_tracer_depth10"]["Mpaths_s"], 2)
     # the CPU oracle's path tracer, all host threads, a bounded sample of spp
     import oracle
     threads = oracle.hardware_threads()
@@ -268,6 +338,22 @@ def c3_extra(torch, res=(1920, 1080), budgets=(16, 64)):
     out = {"config": "8 displaced icospheres (2.6M tris), Principled, env 0.5 + sphere light, depth 16",
            "plain_1080p_64spp": {"s": round(dt, 3), "Mpaths_s": round(1920 * 1080 * 64 / dt / 1e6, 1),
                                  "Mrays_s": round(rays / dt / 1e6, 1), "triangles": int(sc.n_tris)}}
+    # the CPU oracle on all host threads: a crop of the 64 rows at the image
+    # centre at 1 spp, scaled linearly to the full 1920x1080 x 64 spp render
+    import oracle
+    from craystal_gb300.api import flatten_scene
+    threads = oracle.hardware_threads()
+    osc = oracle.OracleScene(flatten_scene(data))
+    osc.set_lights(env, sph)
+    oc = oracle.make_camera(cam.posW, cam.target, cam.up, cam.fovY, 1920, 1080)
+    t = time.perf_counter()
+    _, orays = osc.render(oc, 16, 0.05, True, spp=1, rows=(508, 572), threads=threads)
+    cpu_s = time.perf_counter() - t
+    cpu_rate = 1920 * 64 / cpu_s
+    out["cpu_oracle"] = {"Mpaths_s": round(cpu_rate / 1e6, 4), "Mrays_s": round(orays / cpu_s / 1e6, 4),
+                         "threads": threads, "sample": "rows 508-571 at 1 spp",
+                         "projected_1080p_64spp_s": round(1920 * 1080 * 64 / cpu_rate, 1)}
+    del osc
     w, h = res
     cam.setSensor(type(cam.sensor)((w, h)))
     sc.setCamera(cam)
@@ -285,14 +371,60 @@ def c3_extra(torch, res=(1920, 1080), budgets=(16, 64)):
         img = np.nan_to_num((rgb / wt[..., None]).astype(np.float64))
         return float(np.mean((img - ref) ** 2 / (ref ** 2 + 1e-2)))
 
-    probe = CachedPathTraceIntegrator(cfg, train_every=16, cache=RadianceCache(seed=1))
+    probe = CachedPathTraceIntegrator(cfg, cache=RadianceCache(seed=1))
     probe.dispatch(sc, 16, first_sample=2_000_000, readback=False)
     t_frame = timed(lambda: probe.dispatch(sc, 32, first_sample=3_000_000, readback=False)) / 32
     rows = equal_time_trials(sc, cfg, plain, rel_mse, timed, t_frame, budgets)
     out["equal_time"] = {"resolution": [w, h], "reference_spp": 4096, "ms_per_cached_frame": round(t_frame * 1e3, 3),
+                         "train_every": "adaptive", "train_every_reached": int(probe.stats.last_train_every),
                          "budgets": rows}
     sc.close()
     return out
+
+
+def mlp_extra(torch):
+    """The radiance-cache network alone on device buffers (the calls the
+    cached integrator makes per frame): inference of 4,194,304 queries
+    (inputs and outputs larger than L2) and one Adam training step on 65,536
+    records, CUDA events on the launching stream.  FLOPs: 2 x 27,840 (the
+    weights) per query forward; 3x that per training record (forward, data
+    gradient, weight gradient).  Peak: the measured dense bf16 tensor-core
+    rate (FP16 runs at the same rate)."""
+    from craystal_gb300.api import RadianceCache
+    net = RadianceCache(seed=3)
+    n_inf, n_tr = 1 << 22, 1 << 16
+    g = torch.Generator(device="cuda").manual_seed(0)
+    x = torch.rand((n_inf, 7), device="cuda", generator=g)
+    y = torch.empty((n_inf, 3), device="cuda")
+    t = torch.rand((n_tr, 3), device="cuda", generator=g)
+    s = torch.cuda.current_stream()
+
+    def ev_ms(fn, reps):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for _ in range(reps):
+            fn()
+        e1.record(s)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    ms_inf = ev_ms(lambda: net.infer_device(x.data_ptr(), n_inf, y.data_ptr(), s.cuda_stream), 20)
+    ms_tr = ev_ms(lambda: net.train_step_device(x.data_ptr(), t.data_ptr(), n_tr, s.cuda_stream), 20)
+    net.close()
+    peak, src = tensor_peak()
+    f = 2 * 27840
+    inf_tf = f * n_inf / (ms_inf * 1e-3) / 1e12
+    tr_tf = 3 * f * n_tr / (ms_tr * 1e-3) / 1e12
+    return {"inference": {"queries": n_inf, "ms": round(ms_inf, 4), "Mqueries_s": round(n_inf / ms_inf / 1e3, 1),
+                          "tflops": round(inf_tf, 1), "frac": round(inf_tf / peak, 4)},
+            "train_step": {"records": n_tr, "ms": round(ms_tr, 4), "tflops": round(tr_tf, 1),
+                           "frac": round(tr_tf / peak, 4)},
+            "peak_tflops": peak, "peak_source": f"{src} dense bf16 (burst)",
+            "instruction": {"inference": "tcgen05.mma kind::f16, M128, TMEM accumulators, weights by cp.async.bulk",
+                            "training": "mma.sync m16n8k16 FP16 with FP32 accumulation"}}
 
 
 def wavefront_extra(torch):
@@ -350,6 +482,8 @@ def large_scene_extra(torch, spp=32):
     create_s = time.perf_counter() - t
     st = sc.bvh_stats()
     n_tris = sc.n_tris
+    from craystal_gb300.api import flatten_scene
+    flat = flatten_scene(data)
     del data
     integ = PathTraceIntegrator(PathTraceIntegrator.Configs(maxDepth=12, rrThreshold=0.05, useMIS=True), compat=False)
     integ.dispatch(sc, 1, readback=False)  # allocates the path state
@@ -371,6 +505,25 @@ def large_scene_extra(torch, spp=32):
            "rays_per_path": round(rays / paths, 3),
            "mean_rgb": [round(float(x), 4) for x in np.nanmean(rgb / w[..., None], axis=(0, 1))]}
     sc.close()
+    # the CPU oracle on all host threads: its own BVH build, then a crop of the
+    # 16 rows at the image centre at 1 spp, scaled linearly to the full render
+    import oracle
+    threads = oracle.hardware_threads()
+    t = time.perf_counter()
+    osc = oracle.OracleScene(flat)
+    build_s = time.perf_counter() - t
+    del flat
+    osc.set_lights(env, sun)
+    oc = oracle.make_camera(cam.posW, cam.target, cam.up, cam.fovY, 3840, 2160)
+    t = time.perf_counter()
+    _, orays = osc.render(oc, 12, 0.05, True, spp=1, rows=(1072, 1088), threads=threads)
+    cpu_s = time.perf_counter() - t
+    cpu_rate = 3840 * 16 / cpu_s
+    out["cpu_oracle"] = {"bvh_build_s": round(build_s, 1), "Mpaths_s": round(cpu_rate / 1e6, 4),
+                         "Mrays_s": round(orays / cpu_s / 1e6, 4), "threads": threads,
+                         "sample": "rows 1072-1087 at 1 spp",
+                         "projected_render_s": round(paths / cpu_rate, 1)}
+    del osc
     return out
 
 
@@ -384,7 +537,7 @@ def cache_frames_extra(torch, res=512, frames=32):
     sc = Scene(data)
     sc.setCamera(cam)
     cfg = PathTraceIntegrator.Configs(maxDepth=8, rrThreshold=0.05, useMIS=True)
-    integ = CachedPathTraceIntegrator(cfg, train_every=16)
+    integ = CachedPathTraceIntegrator(cfg)
     integ.dispatch(sc, 16, first_sample=5_000_000, readback=False)
     plain = PathTraceIntegrator(cfg, compat=False)
     plain.dispatch(sc, 4, readback=False)
@@ -401,7 +554,8 @@ def cache_frames_extra(torch, res=512, frames=32):
             "cache_ms_per_frame": round(1e3 * tc / frames, 3), "plain_ms_per_spp": round(1e3 * tp / frames, 3)}
 
 
-def equal_time_trials(sc, cfg, plain, rel_mse, timed, t_frame, budgets, trials=3):
+def equal_time_trials(sc, cfg, plain, rel_mse, timed, t_frame, budgets, trials=3, train_every=0,
+                      train_samples=8192):
     """Per budget (plain spp): `trials` independent pairs of (plain render,
     fresh cache trained and rendering inside the plain render's time) on
     disjoint sample indices and network seeds; relMSE is heavy-tailed
@@ -415,7 +569,8 @@ def equal_time_trials(sc, cfg, plain, rel_mse, timed, t_frame, budgets, trials=3
             t_plain = timed(lambda: plain.dispatch(sc, spp, first_sample=10_000_000 * (k + 1), readback=False))
             e_plain = rel_mse(*sc.film_read())
             frames = max(1, int(t_plain / t_frame))
-            integ = CachedPathTraceIntegrator(cfg, train_every=16, cache=RadianceCache(seed=k))
+            integ = CachedPathTraceIntegrator(cfg, train_every=train_every, train_samples=train_samples,
+                                              cache=RadianceCache(seed=k))
             sc.film_clear()
             t_cache = timed(lambda: integ.dispatch(sc, frames, first_sample=50_000_000 + 10_000_000 * k,
                                                    readback=False))
@@ -466,13 +621,14 @@ def cache_extra(torch, res=512, budgets=(64, 256, 1024)):
         return time.perf_counter() - t
 
     # cost of a cached frame, from a separate cache
-    probe = CachedPathTraceIntegrator(cfg, train_every=16, cache=RadianceCache(seed=1))
+    probe = CachedPathTraceIntegrator(cfg, cache=RadianceCache(seed=1))
     probe.dispatch(sc, 16, first_sample=2_000_000, readback=False)
     t_frame = timed(lambda: probe.dispatch(sc, 32, first_sample=3_000_000, readback=False)) / 32
     rows = equal_time_trials(sc, cfg, plain, rel_mse, timed, t_frame, budgets)
     return {"config": f"cornell {res}x{res}, max depth 8, NEE+MIS; reference 16384 spp plain, FP64 film sum; "
                       "cache trained from scratch inside its time; 3 independent trials per budget",
-            "ms_per_cached_frame": round(t_frame * 1e3, 3), "train_every": 16, "query_vertex": 1, "budgets": rows}
+            "ms_per_cached_frame": round(t_frame * 1e3, 3), "train_every": "adaptive",
+            "train_every_reached": int(probe.stats.last_train_every), "query_vertex": 1, "budgets": rows}
 
 
 def batch_extra(torch, n_scenes=64):
@@ -627,6 +783,7 @@ def run_ours(args):
                                                                       d_hits)
         extra["path_tracer"] = cornell_extra(torch)
         extra["wavefront_vs_megakernel"] = wavefront_extra(torch)
+        extra["radiance_cache_network"] = mlp_extra(torch)
         extra["radiance_cache_equal_time"] = cache_extra(torch, args.cache_res)
         extra["radiance_cache_scene"] = c3_extra(torch)
         extra["batched_scenes"] = batch_extra(torch, args.batch_scenes)
@@ -656,10 +813,22 @@ def run_ours(args):
                            "bytes_per_ray": round(bpr, 1),
                            "per_ray": {k: round(v, 2) for k, v in per.items()},
                            "note": f"of {src}; per-ray counts from the oracle on 262144 rays"}
+        # the same counts as FP32 work: 24 flops per box test, 50 per Moller-Trumbore test
+        fpr = 24 * per["boxes"] + 50 * per["tris"]
+        fp32_peak = fp32_peak_tflops(torch)
+        fp32 = fpr * N_RAYS / (kernel_ms * 1e-3) / 1e12
+        out["roofline"]["fp32"] = {"achieved": round(fp32, 2), "peak": round(fp32_peak, 1), "unit": "TFLOP/s",
+                                   "frac": round(fp32 / fp32_peak, 4), "flops_per_ray": round(fpr, 1),
+                                   "peak_source": "measured here: cuBLAS SGEMM 8192^3, TF32 off"}
+        prof = os.path.join(ROOT, "profiles", "trace_closest_raycast.json")
+        if os.path.exists(prof):
+            with open(prof) as f:
+                out["roofline"]["l2_hit_rate_pct"] = json.load(f).get("l2_hit_rate_pct")
         if not args.skip_cpu:
             v, n, dt = cpu_baseline(osc, rays, threads)
             out["cpu_baseline"] = {"value": round(v, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
-                                   "sample": f"first {n} of the {N_RAYS} rays ({dt:.1f} s wall)"}
+                                   "sample": f"first {n} of the {N_RAYS} rays ({dt:.1f} s wall)",
+                                   "cpu": cpu_model()}
         print(json.dumps(out), flush=True)
     if world > 1:
         dist.barrier()
@@ -681,6 +850,8 @@ def run_only(args):
         r = cache_frames_extra(torch, args.cache_res)
     elif args.only == "large_scene":
         r = large_scene_extra(torch)
+    elif args.only == "radiance_cache_network":
+        r = mlp_extra(torch)
     elif args.only == "radiance_cache_scene":
         r = c3_extra(torch)
     else:
@@ -699,7 +870,7 @@ def main():
     ap.add_argument("--rays", type=int, default=N_RAYS, help="rays per step (profiling a smaller case)")
     ap.add_argument("--tris", type=int, default=N_TRIS, help="triangles (profiling a smaller case)")
     ap.add_argument("--only", choices=["path_tracer", "wavefront", "radiance_cache", "cache_frames", "batched_scenes",
-                                       "large_scene", "radiance_cache_scene"],
+                                       "large_scene", "radiance_cache_scene", "radiance_cache_network"],
                     help="run one secondary workload alone and print its figures (profiling)")
     ap.add_argument("--cache-res", type=int, default=512, help="radiance-cache workload resolution")
     ap.add_argument("--batch-scenes", type=int, default=64, help="scenes in the batched workload")

@@ -88,7 +88,7 @@ class CrCacheConfig(ctypes.Structure):
 
 class CrCacheStats(ctypes.Structure):
     _fields_ = [("frames", ctypes.c_uint64), ("queries", ctypes.c_uint64), ("train_records", ctypes.c_uint64),
-                ("last_loss", ctypes.c_float)]
+                ("last_loss", ctypes.c_float), ("last_train_every", ctypes.c_uint32)]
 
 
 class CrBatchItem(ctypes.Structure):
@@ -153,6 +153,8 @@ SIGNATURES = [
     ("cr_mlp_infer", ctypes.c_int, [_P, _P, _U64, _P]),
     ("cr_mlp_gradients", ctypes.c_int, [_P, _P, _P, _U64, _P, _P]),
     ("cr_mlp_train_step", ctypes.c_int, [_P, _P, _P, _U64, _P]),
+    ("cr_mlp_infer_device", ctypes.c_int, [_P, _P, _U64, _P, _P]),
+    ("cr_mlp_train_step_device", ctypes.c_int, [_P, _P, _P, _U64, _P]),
     ("cr_render_cached", ctypes.c_int, [_P, ctypes.POINTER(CrIntegratorConfig), ctypes.POINTER(CrCacheConfig), _P,
                                         _U32, _U32, _P, ctypes.POINTER(CrCacheStats)]),
     ("cr_batch_create", ctypes.c_int, [_P, _P, _U32, ctypes.POINTER(ctypes.c_void_p)]),

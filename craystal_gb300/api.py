@@ -444,12 +444,22 @@ class RadianceCache:
         check(load().cr_mlp_infer(self._h, ptr(x), len(x), ptr(out)))
         return out
 
+    def infer_device(self, inputs: int, n: int, outputs: int, stream: int = 0):
+        """Inference on device pointers (n x 7 in, n x 3 out), ordered on
+        `stream` without waiting."""
+        check(load().cr_mlp_infer_device(self._h, inputs, n, outputs, stream))
+
+    def train_step_device(self, inputs: int, targets: int, n: int, stream: int = 0):
+        """One Adam step on device pointers (n x 7 inputs, n x 3 targets),
+        ordered on `stream` without waiting."""
+        check(load().cr_mlp_train_step_device(self._h, inputs, targets, n, stream))
+
 
 class CachedPathTraceIntegrator(PathTraceIntegrator):
     """Path tracing with the radiance cache: one frame = one sample per pixel
     (cr_render_cached)."""
 
-    def __init__(self, configs=None, compat=False, query_vertex=1, train_every=16, train_samples=65536,
+    def __init__(self, configs=None, compat=False, query_vertex=1, train_every=0, train_samples=8192,
                  train_steps=1, cache: "RadianceCache" = None, wavefront: Optional[bool] = None):
         # schedule: the wavefront unless wavefront=False (the megakernel form)
         super().__init__(configs or PathTraceIntegrator.Configs(), compat, wavefront=wavefront)

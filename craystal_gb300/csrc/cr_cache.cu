@@ -136,8 +136,8 @@ __global__ void __launch_bounds__(256) kRenderCached(const SceneView sc, const C
                 // targets beyond kMaxTarget come from near-zero throughputs,
                 // not from the scene's radiance; they are left out
                 if (!finite3(t) || maxValue(be) <= 0.0f || maxValue(t) > kMaxTarget) continue;
-                const uint32_t idx = atomicAdd(tCount, 1u);
-                if (idx >= cp.trainCap) break;
+                const uint32_t idx = atomicAdd(tCount, 1u);  // counts records beyond the cap too
+                if (idx >= cp.trainCap) continue;
                 for (int k = 0; k < 7; k++) tIn[(size_t)idx * 7 + k] = hk.f[r][k];
                 tTarget[(size_t)idx * 3 + 0] = t.r;
                 tTarget[(size_t)idx * 3 + 1] = t.g;
@@ -255,8 +255,8 @@ struct CachedMode {
             const Spec t = Spec{be.r > 0.0f ? d.r / be.r : 0.0f, be.g > 0.0f ? d.g / be.g : 0.0f,
                                 be.b > 0.0f ? d.b / be.b : 0.0f};
             if (!finite3(t) || maxValue(be) <= 0.0f || maxValue(t) > kMaxTarget) continue;
-            const uint32_t idx = atomicAdd(tCount, 1u);
-            if (idx >= cp.trainCap) break;
+            const uint32_t idx = atomicAdd(tCount, 1u);  // counts records beyond the cap too
+            if (idx >= cp.trainCap) continue;
             for (int j = 0; j < 7; j++) tIn[(size_t)idx * 7 + j] = recIn[ri * 7 + j];
             tTarget[(size_t)idx * 3 + 0] = t.r;
             tTarget[(size_t)idx * 3 + 1] = t.g;
@@ -317,6 +317,10 @@ struct CacheBuffers {
     float* recIn = nullptr;
     float* recBeta = nullptr;
     float* recBefore = nullptr;
+    // adaptive training-path spacing carried from one call to the next (a
+    // renderer dispatching one frame per call still converges)
+    uint32_t teStart = 0;    // the start value it was adapted from
+    uint32_t teAdapted = 0;  // the spacing for the next frame
 };
 
 void freeCacheBuffers(void* p) {
@@ -365,7 +369,7 @@ int ensureCacheBuffers(cr_scene* s, uint32_t trainCap, uint32_t slotCap, CacheBu
 
 int renderCached(cr_scene* s, const cr_integrator_config* cfg, const cr_cache_config* cc, MlpState* mlp,
                  uint32_t frames, uint32_t first, cudaStream_t st, cr_cache_stats* stats) {
-    const uint32_t trainCap = cc->train_samples ? cc->train_samples : 65536u;
+    const uint32_t trainCap = cc->train_samples ? cc->train_samples : 8192u;
     const bool wavefront = !(cfg->flags & CR_RENDER_MEGAKERNEL);
     CacheParams cp;
     float3 mn = s->rootMin, mx = s->rootMax;
@@ -378,19 +382,27 @@ int renderCached(cr_scene* s, const cr_integrator_config* cfg, const cr_cache_co
     cp.sceneInvExtent = mk3(ext.x > 0 ? 1.0f / ext.x : 0.0f, ext.y > 0 ? 1.0f / ext.y : 0.0f,
                             ext.z > 0 ? 1.0f / ext.z : 0.0f);
     cp.queryVertex = cc->query_vertex;
-    // train_every 0: about train_samples records per frame at ~3 records per
-    // training path
+    // train_every 0 (adaptive): start at about train_samples records per
+    // frame for ~3 records per training path, then after every frame scale the
+    // spacing of the training paths by (records produced / train_samples),
+    // by at most 2x per frame and never below half the start.  Training paths
+    // run to full depth, so more of them than the batch can use only cost time.
     const uint64_t px = (uint64_t)s->cam.width * s->cam.height;
-    cp.trainEvery = cc->train_every ? cc->train_every
-                                    : (uint32_t)std::max<uint64_t>(1, (px * 3 + trainCap / 2) / trainCap);
+    const bool adaptive = cc->train_every == 0;
+    const uint32_t te0 = adaptive ? (uint32_t)std::max<uint64_t>(1, (px * 3 + trainCap / 2) / trainCap)
+                                  : cc->train_every;
+    const uint32_t teMin = adaptive ? std::max(1u, te0 / 2) : te0;
+    const uint32_t teMax = (uint32_t)std::max<uint64_t>(te0, std::min<uint64_t>(px, 1u << 24));
+    cp.trainEvery = te0;
     cp.trainCap = trainCap;
     // training paths of a frame: px / trainEvery on average (the hash picks
-    // them); room for four times that, beyond which a path keeps no records
-    const uint32_t slotCap =
-        wavefront ? (uint32_t)std::min<uint64_t>(px, 4 * (px / cp.trainEvery) + 4096) : 0u;
+    // them); room for four times that at the smallest spacing, beyond which a
+    // path keeps no records
+    const uint32_t slotCap = wavefront ? (uint32_t)std::min<uint64_t>(px, 4 * (px / teMin) + 4096) : 0u;
     CacheBuffers* b = nullptr;
     int rc = ensureCacheBuffers(s, trainCap, slotCap, &b);
     if (rc) return rc;
+    if (adaptive && b->teStart == te0 && b->teAdapted) cp.trainEvery = b->teAdapted;
     WfBuffers* wb = nullptr;
     const uint32_t waveCap = (uint32_t)std::min<uint64_t>(px, kWaveCap);
     if (wavefront) {
@@ -430,6 +442,14 @@ int renderCached(cr_scene* s, const cr_integrator_config* cfg, const cr_cache_co
         CR_CUDA(cudaMemcpyAsync(cnt, b->counters, sizeof(cnt), cudaMemcpyDeviceToHost, st));
         CR_CUDA(cudaStreamSynchronize(st));
         const uint32_t nq = cnt[0], nt = std::min(cnt[1], trainCap);
+        const uint32_t teUsed = cp.trainEvery;
+        if (adaptive) {
+            const double ratio = std::min(2.0, std::max(0.5, (double)cnt[1] / (double)trainCap));
+            const double te = std::min((double)teMax, std::max((double)teMin, (double)cp.trainEvery * ratio));
+            cp.trainEvery = (uint32_t)(te + 0.5);
+            b->teStart = te0;
+            b->teAdapted = cp.trainEvery;
+        }
         rc = mlpInferDevice(mlp, b->qIn, nq, b->qOut, true, st);
         if (rc) return rc;
         kSplatCached<<<(unsigned)((W * H + 255) / 256), 256, 0, st>>>(b->samples, b->qBeta, b->qOut, W, H,
@@ -448,8 +468,11 @@ int renderCached(cr_scene* s, const cr_integrator_config* cfg, const cr_cache_co
             stats->queries += nq;
             stats->train_records += nt;
             stats->frames++;
+            stats->last_train_every = teUsed;
         }
     }
+    rc = mlpCheck(mlp);
+    if (rc) return rc;
     if (stats && lastTrain) {
         float l = 0;
         CR_CUDA(cudaMemcpyAsync(&l, mlpLossPtr(mlp), sizeof(float), cudaMemcpyDeviceToHost, st));

@@ -1,25 +1,32 @@
 // cr_mlp.cu -- the radiance-cache network: a 7-input MLP with a 12-frequency
 // sin / cos encoding (168 features, padded to 176), five hidden layers of 64
 // ReLU units and 3 linear outputs (RGB radiance), FP16 weights and
-// activations with FP32 accumulation on the tensor cores (mma.sync
-// m16n8k16), trained online with Adam on a relative L2 loss.
+// activations with FP32 accumulation on the tensor cores, trained online
+// with Adam on a relative L2 loss.
 //
 // This part has no counterpart in the reference; it is the cache that ends
 // paths early (see cr_cache.cu).
 //
 // Kernels
-//   kInfer     fused forward: one warp carries 16 queries through all six
-//              layers; each layer's accumulator fragments are the next
-//              layer's A fragments (the m16n8k16 C layout of two adjacent
-//              n-tiles is the A layout of one k-tile), so activations never
-//              leave registers.  Weights live in shared memory.
-//   kTrainFwdBwd  the same forward, storing every layer's input activations,
+//   kInferTc   fused forward on the 5th-generation tensor cores: each of
+//              three warpgroups of a persistent CTA carries a tile of 128
+//              queries through all six layers.  The weights are brought into
+//              shared memory once per CTA by bulk asynchronous copies; each
+//              layer is tcgen05.mma (M 128, N 64 or 16, K 16 per instruction)
+//              from shared-memory operands into a 64-column TMEM accumulator
+//              per warpgroup, read back with tcgen05.ld, ReLU'd and written as
+//              the next layer's FP16 operand.  Three tiles in flight per SM
+//              overlap one warpgroup's encoding and epilogue with another's
+//              MMAs.
+//   kTrainFwdBwd  training forward (mma.sync m16n8k16; one warp carries 16
+//              rows, activations in registers, every layer's input stored),
 //              then the loss gradient and the backward pass for the data
 //              gradients, storing every layer's output gradient dY.
 //   kWeightGrad   dW_l = X_l^T dY_l over the batch (split over CTAs,
 //              accumulated with atomics in FP32).
-//   kAdam      Adam on FP32 master weights; refreshes the two FP16 copies
-//              (n-major for the forward B operand, k-major for the backward).
+//   kAdam      Adam on FP32 master weights; kPackWeights refreshes the three
+//              FP16 copies (n-major and k-major for training, core-matrix
+//              tiles for the tensor-core inference).
 
 #include <cstring>
 #include <vector>
@@ -91,17 +98,32 @@ __device__ __forceinline__ float2 unpack2(uint32_t v) {
     return __half22float2(h);
 }
 
-// Encoded features of one query row for the columns a thread owns in k-tile
-// kt: (c, c+1) and (c+8, c+9) with c = kt*16 + tig*2.  Feature j = d*24 +
-// 2f + {0: sin, 1: cos} of sin / cos(pi * 2^f * x_d).
+// The encoding: feature j = d*24 + 2f + {0: sin, 1: cos} of pi * 2^f * x_d.
+// For f = 4q the angle is reduced exactly (2^f x is exact, and so is taking
+// it modulo 2) and sincospif evaluates it; f = 4q+1 .. 4q+3 follow by the
+// double-angle formulas sin 2a = 2 sin a cos a, cos 2a = (cos a - sin a)
+// (cos a + sin a).  Three doublings at most keep the error below 1e-6, far
+// under the FP16 rounding of the features, at a quarter of the sincospif
+// calls.  Training and inference evaluate the same operations.
+__device__ __forceinline__ void sincosBase(float x, int f, float& s, float& c) {
+    float y = ldexpf(x, f);
+    y = y - 2.0f * floorf(y * 0.5f);
+    sincospif(y, &s, &c);
+}
+__device__ __forceinline__ void doubleAngle(float& s, float& c) {
+    const float s2 = 2.0f * s * c;
+    const float c2 = (c - s) * (c + s);
+    s = s2;
+    c = c2;
+}
+
+// Encoded features j, j+1 (j even) of one query row.
 __device__ __forceinline__ uint32_t featurePair(const float* x, int j) {
     if (j >= kIn * kFreq * 2) return 0u;
     const int d = j / (kFreq * 2), f = (j % (kFreq * 2)) >> 1;
-    // pi * 2^f * x, reduced exactly: 2^f * x is exact, fmod by 2 is exact
-    float y = ldexpf(x[d], f);
-    y = y - 2.0f * floorf(y * 0.5f);
     float s, c;
-    sincospif(y, &s, &c);
+    sincosBase(x[d], f & ~3, s, c);
+    for (int r = 0; r < (f & 3); r++) doubleAngle(s, c);
     return pack2(s, c);
 }
 
@@ -206,34 +228,6 @@ __device__ void forwardTile(const __half* sw, const float* __restrict__ in, uint
     out[1] = o[0][1];
     out[2] = o[0][2];
     out[3] = o[0][3];
-}
-
-// Writes the 3 real output columns of a tile; thread (g, tig) holds columns
-// tig*2, tig*2+1 of rows g and g+8.
-__device__ __forceinline__ void storeOut(const float o[4], float* __restrict__ out, uint64_t n, uint64_t row0,
-                                         bool clampNonNeg) {
-    const int g = (threadIdx.x & 31) >> 2, tig = threadIdx.x & 3;
-    const uint64_t r0 = row0 + g, r1 = row0 + g + 8;
-    for (int k = 0; k < 2; k++) {
-        const int col = tig * 2 + k;
-        if (col >= 3) continue;
-        if (r0 < n) out[r0 * 3 + col] = clampNonNeg ? fmaxf(o[k], 0.0f) : o[k];
-        if (r1 < n) out[r1 * 3 + col] = clampNonNeg ? fmaxf(o[2 + k], 0.0f) : o[2 + k];
-    }
-}
-
-__global__ void __launch_bounds__(kThreads) kInfer(const __half* __restrict__ wFwd, const float* __restrict__ in,
-                                                   uint64_t n, float* __restrict__ out, int clampNonNeg) {
-    extern __shared__ __align__(16) __half smem[];
-    loadFwdWeights(wFwd, smem);
-    __syncthreads();
-    const uint64_t warpsTotal = (uint64_t)gridDim.x * kWarps;
-    const uint64_t w = (uint64_t)blockIdx.x * kWarps + (threadIdx.x >> 5);
-    for (uint64_t row0 = w * 16; row0 < n; row0 += warpsTotal * 16) {
-        float o[4];
-        forwardTile(smem, in, n, row0, o, nullptr);
-        storeOut(o, out, n, row0, clampNonNeg != 0);
-    }
 }
 
 struct Acts {
@@ -408,6 +402,236 @@ __global__ void __launch_bounds__(256) kWeightGrad(const __half* __restrict__ ac
     }
 }
 
+// ---------------------------------------------------------------------------
+// inference on the tensor cores (tcgen05)
+// ---------------------------------------------------------------------------
+// Operands sit in shared memory in the canonical K-major layout without
+// swizzle: 8 x 8 FP16 core matrices of 128 contiguous bytes (8 rows of 16 B).
+//   A (a tile's layer input, 128 rows x K): core (m/8, k/8) at
+//     (k/8) * 2048 + (m/8) * 128, so row m's 16-byte chunk k/8 is at
+//     (k/8) * 2048 + m * 16 and a warp's 32 rows write 512 contiguous bytes;
+//     leading-dimension (K) stride 2048 B, stride-dimension (M) stride 128 B.
+//   B (layer l's weights as N x K, K-major): core (n/8, k/8) at
+//     ((k/8) * (Npad/8) + n/8) * 128; K stride Npad * 16 B, N stride 128 B.
+constexpr int kTile = 128;                     // queries per tile (the MMA's M)
+constexpr int kSlots = 3;                      // warpgroups per CTA, one tile each
+__host__ __device__ constexpr int layerNpad(int l) { return l == kLayers - 1 ? 16 : kHid; }
+__host__ __device__ constexpr int tcBytes(int l) { return layerK(l) * layerNpad(l) * 2; }
+__host__ __device__ constexpr int tcOffset(int l) {
+    int o = 0;
+    for (int i = 0; i < l; i++) o += tcBytes(i);
+    return o;
+}
+constexpr int kTcWeightBytes = tcOffset(kLayers);        // 57,344
+constexpr int kTcABytes = kTile * kFeat * 2;             // 45,056 per slot
+constexpr int kTcSmemW = kSlots * kTcABytes;             // the A buffers come first
+constexpr int kTcSmemBar = kTcSmemW + kTcWeightBytes;    // 192,512: mbarriers, TMEM address
+// The allocation extends 4 KB past the barriers, so that every operand read
+// stays inside it even under the other assignment of the two descriptor
+// strides.
+constexpr int kTcSmem = 196608;
+constexpr uint32_t kTcCols = 256;                        // 64 per slot, a power of two
+constexpr uint32_t kTcSpin = 1u << 20;                   // bounded waits (try_wait rounds)
+static_assert(kTcSmemBar + 8 + 8 * kSlots + 4 <= kTcSmem, "tensor-core inference shared memory");
+
+__device__ __forceinline__ uint32_t smemAddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Shared-memory matrix descriptor: start, leading- and stride-dimension byte
+// offsets (each >> 4), the fixed version bit 46, no swizzle.
+__device__ __forceinline__ uint64_t tcDesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+// Instruction descriptor of kind::f16: FP32 accumulator (bits 4-5 = 1), FP16
+// A and B, both K-major, N >> 3 at bit 17, M >> 4 at bit 24.
+__host__ __device__ constexpr uint32_t tcInstr(int m, int n) {
+    return (1u << 4) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void mbarInit(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+// Waits for phase `phase` of the barrier; false after kTcSpin rounds.
+__device__ __forceinline__ bool mbarWait(uint32_t bar, uint32_t phase) {
+    for (uint32_t i = 0; i < kTcSpin; i++) {
+        uint32_t done;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(bar), "r"(phase)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+__device__ __forceinline__ void tcBefore() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tcAfter() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+// makes this thread's shared-memory stores visible to the tensor core's reads
+__device__ __forceinline__ void proxyFence() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void stShared4(uint32_t addr, uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
+    asm volatile("st.shared.v4.b32 [%0], {%1,%2,%3,%4};" ::"r"(addr), "r"(a), "r"(b), "r"(c), "r"(d) : "memory");
+}
+
+__device__ __forceinline__ void tcMma(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+__device__ __forceinline__ void tcCommit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void tcLoad32(uint32_t taddr, uint32_t* v) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,"
+        "%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]),
+          "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]),
+          "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]),
+          "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+        : "r"(taddr));
+}
+__device__ __forceinline__ void tcLoad4(uint32_t taddr, uint32_t* v) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3])
+                 : "r"(taddr));
+}
+__device__ __forceinline__ void tcLoadWait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// Barrier and AND vote over the 128 threads of warpgroup g (named barrier g + 1).
+__device__ __forceinline__ void wgSync(int g) { asm volatile("bar.sync %0, 128;" ::"r"(g + 1) : "memory"); }
+__device__ __forceinline__ bool wgAnd(int g, bool v) {
+    uint32_t r;
+    asm volatile(
+        "{\n.reg .pred p, q;\nsetp.ne.u32 q, %1, 0;\nbar.red.and.pred p, %2, 128, q;\nselp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(r)
+        : "r"((uint32_t)v), "r"(g + 1)
+        : "memory");
+    return r != 0;
+}
+
+// Persistent: CTA b's warpgroup g takes tiles b * kSlots + g, stepping by
+// gridDim.x * kSlots.  A wait that runs out (it should never) sets bit 0 of
+// *err, ends the warpgroup's loop and still frees the TMEM.
+__global__ void __launch_bounds__(kTile * kSlots, 1) kInferTc(const uint8_t* __restrict__ wTc,
+                                                              const float* __restrict__ in, uint64_t n,
+                                                              float* __restrict__ out, int clampNonNeg,
+                                                              uint32_t* __restrict__ err) {
+    extern __shared__ __align__(1024) uint8_t sm[];
+    const int tid = threadIdx.x, g = tid / kTile, lt = tid % kTile, warp = tid >> 5, quarter = warp & 3;
+    const uint32_t sA = smemAddr(sm + g * kTcABytes), sW = smemAddr(sm + kTcSmemW);
+    const uint32_t barW = smemAddr(sm + kTcSmemBar), barM = barW + 8 + 8 * g, slot = barW + 8 + 8 * kSlots;
+    if (tid == 0) {
+        mbarInit(barW, 1);
+        for (int i = 0; i < kSlots; i++) mbarInit(barW + 8 + 8 * i, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot), "r"(kTcCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tcBefore();
+    __syncthreads();
+    tcAfter();
+    const uint32_t tmemBase = *reinterpret_cast<volatile uint32_t*>(sm + kTcSmemBar + 8 + 8 * kSlots);
+    const uint32_t tmem = tmemBase + (uint32_t)(g * 64);               // this warpgroup's accumulator
+    const uint32_t tq = tmem + ((uint32_t)(quarter * 32) << 16);        // the lanes (rows) this warp reads
+    if (tid == 0) {
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(barW), "r"((uint32_t)kTcWeightBytes)
+                     : "memory");
+        for (int off = 0; off < kTcWeightBytes; off += 8192) {
+            const uint32_t bytes = (uint32_t)(kTcWeightBytes - off < 8192 ? kTcWeightBytes - off : 8192);
+            asm volatile(
+                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(sW + off),
+                "l"(wTc + off), "r"(bytes), "r"(barW)
+                : "memory");
+        }
+    }
+    bool ok = wgAnd(g, mbarWait(barW, 0));
+    uint32_t phase = 0;
+    const uint64_t tiles = (n + kTile - 1) / kTile;
+    for (uint64_t tile = (uint64_t)blockIdx.x * kSlots + g; ok && tile < tiles; tile += (uint64_t)gridDim.x * kSlots) {
+        // encode this thread's row: chunk 3d + q holds f = 4q .. 4q+3 of input d
+        const uint64_t row = tile * kTile + lt;
+#pragma unroll 1
+        for (int d = 0; d < kIn; d++) {
+            const float xd = row < n ? in[row * kIn + d] : 0.0f;
+#pragma unroll
+            for (int q = 0; q < kFreq / 4; q++) {
+                float sn, cs;
+                sincosBase(xd, 4 * q, sn, cs);
+                uint32_t v[4];
+#pragma unroll
+                for (int r = 0; r < 4; r++) {
+                    if (r) doubleAngle(sn, cs);
+                    v[r] = pack2(sn, cs);
+                }
+                stShared4(sA + (d * 3 + q) * 2048 + lt * 16, v[0], v[1], v[2], v[3]);
+            }
+        }
+        stShared4(sA + (kFeat / 8 - 1) * 2048 + lt * 16, 0u, 0u, 0u, 0u);  // features 168..175
+        proxyFence();
+        tcBefore();
+        wgSync(g);
+#pragma unroll 1
+        for (int l = 0; l < kLayers; l++) {
+            if (lt == 0) {
+                tcAfter();
+                const int K = layerK(l), Np = layerNpad(l);
+                const uint32_t idesc = tcInstr(kTile, Np), wl = sW + tcOffset(l);
+                for (int k = 0; k < K / 16; k++)
+                    tcMma(tmem, tcDesc(sA + k * 2 * 2048, 2048, 128), tcDesc(wl + k * 2 * (Np * 16), Np * 16, 128),
+                          idesc, k > 0 ? 1u : 0u);
+                tcCommit(barM);
+            }
+            ok = wgAnd(g, mbarWait(barM, phase));
+            phase ^= 1u;
+            tcAfter();
+            if (!ok) break;
+            if (l < kLayers - 1) {
+                // ReLU, FP16, and into A as the next layer's input (chunks 0..7)
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    uint32_t v[32];
+                    tcLoad32(tq + h * 32, v);
+                    tcLoadWait();
+#pragma unroll
+                    for (int c = 0; c < 4; c++) {
+                        uint32_t q[4];
+#pragma unroll
+                        for (int e = 0; e < 4; e++)
+                            q[e] = pack2(fmaxf(__uint_as_float(v[c * 8 + 2 * e]), 0.0f),
+                                         fmaxf(__uint_as_float(v[c * 8 + 2 * e + 1]), 0.0f));
+                        stShared4(sA + (h * 4 + c) * 2048 + lt * 16, q[0], q[1], q[2], q[3]);
+                    }
+                }
+                proxyFence();
+            } else {
+                uint32_t v[4];
+                tcLoad4(tq, v);
+                tcLoadWait();
+                if (row < n) {
+#pragma unroll
+                    for (int c = 0; c < 3; c++) {
+                        const float o = __uint_as_float(v[c]);
+                        out[row * 3 + c] = clampNonNeg ? fmaxf(o, 0.0f) : o;
+                    }
+                }
+            }
+            // the next MMAs overwrite the accumulator and read A: all loads and stores first
+            tcBefore();
+            wgSync(g);
+        }
+    }
+    tcBefore();
+    __syncthreads();
+    tcAfter();
+    if (!ok && lt == 0) atomicOr(err, 1u);
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmemBase), "r"(kTcCols) : "memory");
+}
+
 __global__ void kAdam(float* __restrict__ w, float* __restrict__ m, float* __restrict__ v, float* __restrict__ grad,
                       int count, float lr, float b1, float b2, float eps, float c1, float c2) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -421,18 +645,21 @@ __global__ void kAdam(float* __restrict__ w, float* __restrict__ m, float* __res
     grad[i] = 0.0f;
 }
 
-// Refreshes the FP16 forward (n-major) and backward (k-major) copies.
-__global__ void kPackWeights(const float* __restrict__ w, __half* __restrict__ fwd, __half* __restrict__ bwd) {
+// Refreshes the FP16 copies: forward (n-major) and backward (k-major) for
+// training, core-matrix tiles for the tensor-core inference (its padding,
+// zeroed once, is never written).
+__global__ void kPackWeights(const float* __restrict__ w, __half* __restrict__ fwd, __half* __restrict__ bwd,
+                             __half* __restrict__ tc) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kParams) return;
     int l = 0;
     while (l < kLayers - 1 && i >= paramOffset(l + 1)) l++;
-    const int K = layerK(l), N = layerN(l);
+    const int N = layerN(l);
     const int local = i - paramOffset(l), k = local / N, n = local % N;
     const __half h = __float2half_rn(w[i]);
     fwd[fwdOffset(l) + n * fwdStride(l) + k] = h;
     bwd[bwdOffset(l) + k * bwdStride(l) + n] = h;
-    (void)K;
+    tc[(tcOffset(l) + ((k >> 3) * (layerNpad(l) >> 3) + (n >> 3)) * 128 + (n & 7) * 16 + (k & 7) * 2) / 2] = h;
 }
 
 inline unsigned cdiv(uint64_t a, uint64_t b) { return (unsigned)((a + b - 1) / b); }
@@ -452,6 +679,8 @@ struct MlpState {
     float* loss = nullptr;
     __half* wFwd = nullptr;
     __half* wBwd = nullptr;
+    __half* wTc = nullptr;      // inference operand tiles (kTcWeightBytes)
+    uint32_t* err = nullptr;    // bit 0: a tensor-core wait ran out
     uint64_t cap = 0;       // rows of the training buffers
     __half* act[kLayers] = {};
     __half* dy[kLayers] = {};
@@ -491,12 +720,11 @@ int ensureStage(MlpState* s, uint64_t n) {
 }
 
 int pack(MlpState* s, cudaStream_t st) {
-    kPackWeights<<<cdiv(kParams, 256), 256, 0, st>>>(s->w, s->wFwd, s->wBwd);
+    kPackWeights<<<cdiv(kParams, 256), 256, 0, st>>>(s->w, s->wFwd, s->wBwd, s->wTc);
     CR_LAUNCH_CHECK();
     return CR_OK;
 }
 
-constexpr size_t kInferSmem = (size_t)kFwdHalves * sizeof(__half);
 constexpr size_t kTrainSmem = (size_t)(kFwdHalves + kBwdHalves) * sizeof(__half);
 
 }  // namespace
@@ -513,6 +741,10 @@ int mlpCreate(const cr_mlp_config* cfg, MlpState** out) {
     CR_CUDA(cudaMalloc(&s->loss, sizeof(float)));
     CR_CUDA(cudaMalloc(&s->wFwd, kFwdHalves * sizeof(__half)));
     CR_CUDA(cudaMalloc(&s->wBwd, kBwdHalves * sizeof(__half)));
+    CR_CUDA(cudaMalloc(&s->wTc, kTcWeightBytes));
+    CR_CUDA(cudaMemset(s->wTc, 0, kTcWeightBytes));
+    CR_CUDA(cudaMalloc(&s->err, sizeof(uint32_t)));
+    CR_CUDA(cudaMemset(s->err, 0, sizeof(uint32_t)));
     CR_CUDA(cudaMemset(s->wFwd, 0, kFwdHalves * sizeof(__half)));
     CR_CUDA(cudaMemset(s->wBwd, 0, kBwdHalves * sizeof(__half)));
     CR_CUDA(cudaMemset(s->m, 0, kParams * sizeof(float)));
@@ -530,7 +762,7 @@ int mlpCreate(const cr_mlp_config* cfg, MlpState** out) {
         }
     }
     CR_CUDA(cudaMemcpy(s->w, w.data(), kParams * sizeof(float), cudaMemcpyHostToDevice));
-    CR_CUDA(cudaFuncSetAttribute(kInfer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kInferSmem));
+    CR_CUDA(cudaFuncSetAttribute(kInferTc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem));
     CR_CUDA(cudaFuncSetAttribute(kTrainFwdBwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTrainSmem));
     int rc = pack(s, 0);
     if (rc) return rc;
@@ -542,7 +774,7 @@ int mlpCreate(const cr_mlp_config* cfg, MlpState** out) {
 void mlpDestroy(MlpState* s) {
     if (!s) return;
     cudaSetDevice(s->device);
-    void* p[] = {s->w, s->m, s->v, s->grad, s->loss, s->wFwd, s->wBwd, s->stageIn, s->stageOut};
+    void* p[] = {s->w, s->m, s->v, s->grad, s->loss, s->wFwd, s->wBwd, s->wTc, s->err, s->stageIn, s->stageOut};
     for (void* q : p)
         if (q) cudaFree(q);
     for (int l = 0; l < kLayers; l++) {
@@ -554,9 +786,22 @@ void mlpDestroy(MlpState* s) {
 
 int mlpInferDevice(MlpState* s, const float* in, uint64_t n, float* out, bool clampNonNeg, cudaStream_t st) {
     if (n == 0) return CR_OK;
-    const unsigned blocks = std::min<unsigned>(cdiv(n, kWarps * 16), (unsigned)s->sms * 2);
-    kInfer<<<blocks, kThreads, kInferSmem, st>>>(s->wFwd, in, n, out, clampNonNeg ? 1 : 0);
+    // one persistent CTA per SM (its shared memory admits one), fewer for small batches
+    const unsigned blocks = std::min<unsigned>(cdiv(cdiv(n, kTile), kSlots), (unsigned)s->sms);
+    kInferTc<<<blocks, kTile * kSlots, kTcSmem, st>>>(reinterpret_cast<const uint8_t*>(s->wTc), in, n, out,
+                                                        clampNonNeg ? 1 : 0, s->err);
     CR_LAUNCH_CHECK();
+    return CR_OK;
+}
+
+// Reports (and clears) a tensor-core wait that ran out; synchronises.
+int mlpCheck(MlpState* s) {
+    uint32_t e = 0;
+    CR_CUDA(cudaMemcpy(&e, s->err, sizeof(e), cudaMemcpyDeviceToHost));
+    if (e) {
+        CR_CUDA(cudaMemset(s->err, 0, sizeof(uint32_t)));
+        return fail(CR_ERR_CUDA, "radiance-cache inference: a tensor-core wait timed out");
+    }
     return CR_OK;
 }
 
@@ -655,7 +900,7 @@ int cr_mlp_infer(cr_mlp* m, const float* inputs, uint64_t n, float* outputs) {
     rc = mlpInferDevice(m->s, m->s->stageIn, n, m->s->stageOut, false, 0);
     if (rc) return rc;
     CR_CUDA(cudaMemcpy(outputs, m->s->stageOut, n * 3 * sizeof(float), cudaMemcpyDeviceToHost));
-    return CR_OK;
+    return mlpCheck(m->s);
 }
 
 static int gradOrTrain(cr_mlp* m, const float* inputs, const float* targets, uint64_t n, float* grads, float* loss,
@@ -685,6 +930,25 @@ static int gradOrTrain(cr_mlp* m, const float* inputs, const float* targets, uin
     }
     CR_CUDA(cudaDeviceSynchronize());
     return CR_OK;
+}
+
+int cr_mlp_infer_device(cr_mlp* m, const float* inputs, uint64_t n, float* outputs, void* stream) {
+    clearError();
+    if (!m || (n && (!inputs || !outputs))) return fail(CR_ERR_INVALID_ARGUMENT, "NULL argument");
+    CR_CUDA(cudaSetDevice(m->s->device));
+    return mlpInferDevice(m->s, inputs, n, outputs, false, (cudaStream_t)stream);
+}
+
+int cr_mlp_train_step_device(cr_mlp* m, const float* inputs, const float* targets, uint64_t n, void* stream) {
+    clearError();
+    if (!m || (n && (!inputs || !targets))) return fail(CR_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (n == 0) return CR_OK;
+    CR_CUDA(cudaSetDevice(m->s->device));
+    // kAdam leaves the gradient zeroed, so every step starts from zero
+    const cudaStream_t st = (cudaStream_t)stream;
+    int rc = mlpGradDevice(m->s, inputs, targets, n, st);
+    if (rc) return rc;
+    return mlpAdamDevice(m->s, st);
 }
 
 int cr_mlp_gradients(cr_mlp* m, const float* inputs, const float* targets, uint64_t n, float* grads, float* loss) {

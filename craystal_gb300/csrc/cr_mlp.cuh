@@ -18,6 +18,8 @@ int mlpInferDevice(MlpState* s, const float* in, uint64_t n, float* out, bool cl
 int mlpGradDevice(MlpState* s, const float* in, const float* target, uint64_t n, cudaStream_t st);
 int mlpAdamDevice(MlpState* s, cudaStream_t st);
 float* mlpLossPtr(MlpState* s);
+// reports a tensor-core wait of the inference that ran out (synchronises)
+int mlpCheck(MlpState* s);
 
 }  // namespace cr
 

@@ -71,15 +71,17 @@ __device__ __forceinline__ float raySphere(float3 o, float3 d, float4 s, float t
 
 // SceneView::intersect (Scene/Scene.cu:5-14): the BVH, then the sphere
 // lights (an extension) under the closest-hit rule.
-__device__ __forceinline__ bool closest(PathCtx& c, float3 o, float3 d, THit& h) {
+template <int kShared = 0>
+__device__ __forceinline__ bool closest(PathCtx& c, float3 o, float3 d, THit& h,
+                                        uint2 (*shStack)[kStackBlock] = nullptr) {
     c.rays++;
     h.t = INFINITY;
     h.prim = CR_MISS;
     h.u = h.v = 0.0f;
     const TRay r = makeTRay(o, 0.0f, d, INFINITY);
     bool hit = false;
-    if (c.sc.sph.hasRoot) hit = traverseSpheres<false>(c.sc, r, h);
-    hit |= traverse<false>(c.sc, r, h);
+    if (c.sc.sph.hasRoot) hit = traverseSpheres<false, kShared>(c.sc, r, h, shStack);
+    hit |= traverse<false, kShared>(c.sc, r, h, shStack);
     for (uint32_t i = 0; i < c.sc.nSpheres; i++) {
         const float t = raySphere(o, d, __ldg(c.sc.spheres + i), 0.0f, h.t);
         if (t < h.t) {

@@ -8,7 +8,7 @@
 namespace cr {
 namespace {
 
-constexpr int kTraceThreads = 128;
+constexpr int kTraceThreads = kStackBlock;  // the top of the stack is in shared memory
 
 // One thread per ray.  (A persistent variant that refills the lanes of a
 // warp from a per-warp ray range measured slower on GB300 for this
@@ -21,6 +21,7 @@ template <bool kAnyHit, bool kSpheres>
 __global__ void __launch_bounds__(kTraceThreads) kTrace(const SceneView sc, const cr_ray* __restrict__ rays,
                                                         uint64_t n, cr_hit* __restrict__ hits,
                                                         uint8_t* __restrict__ occ) {
+    __shared__ SharedStackArea stk;
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float4* rp = reinterpret_cast<const float4*>(rays + i);
@@ -31,8 +32,8 @@ __global__ void __launch_bounds__(kTraceThreads) kTrace(const SceneView sc, cons
     h.u = h.v = 0.0f;
     h.prim = CR_MISS;
     bool hit = false;
-    if (kSpheres) hit = traverseSpheres<kAnyHit>(sc, r, h);
-    if (!(kAnyHit && hit)) hit |= traverse<kAnyHit>(sc, r, h);
+    if (kSpheres) hit = traverseSpheres<kAnyHit, kSharedStack>(sc, r, h, stk);
+    if (!(kAnyHit && hit)) hit |= traverse<kAnyHit, kSharedStack>(sc, r, h, stk);
     if (kAnyHit) {
         occ[i] = hit ? 1 : 0;
     } else {

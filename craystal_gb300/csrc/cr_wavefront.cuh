@@ -121,6 +121,7 @@ __device__ __forceinline__ void addRays(unsigned long long* counter, uint32_t ra
 //
 // One scene: path g is pixel g mod (w h) at sample p.first + g / (w h).
 struct OneScene {
+    static constexpr int kShadeMinBlocks = 4;  // 128 registers
     SceneView view;
     CameraGpu cam;
     Params p;
@@ -162,6 +163,8 @@ struct __align__(16) WfScene {
 };
 
 struct ManyScenes {
+    // 128 registers: it spills there, but 3 blocks of 168 measured 10 % slower
+    static constexpr int kShadeMinBlocks = 4;
     const WfScene* scenes;
     uint32_t n;
     __device__ __forceinline__ const SceneView& sceneOf(uint32_t i) const { return scenes[i].view; }
@@ -233,6 +236,8 @@ __global__ void __launch_bounds__(kWfThreads) kWfExtend(const __grid_constant__ 
                                                         const uint32_t* __restrict__ queue,
                                                         const uint32_t* __restrict__ count,
                                                         uint32_t* __restrict__ keys) {
+    static_assert(kWfThreads == kStackBlock, "the extension query keeps the top of its stack in shared memory");
+    __shared__ SharedStackArea stk;
     const uint32_t n = *count;
     if (blockIdx.x * blockDim.x >= n) return;  // the whole block is past the live paths
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -244,7 +249,7 @@ __global__ void __launch_bounds__(kWfThreads) kWfExtend(const __grid_constant__ 
         PathCtx c{sc, 0u, SpectralPath{}};
         const float4 o = st.ro[k], d = st.rd[k];
         THit h;
-        closest(c, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), h);
+        closest<kSharedStack>(c, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), h, stk);
         st.hit[k] = make_float4(__uint_as_float(h.prim), h.t, h.u, h.v);
         const uint32_t nMats = src.nMatsOf(item);
         uint32_t key;
@@ -351,7 +356,7 @@ __global__ void kWfAdvance(uint32_t* __restrict__ counts, uint32_t* __restrict__
 // supplies the hooks of shadeBounce (with their per-path state in st.aux)
 // and what happens to a path that ends.
 template <class Src, class Mode>
-__global__ void __launch_bounds__(kWfThreads) kWfShade(const __grid_constant__ Src src, WfState st,
+__global__ void __launch_bounds__(kWfThreads, Src::kShadeMinBlocks) kWfShade(const __grid_constant__ Src src, WfState st,
                                                        const __grid_constant__ Mode mode,
                                                        const uint32_t* __restrict__ order,
                                                        const uint32_t* __restrict__ count, uint32_t depth,

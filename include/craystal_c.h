@@ -423,6 +423,13 @@ int cr_mlp_gradients(cr_mlp* mlp, const float* inputs, const float* targets,
 /* one Adam step on n samples; loss (may be NULL) before the step */
 int cr_mlp_train_step(cr_mlp* mlp, const float* inputs, const float* targets,
                       uint64_t n, float* loss);
+/* The same two operations on device-resident buffers, ordered on `stream`
+ * (NULL = the default stream) and returning without waiting: inputs n x 7,
+ * outputs / targets n x 3 device floats.  These are the calls the cached
+ * integrator makes each frame. */
+int cr_mlp_infer_device(cr_mlp* mlp, const float* inputs, uint64_t n, float* outputs, void* stream);
+int cr_mlp_train_step_device(cr_mlp* mlp, const float* inputs, const float* targets,
+                             uint64_t n, void* stream);
 
 /* ---- path tracing with the radiance cache (no counterpart in the
  * reference) ----
@@ -437,8 +444,10 @@ int cr_mlp_train_step(cr_mlp* mlp, const float* inputs, const float* targets,
  * Frames use sample indices first_sample, first_sample + 1, ... */
 typedef struct {
     uint32_t query_vertex;   /* 1 */
-    uint32_t train_every;    /* 16; 0 = about train_samples records per frame */
-    uint32_t train_samples;  /* 65536 (2^16 path suffixes per frame) */
+    uint32_t train_every;    /* 0 = adaptive: the spacing that yields about
+                                train_samples records per frame, re-aimed after
+                                every frame from the records it produced */
+    uint32_t train_samples;  /* 8192 (path suffixes per frame; 0 = 8192) */
     uint32_t train_steps;    /* 1 */
     uint32_t freeze;         /* 1 = render with the cache as it is, no training */
     float scene_min[3];      /* position normalisation box; scene_max <= scene_min */
@@ -449,6 +458,7 @@ typedef struct {
     uint64_t queries;
     uint64_t train_records;
     float last_loss;
+    uint32_t last_train_every;  /* training-path spacing of the last frame */
 } cr_cache_stats;
 /* stats (may be NULL) is added to, not reset. */
 int cr_render_cached(cr_scene* scene, const cr_integrator_config* cfg,

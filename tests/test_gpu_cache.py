@@ -112,3 +112,22 @@ def test_trained_network_recovers_the_light_beyond_the_query(gpu_lib):
     e_cache = rel_mse(rgb / w[..., None], ref)
     print(f"relMSE: zeroed network {e_trunc:.5f}, trained network {e_cache:.5f}")
     assert e_cache < 0.5 * e_trunc, (e_cache, e_trunc)
+
+
+def test_adaptive_training_spacing_tracks_the_batch(gpu_lib):
+    """train_every = 0: after each frame the spacing of the training paths is
+    re-aimed at train_samples records per frame, so a frame fills most of its
+    batch, and a smaller batch leaves sparser (cheaper) training paths."""
+    sc, _ = cornell(128)
+    spacing = {}
+    for cap in (1024, 8192):
+        integ = CachedPathTraceIntegrator(CFG, train_samples=cap)
+        integ.dispatch(sc, 24, readback=False)
+        spacing[cap] = integ.stats.last_train_every
+        before = integ.stats.train_records
+        # a separate call continues from the spacing the scene reached
+        integ.dispatch(sc, 1, first_sample=100, readback=False)
+        got = integ.stats.train_records - before
+        assert 0.3 * cap <= got <= cap, (cap, got)
+        assert integ.stats.last_train_every >= 1
+    assert spacing[1024] > 2 * spacing[8192], spacing

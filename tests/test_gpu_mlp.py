@@ -51,6 +51,19 @@ def test_inference_matches_fp64(net):
     np.testing.assert_allclose(out, y, rtol=1e-3, atol=1e-3 * np.abs(y).max())
 
 
+@pytest.mark.parametrize("n", [1, 127, 128, 129, 383, 385, 70001])
+def test_inference_ragged_batches(net, n):
+    """Tensor-core inference over partial tiles (128 queries per tile, three
+    tiles per CTA in flight) and over grids of one CTA up to one per SM."""
+    from craystal_gb300._lib import check, load, ptr
+    x, _ = _inputs(n, 10 + n)
+    out = np.full((n, 3), np.nan, np.float32)
+    check(load().cr_mlp_infer(net, ptr(x), n, ptr(out)))
+    y, _ = ref.forward(_params(net), x)
+    assert np.isfinite(out).all()
+    np.testing.assert_allclose(out, y, rtol=1e-3, atol=1e-3 * np.abs(y).max())
+
+
 def test_gradients_match_fp64(net):
     from craystal_gb300._lib import check, load, ptr
     x, t = _inputs(4096, 2)
@@ -93,3 +106,47 @@ def test_adam_step_matches_fp64(net):
     m = np.abs(g) > 1e-6
     assert m.mean() > 0.5
     np.testing.assert_allclose(p1[m], expect[m], rtol=1e-5, atol=1e-6)
+
+
+def test_device_forms_match_host_forms(gpu_lib):
+    """cr_mlp_infer_device / cr_mlp_train_step_device (device buffers, the
+    calls the cached integrator makes) give what the host-buffer forms give."""
+    import torch
+    from craystal_gb300._lib import CrMlpConfig, check, load, ptr
+    lib = load()
+    nets = []
+    for _ in range(2):
+        h = ctypes.c_void_p()
+        check(lib.cr_mlp_create(ctypes.byref(CrMlpConfig(1e-2, 0.9, 0.99, 1e-8, 11)), ctypes.byref(h)))
+        nets.append(h)
+    try:
+        x, t = _inputs(5000, 5)
+        out_h = np.zeros((len(x), 3), np.float32)
+        check(lib.cr_mlp_infer(nets[0], ptr(x), len(x), ptr(out_h)))
+        dx, dt = torch.from_numpy(x).cuda(), torch.from_numpy(t).cuda()
+        dout = torch.empty((len(x), 3), dtype=torch.float32, device="cuda")
+        s = torch.cuda.current_stream()
+        check(lib.cr_mlp_infer_device(nets[1], dx.data_ptr(), len(x), dout.data_ptr(), s.cuda_stream))
+        assert np.array_equal(dout.cpu().numpy(), out_h)
+        g = np.zeros(lib.cr_mlp_param_count(), np.float32)
+        check(lib.cr_mlp_gradients(nets[0], ptr(x), ptr(t), len(x), ptr(g), None))
+        check(lib.cr_mlp_train_step(nets[0], ptr(x), ptr(t), len(x), None))
+        check(lib.cr_mlp_train_step_device(nets[1], dx.data_ptr(), dt.data_ptr(), len(x), s.cuda_stream))
+        torch.cuda.synchronize()
+        p0, p1 = _params(nets[0]), _params(nets[1])
+        # gradients are summed with float atomics, so compare where |g| is
+        # well above their noise; elsewhere both moved by at most 2 lr
+        m = np.abs(g) > 1e-6
+        assert m.mean() > 0.5
+        np.testing.assert_allclose(p1[m], p0[m], rtol=1e-5, atol=1e-6)
+        assert np.abs(p1 - p0).max() <= 2.0 * 1e-2 + 1e-6
+        # a second device step keeps training: the loss goes down
+        for _ in range(50):
+            check(lib.cr_mlp_train_step_device(nets[1], dx.data_ptr(), dt.data_ptr(), len(x), s.cuda_stream))
+        torch.cuda.synchronize()
+        l0, _ = ref.loss_and_grads(p0, x, t)
+        l1, _ = ref.loss_and_grads(_params(nets[1]), x, t)
+        assert l1 < l0
+    finally:
+        for h in nets:
+            lib.cr_mlp_destroy(h)
