@@ -284,7 +284,9 @@ int buildBvh(cr_scene* s);
 int buildSphereBvh(cr_scene* s);
 int exportBvh(const cr_scene* s, cr_bvh_node* nodes, uint32_t* primMap);
 // implemented in cr_trace.cu
-int traceClosestDevice(cr_scene* s, const cr_ray* rays, uint64_t n, cr_hit* hits, cudaStream_t st);
+// mayAllocate = false: no device allocation (the no-allocation entry point)
+int traceClosestDevice(cr_scene* s, const cr_ray* rays, uint64_t n, cr_hit* hits, cudaStream_t st,
+                       bool mayAllocate = true);
 int traceOccludedDevice(cr_scene* s, const cr_ray* rays, uint64_t n, uint8_t* occ, cudaStream_t st);
 // implemented in cr_render.cu
 int renderWavefront(cr_scene* s, const cr_integrator_config* cfg, uint32_t spp, uint32_t first,

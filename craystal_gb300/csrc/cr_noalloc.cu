@@ -85,7 +85,7 @@ extern "C" int cr_trace_closest_noalloc(cr_scene* scene, const cr_ray* rays, uin
     if (rc) return rc;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     CR_CUDA(cudaMemcpyAsync(a.rays, rays, n * sizeof(cr_ray), cudaMemcpyHostToDevice, st));
-    rc = traceClosestDevice(scene, a.rays, n, a.hits, st);
+    rc = traceClosestDevice(scene, a.rays, n, a.hits, st, false);
     if (rc) return rc;
     CR_CUDA(cudaMemcpyAsync(hits, a.hits, n * sizeof(cr_hit), cudaMemcpyDeviceToHost, st));
     CR_CUDA(cudaStreamSynchronize(st));

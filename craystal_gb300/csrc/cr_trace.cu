@@ -10,13 +10,9 @@ namespace {
 
 constexpr int kTraceThreads = kStackBlock;  // the top of the stack is in shared memory
 
-// One thread per ray.  (A persistent variant that refills the lanes of a
-// warp from a per-warp ray range measured slower on GB300 for this
-// incoherent workload: the lanes' rounds synchronise on the slowest lane.)
-//
-// kSpheres: the scene has analytic spheres, tested first as
-// SceneView::intersect does (a separate instance keeps the triangle-only
-// kernel free of the sphere code).
+// One thread per ray: the form for scenes with analytic spheres, which are
+// tested first as SceneView::intersect does (a separate instance keeps the
+// triangle-only kernels free of the sphere code).
 template <bool kAnyHit, bool kSpheres>
 __global__ void __launch_bounds__(kTraceThreads) kTrace(const SceneView sc, const cr_ray* __restrict__ rays,
                                                         uint64_t n, cr_hit* __restrict__ hits,
@@ -42,33 +38,144 @@ __global__ void __launch_bounds__(kTraceThreads) kTrace(const SceneView sc, cons
     }
 }
 
-constexpr uint64_t kMaxRaysPerLaunch = 0x7fffffffull * kTraceThreads;
+// Triangle-only scenes: persistent blocks with dynamic ray fetch.  The
+// lanes of a warp take rays from a counter as they finish, at least kRefill
+// lanes at a time, so that a warp keeps most of its lanes busy until the
+// rays run out instead of waiting for its slowest ray (incoherent rays leave
+// a one-ray-per-thread warp with 6 of 32 lanes busy on average).  Every ray
+// is traversed exactly as in kTrace (the same cursor, order and culling);
+// only the lane that carries it changes.
+//
+// counter != nullptr: one zeroed device counter over all n rays, which
+// keeps every SM busy to the end (12 % faster than one ray per thread on the
+// 16M-ray cast).  nullptr: block b takes rays [b * chunk, (b + 1) * chunk)
+// from a shared-memory counter, for callers that allocate nothing (4 %).
+constexpr int kRefill = 8;
 
 template <bool kAnyHit>
-int launchTrace(cr_scene* s, const cr_ray* rays, uint64_t n, cr_hit* hits, uint8_t* occ, cudaStream_t st) {
+__global__ void __launch_bounds__(kTraceThreads) kTraceDyn(const SceneView sc, const cr_ray* __restrict__ rays,
+                                                           uint64_t n, cr_hit* __restrict__ hits,
+                                                           uint8_t* __restrict__ occ,
+                                                           unsigned long long* __restrict__ counter) {
+    __shared__ SharedStackArea stk;
+    __shared__ unsigned long long blockNext;
+    uint64_t hi = n;
+    unsigned long long* next = counter;
+    if (!counter) {
+        const uint64_t chunk = (n + gridDim.x - 1) / gridDim.x;
+        const uint64_t lo = min(n, (uint64_t)blockIdx.x * chunk);
+        hi = min(n, lo + chunk);
+        if (threadIdx.x == 0) blockNext = lo;
+        next = &blockNext;
+    }
+    __syncthreads();
+    const BvhView bv{sc.pairs, sc.leaves, sc.rootRef, sc.rootFlags, sc.rootMin, sc.rootMax, sc.hasRoot};
+    const TriLeaf<kAnyHit> leaf{sc.leaves, sc.tris};
+    TravStack<kSharedStack> stack;
+    stack.sh = stk;
+    TravState cur;
+    TRay r;
+    THit h;
+    uint64_t idx = 0;
+    bool active = false, exhausted = false;
+    const int lane = threadIdx.x & 31;
+    const unsigned full = 0xffffffffu;
+    auto finish = [&](bool hit) {
+        if (kAnyHit) {
+            occ[idx] = hit ? 1 : 0;
+        } else {
+            reinterpret_cast<float4*>(hits)[idx] = hit ? make_float4(__uint_as_float(h.prim), h.t, h.u, h.v)
+                                                       : make_float4(__uint_as_float(CR_MISS), INFINITY, 0.0f, 0.0f);
+        }
+    };
+    while (true) {
+        const unsigned idle = __ballot_sync(full, !active);
+        if (!exhausted && __popc(idle) >= kRefill) {
+            const int leader = __ffs(idle) - 1;
+            unsigned long long base = 0;
+            if (lane == leader) base = atomicAdd(next, (unsigned long long)__popc(idle));
+            base = __shfl_sync(full, base, leader);
+            if (base + (unsigned)__popc(idle) >= hi) exhausted = true;
+            if (!active) {
+                idx = base + (unsigned)__popc(idle & ((1u << lane) - 1u));
+                if (idx < hi) {
+                    const float4* rp = reinterpret_cast<const float4*>(rays + idx);
+                    const float4 a = __ldg(rp), b = __ldg(rp + 1);
+                    r = makeTRay(mk3(a.x, a.y, a.z), a.w, mk3(b.x, b.y, b.z), b.w);
+                    h.t = INFINITY;
+                    h.u = h.v = 0.0f;
+                    h.prim = CR_MISS;
+                    if (travBegin(cur, bv, r)) active = true;
+                    else finish(false);
+                }
+            }
+        }
+        if (!__any_sync(full, active)) {
+            if (exhausted) break;
+            continue;  // every lane idle: the next round refills all 32
+        }
+        if (active && !travStep<kAnyHit>(cur, stack, bv, sc.errFlags, leaf, r, h)) {
+            finish(cur.isHit);
+            active = false;
+        }
+    }
+}
+
+int traceDynBlocks(bool anyHit, uint64_t n) {
+    static int occClosest = 0, occAny = 0;
+    int& occ = anyHit ? occAny : occClosest;
+    if (!occ) {
+        int b = 0;
+        if (anyHit) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kTraceDyn<true>, kTraceThreads, 0);
+        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kTraceDyn<false>, kTraceThreads, 0);
+        occ = b > 0 ? b : 1;
+    }
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const uint64_t perThread = (n + kTraceThreads - 1) / kTraceThreads;
+    return (int)std::min<uint64_t>((uint64_t)sms * occ, std::max<uint64_t>(1, perThread));
+}
+
+constexpr uint64_t kMaxRaysPerLaunch = 0x7fffffffull * kTraceThreads;
+
+// mayAllocate: the ray counter of the dynamic fetch is a stream-ordered
+// allocation (cudaMallocAsync / cudaFreeAsync on st), so that calls on
+// different streams never share one; without it, per-block ranges.
+template <bool kAnyHit>
+int launchTrace(cr_scene* s, const cr_ray* rays, uint64_t n, cr_hit* hits, uint8_t* occ, cudaStream_t st,
+                bool mayAllocate) {
     const SceneView v = s->view();
     for (uint64_t off = 0; off < n; off += kMaxRaysPerLaunch) {
         const uint64_t m = std::min(n - off, kMaxRaysPerLaunch);
         const unsigned blocks = (unsigned)((m + kTraceThreads - 1) / kTraceThreads);
-        if (s->sphHasRoot)
+        if (s->sphHasRoot) {
             kTrace<kAnyHit, true><<<blocks, kTraceThreads, 0, st>>>(v, rays + off, m, hits ? hits + off : nullptr,
                                                                     occ ? occ + off : nullptr);
-        else
-            kTrace<kAnyHit, false><<<blocks, kTraceThreads, 0, st>>>(v, rays + off, m, hits ? hits + off : nullptr,
-                                                                     occ ? occ + off : nullptr);
+            CR_LAUNCH_CHECK();
+            continue;
+        }
+        unsigned long long* counter = nullptr;
+        if (mayAllocate) {
+            CR_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&counter), sizeof(unsigned long long), st));
+            CR_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st));
+        }
+        kTraceDyn<kAnyHit><<<traceDynBlocks(kAnyHit, m), kTraceThreads, 0, st>>>(
+            v, rays + off, m, hits ? hits + off : nullptr, occ ? occ + off : nullptr, counter);
         CR_LAUNCH_CHECK();
+        if (counter) CR_CUDA(cudaFreeAsync(counter, st));
     }
     return CR_OK;
 }
 
 }  // namespace
 
-int traceClosestDevice(cr_scene* s, const cr_ray* rays, uint64_t n, cr_hit* hits, cudaStream_t st) {
-    return launchTrace<false>(s, rays, n, hits, nullptr, st);
+int traceClosestDevice(cr_scene* s, const cr_ray* rays, uint64_t n, cr_hit* hits, cudaStream_t st, bool mayAllocate) {
+    return launchTrace<false>(s, rays, n, hits, nullptr, st, mayAllocate);
 }
 
 int traceOccludedDevice(cr_scene* s, const cr_ray* rays, uint64_t n, uint8_t* occ, cudaStream_t st) {
-    return launchTrace<true>(s, rays, n, nullptr, occ, st);
+    return launchTrace<true>(s, rays, n, nullptr, occ, st, true);
 }
 
 }  // namespace cr

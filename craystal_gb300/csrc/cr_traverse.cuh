@@ -255,65 +255,84 @@ struct SphereLeaf {
     }
 };
 
-// BVHData::intersect (Core/BVH.cu:13-84) for one ray over one BVH.  h.t
-// must hold the initial closest t (infinity for a fresh RayHit).  Returns
-// whether any primitive was hit inside [tMin, tMax] (not only closer ones),
-// as the reference does.
+// BVHData::intersect (Core/BVH.cu:13-84) for one ray over one BVH, as a
+// resumable traversal: travBegin() tests the root box, each travStep() is
+// one iteration of the traversal loop (a culled entry, a leaf or an interior
+// node).  The scalar state (TravState) is kept apart from the stack array so
+// that it stays in registers.
 //
-// One loop; the entry e being visited lives in registers.  When both
-// children pass, the far one is pushed and the near one becomes e (the
-// reference pushes both and pops the near one at once); an entry taken from
-// the stack is culled at the top of the loop when its distance is beyond
-// the closest hit, as at Core/BVH.cu:34-36.
+// The entry e being visited lives in registers.  When both children pass,
+// the far one is pushed and the near one becomes e (the reference pushes
+// both and pops the near one at once); an entry taken from the stack is
+// culled when its distance is beyond the closest hit, as at
+// Core/BVH.cu:34-36.  h.t must hold the initial closest t (infinity for a
+// fresh RayHit).  isHit: whether any primitive was hit inside [tMin, tMax]
+// (not only closer ones), as the reference returns.
+struct TravState {
+    uint2 e;
+    int sp;
+    bool isHit;
+};
+
+// false: the ray misses the root box and there is nothing to visit
+__device__ __forceinline__ bool travBegin(TravState& s, const BvhView& bv, const TRay& r) {
+    s.sp = 0;
+    s.isHit = false;
+    s.e = make_uint2(bv.rootRef, __float_as_uint(0.0f));
+    float tr;
+    return bv.hasRoot && boxTest(bv.rootMin, bv.rootMax, bv.rootFlags, r, tr);
+}
+
+// One iteration; false once the traversal is over (an any-hit query that
+// found a hit stops at once).
+template <bool kAnyHit, class Leaf, class Stack>
+__device__ __forceinline__ bool travStep(TravState& s, Stack& stack, const BvhView& bv, uint32_t* errFlags,
+                                         const Leaf& leaf, const TRay& r, THit& h) {
+    if (__uint_as_float(s.e.y) > h.t || (s.e.x & kLeafBit)) {
+        if (!(__uint_as_float(s.e.y) > h.t) && leaf(r, h, s.isHit, s.e.x)) return false;
+        if (s.sp == 0) return false;
+        s.e = stack.get(--s.sp);
+        return true;
+    }
+    const float4* np = reinterpret_cast<const float4*>(bv.pairs + s.e.x);
+    const float4 p0 = __ldg(np), p1 = __ldg(np + 1), p2 = __ldg(np + 2);
+    const uint4 ref = __ldg(reinterpret_cast<const uint4*>(np + 3));
+    float lt = INFINITY, rt = INFINITY;
+    const bool hl = boxTest(mk3(p0.x, p0.y, p0.z), mk3(p0.w, p1.x, p1.y), ref.z & 7u, r, lt);
+    const bool hr = boxTest(mk3(p1.z, p1.w, p2.x), mk3(p2.y, p2.z, p2.w), (ref.z >> 3) & 7u, r, rt);
+    const float ct = h.t;
+    const bool gl = hl && lt < ct, gr = hr && rt < ct;
+    if (gl && gr) {
+        // near = the child the reference pushes last: right when lt > rt
+        const bool rightNear = lt > rt;
+        if (s.sp >= kStackSize) {  // unreachable for depth <= 20; never overrun
+            atomicOr(errFlags, kErrStackOverflow);
+            return false;
+        }
+        stack.put(s.sp++, rightNear ? make_uint2(ref.x, __float_as_uint(lt)) : make_uint2(ref.y, __float_as_uint(rt)));
+        s.e = rightNear ? make_uint2(ref.y, __float_as_uint(rt)) : make_uint2(ref.x, __float_as_uint(lt));
+        return true;
+    }
+    if (gl || gr) {
+        s.e = gl ? make_uint2(ref.x, __float_as_uint(lt)) : make_uint2(ref.y, __float_as_uint(rt));
+        return true;
+    }
+    if (s.sp == 0) return false;
+    s.e = stack.get(--s.sp);
+    return true;
+}
+
+// The whole traversal of one ray; returns isHit.
 template <bool kAnyHit, class Leaf, int kShared = 0>
 __device__ __forceinline__ bool traverseBvh(const BvhView& bv, uint32_t* errFlags, const Leaf& leaf, const TRay& r,
                                             THit& h, uint2 (*shStack)[kStackBlock] = nullptr) {
-    float tr;
-    if (!bv.hasRoot || !boxTest(bv.rootMin, bv.rootMax, bv.rootFlags, r, tr)) return false;
     TravStack<kShared> stack;
     stack.sh = shStack;
-    int sp = 0;
-    uint2 e = make_uint2(bv.rootRef, __float_as_uint(0.0f));
-    bool have = true, isHit = false;
-    while (have) {
-        if (__uint_as_float(e.y) > h.t) {
-            have = sp > 0;
-            if (have) e = stack.get(--sp);
-            continue;
-        }
-        if (e.x & kLeafBit) {
-            if (leaf(r, h, isHit, e.x)) return true;
-            have = sp > 0;
-            if (have) e = stack.get(--sp);
-            continue;
-        }
-        const float4* np = reinterpret_cast<const float4*>(bv.pairs + e.x);
-        const float4 p0 = __ldg(np), p1 = __ldg(np + 1), p2 = __ldg(np + 2);
-        const uint4 ref = __ldg(reinterpret_cast<const uint4*>(np + 3));
-        float lt = INFINITY, rt = INFINITY;
-        const bool hl = boxTest(mk3(p0.x, p0.y, p0.z), mk3(p0.w, p1.x, p1.y), ref.z & 7u, r, lt);
-        const bool hr = boxTest(mk3(p1.z, p1.w, p2.x), mk3(p2.y, p2.z, p2.w), (ref.z >> 3) & 7u, r, rt);
-        const float ct = h.t;
-        const bool gl = hl && lt < ct, gr = hr && rt < ct;
-        if (gl && gr) {
-            // near = the child the reference pushes last: right when lt > rt
-            const bool rightNear = lt > rt;
-            if (sp >= kStackSize) {  // unreachable for depth <= 20; never overrun
-                atomicOr(errFlags, kErrStackOverflow);
-                break;
-            }
-            stack.put(sp++, rightNear ? make_uint2(ref.x, __float_as_uint(lt)) : make_uint2(ref.y, __float_as_uint(rt)));
-            e = rightNear ? make_uint2(ref.y, __float_as_uint(rt)) : make_uint2(ref.x, __float_as_uint(lt));
-        } else if (gl) {
-            e = make_uint2(ref.x, __float_as_uint(lt));
-        } else if (gr) {
-            e = make_uint2(ref.y, __float_as_uint(rt));
-        } else {
-            have = sp > 0;
-            if (have) e = stack.get(--sp);
-        }
+    TravState s;
+    if (!travBegin(s, bv, r)) return false;
+    while (travStep<kAnyHit>(s, stack, bv, errFlags, leaf, r, h)) {
     }
-    return isHit;
+    return s.isHit;
 }
 
 // The triangle BVH of the scene.

@@ -79,7 +79,7 @@ inline int ensureWavefrontBuffers(void*& slot, uint32_t cap, uint32_t nKeys, WfB
         CR_CUDA(wfAlloc(b->qb, cap));
         CR_CUDA(wfAlloc(b->keys, cap));
         CR_CUDA(wfAlloc(b->sorted, cap));
-        CR_CUDA(wfAlloc(b->counts, 2));
+        CR_CUDA(wfAlloc(b->counts, 3));  // live paths, next queue, extension fetch counter
         CR_CUDA(wfAlloc(b->hist, nKeys));
         b->cap = cap;
         b->keyCap = nKeys;
@@ -231,25 +231,45 @@ __global__ void __launch_bounds__(kWfThreads) kWfInit(const __grid_constant__ Sr
 
 // The closest-hit query of every live path; key = the scene's key base plus
 // the material to shade (nMats for a miss, nMats + 1 for a sphere light).
+//
+// Persistent blocks with dynamic fetch: the lanes of a warp take queue
+// entries from counts[2] (zeroed by the kernel before) as they finish, at
+// least kWfRefill at a time, so that a warp keeps most lanes busy until the
+// queue runs out instead of waiting for its slowest ray.  Each query is the
+// closest() of the megakernel: the analytic-sphere BVH first (run whole when
+// the scene has one), then the triangle BVH one cursor step per round, then
+// the sphere lights; only the lane that carries a path changes.
+constexpr int kWfRefill = 8;
+
 template <class Src>
 __global__ void __launch_bounds__(kWfThreads) kWfExtend(const __grid_constant__ Src src, WfState st,
                                                         const uint32_t* __restrict__ queue,
-                                                        const uint32_t* __restrict__ count,
+                                                        uint32_t* __restrict__ counts,
                                                         uint32_t* __restrict__ keys) {
     static_assert(kWfThreads == kStackBlock, "the extension query keeps the top of its stack in shared memory");
     __shared__ SharedStackArea stk;
-    const uint32_t n = *count;
-    if (blockIdx.x * blockDim.x >= n) return;  // the whole block is past the live paths
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    uint32_t item = 0, rays = 0;
-    if (i < n) {
-        const uint32_t k = queue[i];
-        item = st.item[k];
+    const uint32_t n = counts[0];
+    if (blockIdx.x * blockDim.x >= n) return;  // more blocks than the queue needs (uniform per block)
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    TravStack<kSharedStack> stack;
+    stack.sh = stk;
+    TravState cur;
+    TRay r;
+    THit h;
+    bool active = false, exhausted = false;
+    uint32_t i = 0, k = 0, item = 0;
+    // rays traced and not yet added to the counter of scene rayItem
+    uint32_t pending = 0, rayItem = 0;
+    auto finish = [&]() {
         const SceneView& sc = src.sceneOf(item);
-        PathCtx c{sc, 0u, SpectralPath{}};
-        const float4 o = st.ro[k], d = st.rd[k];
-        THit h;
-        closest<kSharedStack>(c, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), h, stk);
+        for (uint32_t q = 0; q < sc.nSpheres; q++) {
+            const float t = raySphere(r.o, r.d, __ldg(sc.spheres + q), 0.0f, h.t);
+            if (t < h.t) {
+                h.t = t;
+                h.prim = kSpherePrim + q;
+            }
+        }
         st.hit[k] = make_float4(__uint_as_float(h.prim), h.t, h.u, h.v);
         const uint32_t nMats = src.nMatsOf(item);
         uint32_t key;
@@ -258,9 +278,69 @@ __global__ void __launch_bounds__(kWfThreads) kWfExtend(const __grid_constant__ 
         else if (isSphereHit(h.prim)) key = __ldg(sc.sphMat + (h.prim & ~kSphereBit));
         else key = sc.meshes[sc.primToMesh[h.prim]].material_id;
         keys[i] = src.keyBase(item) + key;
-        rays = c.rays;
+    };
+    while (true) {
+        const unsigned idle = __ballot_sync(full, !active);
+        if (!exhausted && __popc(idle) >= kWfRefill) {
+            const int leader = __ffs(idle) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(counts + 2, (uint32_t)__popc(idle));
+            base = __shfl_sync(full, base, leader);
+            if (base + (uint32_t)__popc(idle) >= n) exhausted = true;
+            if (!active) {
+                i = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
+                if (i < n) {
+                    k = queue[i];
+                    item = st.item[k];
+                    if (item != rayItem) {
+                        if (pending) atomicAdd(src.raysOf(rayItem), (unsigned long long)pending);
+                        pending = 0;
+                        rayItem = item;
+                    }
+                    pending++;
+                    const SceneView& sc = src.sceneOf(item);
+                    const float4 o = st.ro[k], d = st.rd[k];
+                    r = makeTRay(mk3(o.x, o.y, o.z), 0.0f, mk3(d.x, d.y, d.z), INFINITY);
+                    h.t = INFINITY;
+                    h.prim = CR_MISS;
+                    h.u = h.v = 0.0f;
+                    if (sc.sph.hasRoot) traverseSpheres<false, kSharedStack>(sc, r, h, stk);
+                    const BvhView bv{sc.pairs, sc.leaves, sc.rootRef, sc.rootFlags, sc.rootMin, sc.rootMax, sc.hasRoot};
+                    if (travBegin(cur, bv, r)) active = true;
+                    else finish();
+                }
+            }
+        }
+        if (!__any_sync(full, active)) {
+            if (exhausted) break;
+            continue;  // every lane idle: the next round refills all 32
+        }
+        if (active) {
+            const SceneView& sc = src.sceneOf(item);
+            const BvhView bv{sc.pairs, sc.leaves, sc.rootRef, sc.rootFlags, sc.rootMin, sc.rootMax, sc.hasRoot};
+            const TriLeaf<false> leaf{sc.leaves, sc.tris};
+            if (!travStep<false>(cur, stack, bv, sc.errFlags, leaf, r, h)) {
+                finish();
+                active = false;
+            }
+        }
     }
-    addRays(src.raysOf(item), rays);
+    addRays(src.raysOf(rayItem), pending);
+}
+
+// Blocks of the persistent extension kernel: as many as stay resident.
+template <class Src>
+unsigned wfExtendBlocks() {
+    static int occ = 0;
+    if (!occ) {
+        int b = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kWfExtend<Src>, kWfThreads, 0);
+        occ = b > 0 ? b : 1;
+    }
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return (unsigned)(sms * occ);
 }
 
 // Counting sort of the live paths by key.  Keys beyond kSmemKeys bins fall
@@ -349,6 +429,7 @@ __global__ void kWfAdvance(uint32_t* __restrict__ counts, uint32_t* __restrict__
     if (threadIdx.x == 0) {
         counts[0] = counts[1];
         counts[1] = 0;
+        counts[2] = 0;
     }
 }
 
@@ -455,6 +536,7 @@ __global__ void kWfStart(uint32_t* __restrict__ counts, uint32_t* __restrict__ h
     if (threadIdx.x == 0) {
         counts[0] = 0;
         counts[1] = 0;
+        counts[2] = 0;
     }
 }
 
@@ -483,7 +565,8 @@ int runWave(const Src& src, const Mode& mode, WfBuffers* b, uint64_t base, uint3
     uint32_t* live = b->qa;
     uint32_t* nextQ = b->qb;
     for (uint32_t depth = 0; depth < maxDepth; depth++) {
-        kWfExtend<Src><<<blocks(n), kWfThreads, 0, stream>>>(src, st, live, b->counts, b->keys);
+        kWfExtend<Src><<<std::min(blocks(n), wfExtendBlocks<Src>()), kWfThreads, 0, stream>>>(src, st, live,
+                                                                                              b->counts, b->keys);
         CR_LAUNCH_CHECK();
         kWfHistogram<<<blocks(n), kWfThreads, 0, stream>>>(b->keys, b->counts, nKeys, b->hist);
         CR_LAUNCH_CHECK();

@@ -342,6 +342,11 @@ int cr_render_ray_count(cr_scene* scene, uint64_t* rays);
  * pipelined with the traversal. */
 int cr_trace_closest(cr_scene* scene, const cr_ray* rays, uint64_t n,
                      cr_hit* hits);
+/* The same on device buffers, ordered on `stream` (NULL = the default
+ * stream) and returning without waiting.  Each call takes an 8-byte
+ * stream-ordered allocation (cudaMallocAsync / cudaFreeAsync on `stream`)
+ * for its ray counter, so concurrent calls on different streams are
+ * independent and the call can be captured in a CUDA graph. */
 int cr_trace_closest_device(cr_scene* scene, const cr_ray* rays, uint64_t n,
                             cr_hit* hits, void* stream);
 

@@ -154,3 +154,46 @@ def test_full_size_ray_cast(gpu_lib):
     gh = g.trace_closest(rays)
     oh, ties = o.trace_closest(rays)
     assert_same_hits(gh, oh, ties)
+
+
+@pytest.mark.parametrize("n", [1, 31, 33, 1000, 123457])
+def test_dynamic_fetch_sizes(gpu_lib, n):
+    """The persistent ray cast hands rays to lanes as they free up; every
+    batch size (partial warps, fewer rays than lanes, many rays per block)
+    gives the oracle's hits, and the occlusion answers too."""
+    g, o = both(scenes.random_triangle_scene(30000, seed=40))
+    rays = scenes.random_rays(n, seed=41)
+    gh = g.trace_closest(rays)
+    oh, ties = o.trace_closest(rays)
+    assert_same_hits(gh, oh, ties)
+    rays["tmax"] = np.float32(1.5)
+    assert np.array_equal(g.trace_occluded(rays), o.trace_occluded(rays))
+
+
+def test_concurrent_streams_and_graph_capture(gpu_lib):
+    """Device-buffer queries on two streams at once (each call has its own
+    stream-ordered ray counter), and one captured in a CUDA graph and
+    replayed, give the host entry point's hits."""
+    import torch
+    g, _ = both(scenes.random_triangle_scene(50000, seed=42))
+    ra, rb = scenes.random_rays(300000, seed=43), scenes.random_rays(200000, seed=44)
+    ha, hb = g.trace_closest(ra), g.trace_closest(rb)
+    dra = torch.from_numpy(ra.view(np.uint8)).cuda()
+    drb = torch.from_numpy(rb.view(np.uint8)).cuda()
+    dha = torch.zeros(len(ra) * 16, dtype=torch.uint8, device="cuda")
+    dhb = torch.zeros(len(rb) * 16, dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+    for _ in range(3):
+        g.trace_closest_device(dra.data_ptr(), len(ra), dha.data_ptr(), s1.cuda_stream)
+        g.trace_closest_device(drb.data_ptr(), len(rb), dhb.data_ptr(), s2.cuda_stream)
+    torch.cuda.synchronize()
+    assert np.array_equal(dha.cpu().numpy().view(np.uint32), ha.view(np.uint32))
+    assert np.array_equal(dhb.cpu().numpy().view(np.uint32), hb.view(np.uint32))
+    dha.zero_()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        g.trace_closest_device(dra.data_ptr(), len(ra), dha.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    graph.replay()
+    torch.cuda.synchronize()
+    assert np.array_equal(dha.cpu().numpy().view(np.uint32), ha.view(np.uint32))
