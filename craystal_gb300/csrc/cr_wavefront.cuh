@@ -121,7 +121,7 @@ __device__ __forceinline__ void addRays(unsigned long long* counter, uint32_t ra
 //
 // One scene: path g is pixel g mod (w h) at sample p.first + g / (w h).
 struct OneScene {
-    static constexpr int kShadeMinBlocks = 4;  // 128 registers
+    static constexpr int kShadeMinBlocks = 5;  // 96 registers: spills a little, 2 % faster than 4 blocks of 128
     SceneView view;
     CameraGpu cam;
     Params p;
