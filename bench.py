@@ -809,7 +809,7 @@ def run_ours(args):
         traffic = traffic_from_profile()
         out["roofline"] = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                            "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": src,
-                           "kernel": "kTrace<closest>", "kernel_ms": round(kernel_ms, 4),
+                           "kernel": "kTraceDyn<closest>", "kernel_ms": round(kernel_ms, 4),
                            "bytes_per_ray": round(bpr, 1),
                            "per_ray": {k: round(v, 2) for k, v in per.items()},
                            "note": f"of {src}; per-ray counts from the oracle on 262144 rays"}
