@@ -20,7 +20,7 @@
 //   4. train_steps Adam steps on the frame's training records.
 // The cache learns L_o(x, w_o) of the reference estimator itself, so a
 // perfect cache makes the cached image unbiased with respect to the plain
-// one; the plain tracer's image is the judge of its error.
+// one; its error is measured against the plain tracer's image.
 
 #include <cstring>
 

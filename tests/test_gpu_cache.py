@@ -1,5 +1,5 @@
 """The radiance-cache integrator (cr_render_cached) against the plain path
-tracer, which is the judge of its error.
+tracer, the measure of its error.
 
 - With every pixel a training path the cached integrator traces exactly the
   plain tracer's paths: equal films (float-atomic summation order aside).
