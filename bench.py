@@ -766,7 +766,7 @@ def run_ours(args):
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         check(lib.cr_trace_closest(sc.handle, rp, N_RAYS, hp))
-    e2e_s = time.perf_counter() - t0
+    e2e_s = slowest_rank_ms((time.perf_counter() - t0) * 1e3, world, f"cuda:{local}") * 1e-3
     e2e = N_RAYS * e2e_steps * world / e2e_s / 1e6
     # the host-path result is the device-path result
     hits_host = pin_h.numpy().view(cg.HIT_DTYPE)
@@ -778,7 +778,9 @@ def run_ours(args):
                      "device_mib": round(st["device_bytes"] / 2 ** 20, 1)},
              "host_path_matches_device_path": same,
              "hit_fraction": round(float((hits_dev["prim"] != cg.CR_MISS).mean()), 4)}
-    if not args.skip_extra:
+    # the extras are single-GPU configurations (and time the CPU oracle on the
+    # host's cores): a replica run under torchrun measures the ray cast only
+    if not args.skip_extra and world == 1:
         extra["restated_reference_kernel"] = restated_reference_extra(torch, sc, flatten_scene(data), d_rays, N_RAYS,
                                                                       d_hits)
         extra["path_tracer"] = cornell_extra(torch)
