@@ -521,7 +521,7 @@ class BatchRenderer:
 
     def set_tuning(self, tile=16, spp_per_item=4, blocks_per_sm=0, wave_log2=0):
         """wave_log2 = 0: the persistent megakernel with (tile, spp_per_item,
-        blocks_per_sm); 16..23: the wavefront in waves of 2^wave_log2 paths."""
+        blocks_per_sm); 16..25: the wavefront in waves of 2^wave_log2 paths."""
         from ._lib import CrBatchTuning
         t = CrBatchTuning(tile, spp_per_item, blocks_per_sm, wave_log2)
         check(load().cr_batch_set_tuning(self._h, ctypes.byref(t)))

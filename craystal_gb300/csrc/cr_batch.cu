@@ -106,6 +106,16 @@ int blocksPerSm(int tw, int* out) {
     return CR_OK;
 }
 
+// On the wavefront schedule a scene with at least one whole wave of paths
+// renders on its own single-scene wavefront (waves of up to kWaveCap paths,
+// cr_render's form), and only the smaller scenes share the captured
+// many-scene waves: sharing a wave pays only for scenes smaller than one.
+bool ownWaves(const cr_batch* b, size_t i) {
+    const cr_scene* s = b->scenes[i];
+    return b->tuning.wave_log2 &&
+           (uint64_t)s->cam.width * s->cam.height * b->items[i].spp >= (1ull << b->tuning.wave_log2);
+}
+
 // Descriptors (re-uploaded on every render, so that sample indices can
 // advance between replays) and the work list plus graph (rebuilt when the
 // tuning changes).
@@ -152,7 +162,8 @@ int uploadDescriptors(cr_batch* b, cudaStream_t st) {
             w[i].pathBase = path;
             w[i].keyBase = key;
             w[i].nMats = s->nMats;
-            path += (uint64_t)s->cam.width * s->cam.height * b->items[i].spp;
+            // a scene on its own waves holds an empty range of the shared sequence
+            if (!ownWaves(b, i)) path += (uint64_t)s->cam.width * s->cam.height * b->items[i].spp;
             key += s->nMats + 2;
         }
         CR_CUDA(cudaMemcpyAsync(b->dWf, w.data(), w.size() * sizeof(WfScene), cudaMemcpyHostToDevice, st));
@@ -167,19 +178,25 @@ int buildWavefront(cr_batch* b, cudaStream_t st) {
     uint32_t keys = 0, maxDepth = 0;
     for (size_t i = 0; i < b->scenes.size(); i++) {
         const cr_scene* s = b->scenes[i];
-        total += (uint64_t)s->cam.width * s->cam.height * b->items[i].spp;
         keys += s->nMats + 2;
+        if (ownWaves(b, i)) continue;
+        total += (uint64_t)s->cam.width * s->cam.height * b->items[i].spp;
         maxDepth = std::max(maxDepth, b->items[i].config.max_depth);
     }
-    const uint32_t cap = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(total, 1), 1ull << b->tuning.wave_log2);
-    WfBuffers* wb = nullptr;
-    int rc = ensureWavefrontBuffers(b->wfBuffers, cap, keys, wb);
-    if (rc) return rc;
     if (!b->dWf) CR_CUDA(cudaMalloc(&b->dWf, b->scenes.size() * sizeof(WfScene)));
     if (!b->dWaveBase) CR_CUDA(cudaMalloc(&b->dWaveBase, sizeof(uint64_t)));
     b->wfTotal = total;
     b->wfKeys = keys;
     b->wfMaxDepth = maxDepth;
+    if (total == 0) {  // every scene renders on its own waves
+        b->wfWaves = 0;
+        b->built = true;
+        return CR_OK;
+    }
+    const uint32_t cap = (uint32_t)std::min<uint64_t>(total, 1ull << b->tuning.wave_log2);
+    WfBuffers* wb = nullptr;
+    int rc = ensureWavefrontBuffers(b->wfBuffers, cap, keys, wb);
+    if (rc) return rc;
     b->wfWaves = (uint32_t)((total + cap - 1) / cap);
     const ManyScenes src{b->dWf, (uint32_t)b->scenes.size()};
     CR_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
@@ -246,9 +263,18 @@ int renderOnce(cr_batch* b, cudaStream_t st) {
     int rc = uploadDescriptors(b, st);
     if (rc) return rc;
     if (b->tuning.wave_log2) {
-        CR_CUDA(cudaMemsetAsync(b->dWaveBase, 0, sizeof(uint64_t), st));
-        for (uint32_t w = 0; w < b->wfWaves; w++) CR_CUDA(cudaGraphLaunch(b->exec, st));
-        countLaunch(b->wfWaves);
+        if (b->wfWaves) {
+            CR_CUDA(cudaMemsetAsync(b->dWaveBase, 0, sizeof(uint64_t), st));
+            for (uint32_t w = 0; w < b->wfWaves; w++) CR_CUDA(cudaGraphLaunch(b->exec, st));
+            countLaunch(b->wfWaves);
+        }
+        for (size_t i = 0; i < b->scenes.size(); i++) {
+            if (!ownWaves(b, i)) continue;
+            const cr_batch_item& it = b->items[i];
+            rc = renderWavefront(b->scenes[i], &it.config, it.spp, it.first_sample + (uint32_t)(b->replays * it.spp),
+                                 st);
+            if (rc) return rc;
+        }
     } else {
         CR_CUDA(cudaGraphLaunch(b->exec, st));
         countLaunch();
@@ -304,8 +330,8 @@ int cr_batch_destroy(cr_batch* b) {
 int cr_batch_set_tuning(cr_batch* b, const cr_batch_tuning* t) {
     clearError();
     if (!b || !t) return fail(CR_ERR_INVALID_ARGUMENT, "NULL argument");
-    if (t->wave_log2 && (t->wave_log2 < 16 || t->wave_log2 > 23))
-        return fail(CR_ERR_INVALID_ARGUMENT, "wave_log2 must be 0 or 16..23");
+    if (t->wave_log2 && (t->wave_log2 < 16 || t->wave_log2 > 25))
+        return fail(CR_ERR_INVALID_ARGUMENT, "wave_log2 must be 0 or 16..25");
     if (!t->wave_log2 && t->tile != 8 && t->tile != 16) return fail(CR_ERR_INVALID_ARGUMENT, "tile must be 8 or 16");
     if (!t->wave_log2 && t->spp_per_item == 0) return fail(CR_ERR_INVALID_ARGUMENT, "spp_per_item must be positive");
     b->tuning = *t;
@@ -339,7 +365,7 @@ int cr_batch_autotune(cr_batch* b, cr_batch_tuning* best, cr_batch_tuning_result
     std::vector<cr_batch_tuning> cands;
     for (uint32_t tw : {8u, 16u})
         for (uint32_t r : {1u, 2u, 4u, 8u, 16u}) cands.push_back(cr_batch_tuning{tw, r, 0, 0});
-    for (uint32_t w : {19u, 20u, 21u, 22u}) cands.push_back(cr_batch_tuning{16, 4, 0, w});
+    for (uint32_t w : {20u, 22u, 23u, 24u, 25u}) cands.push_back(cr_batch_tuning{16, 4, 0, w});
     cudaEvent_t e0, e1;
     CR_CUDA(cudaEventCreate(&e0));
     CR_CUDA(cudaEventCreate(&e1));

@@ -404,10 +404,11 @@ int renderCached(cr_scene* s, const cr_integrator_config* cfg, const cr_cache_co
     if (rc) return rc;
     if (adaptive && b->teStart == te0 && b->teAdapted) cp.trainEvery = b->teAdapted;
     WfBuffers* wb = nullptr;
-    const uint32_t waveCap = (uint32_t)std::min<uint64_t>(px, kWaveCap);
+    uint32_t waveCap = 0;
     if (wavefront) {
-        rc = ensureWavefrontBuffers(s->wfBuffers, waveCap, s->nMats + 2, wb);
+        rc = ensureWavefrontWave(s->wfBuffers, px, s->nMats + 2, wb, waveCap);
         if (rc) return rc;
+        clearError();
     }
     Params p;
     p.maxDepth = cfg->max_depth;
@@ -429,8 +430,10 @@ int renderCached(cr_scene* s, const cr_integrator_config* cfg, const cr_cache_co
                                   b->recBeta, b->recBefore, b->counters + 2, slotCap, b->tIn, b->tTarget,
                                   b->counters + 1, b->samples};
             for (uint64_t base = 0; base < px; base += waveCap) {
+                // after the query vertex only training paths are live: one
+                // launch finishes them
                 rc = runWave(oneScene(s, p), mode, wb, base, (uint32_t)std::min<uint64_t>(waveCap, px - base),
-                             p.maxDepth, s->nMats + 2, st);
+                             p.maxDepth, s->nMats + 2, st, nullptr, 0, cp.queryVertex + 1);
                 if (rc) return rc;
             }
         } else {

@@ -26,10 +26,11 @@ int renderWavefront(cr_scene* s, const cr_integrator_config* cfg, uint32_t spp, 
     p.spectral = (cfg->flags & CR_RENDER_SPECTRAL) ? 1u : 0u;
     p.wb = whiteBalance();
     const uint64_t total = (uint64_t)s->cam.width * s->cam.height * spp;
-    const uint32_t cap = (uint32_t)std::min<uint64_t>(total, kWaveCap);
     WfBuffers* b = nullptr;
-    int rc = ensureWavefrontBuffers(s->wfBuffers, cap, s->nMats + 2, b);
+    uint32_t cap = 0;
+    int rc = ensureWavefrontWave(s->wfBuffers, total, s->nMats + 2, b, cap);
     if (rc) return rc;
+    clearError();
     const OneScene src = oneScene(s, p);
     for (uint64_t base = 0; base < total; base += cap) {
         rc = runWave(src, PlainMode{}, b, base, (uint32_t)std::min<uint64_t>(cap, total - base), p.maxDepth,

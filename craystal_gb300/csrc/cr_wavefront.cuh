@@ -22,7 +22,7 @@
 //   hit   (prim, t, u, v) of the extend stage
 //   aux   per-path state of the Mode's hooks
 // Paths run in waves of at most kWaveCap (the whole image x spp when it
-// fits), 128 bytes each.  Every stage reads the live-path count from device
+// fits), 132 bytes each.  Every stage reads the live-path count from device
 // memory, so a render is a fixed sequence of launches on one stream: no
 // host synchronisation, and it can be captured into a CUDA graph.
 
@@ -91,8 +91,28 @@ inline int ensureWavefrontBuffers(void*& slot, uint32_t cap, uint32_t nKeys, WfB
 namespace {
 
 
-constexpr uint32_t kWaveCap = 1u << 21;
+// Waves of up to 2^25 paths (4.4 GB of path state).  Every wave ends with a
+// tail of bounces in which few paths are left and most SMs idle, so fewer,
+// larger waves render faster: on GB300, 2^21 / 2^23 / 2^25-path waves take
+// 0.42 / 0.24 / 0.20 s for 1920x1080 at 64 spp (depth 16) and 2.19 / 1.19 /
+// 0.83 s for 3840x2160 at 32 spp.  A render whose path state cannot be
+// allocated halves its wave, down to kWaveCapMin.
+constexpr uint32_t kWaveCap = 1u << 25;
+constexpr uint32_t kWaveCapMin = 1u << 20;
 constexpr int kWfThreads = 128;
+
+// Path state for waves of up to `want` paths, halving the wave while the
+// allocation fails; cap receives the wave size in use.
+inline int ensureWavefrontWave(void*& slot, uint64_t want, uint32_t nKeys, WfBuffers*& out, uint32_t& cap) {
+    cap = (uint32_t)std::min<uint64_t>(want, kWaveCap);
+    while (true) {
+        const int rc = ensureWavefrontBuffers(slot, cap, nKeys, out);
+        if (rc != CR_ERR_OUT_OF_MEMORY || cap <= kWaveCapMin) return rc;
+        (void)cudaGetLastError();  // a failed allocation leaves no sticky error
+        static_cast<WfBuffers*>(slot)->release();
+        cap /= 2;
+    }
+}
 
 struct WfState {
     float4* ro;
@@ -536,6 +556,45 @@ __global__ void __launch_bounds__(kWfThreads) kWfEndUntraced(const __grid_consta
     }
 }
 
+// The remaining bounces of every live path in one launch, from bounce
+// depth0 on: closest() and shadeBounce() in a loop per path, the
+// megakernel's form resumed from the wave's path state.  The cached
+// integrator uses it once only its training paths (one pixel in hundreds)
+// are left: a wavefront bounce per remaining depth would cost six launches
+// for a few thousand paths each.  The same operations in the same order as
+// the bounce-by-bounce form, so the results are those of kWfShade.
+template <class Src, class Mode>
+__global__ void __launch_bounds__(kWfThreads) kWfFinish(const __grid_constant__ Src src, WfState st,
+                                                        const __grid_constant__ Mode mode,
+                                                        const uint32_t* __restrict__ queue,
+                                                        const uint32_t* __restrict__ count, uint32_t depth0) {
+    const uint32_t n = *count;
+    if (blockIdx.x * blockDim.x >= n) return;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t item = 0, rays = 0;
+    if (i < n) {
+        const uint32_t k = queue[i];
+        item = st.item[k];
+        const Params& p = src.paramsOf(item);
+        PathCtx c{src.sceneOf(item), 0u, SpectralPath{}};
+        const uint4 meta = st.meta[k];
+        c.spec = makeSpectralPath(p.spectral != 0, meta.x, meta.y, meta.z);
+        Sampler smp = Sampler::resume(meta.w, st.inc[k]);
+        const float4 o = st.ro[k], d = st.rd[k], b = st.beta[k], r = st.rad[k];
+        float3 ro = mk3(o.x, o.y, o.z), rd = mk3(d.x, d.y, d.z);
+        Spec beta = sp(b.x, b.y, b.z), radiance = sp(r.x, r.y, r.z);
+        typename Mode::Hooks hk = mode.hooks(st, k, meta);
+        for (uint32_t depth = depth0; depth < p.maxDepth; depth++) {
+            THit h;
+            closest(c, ro, rd, h);
+            if (!shadeBounce<typename Mode::Hooks, true>(c, p, smp, depth, h, ro, rd, beta, radiance, hk)) break;
+        }
+        mode.end(src, item, st, k, meta, c, radiance, make_float2(o.w, d.w), hk);
+        rays = c.rays;
+    }
+    addRays(src.raysOf(item), rays);
+}
+
 __global__ void kWfNextWave(uint64_t* __restrict__ waveBase, uint32_t cap) { *waveBase += cap; }
 
 __global__ void kWfStart(uint32_t* __restrict__ counts, uint32_t* __restrict__ hist, uint32_t nKeys) {
@@ -557,9 +616,13 @@ inline unsigned blocks(uint64_t n) { return (unsigned)((n + kWfThreads - 1) / kW
 // With waveBase set (device memory), the wave starts at *waveBase, holds
 // min(n, total - *waveBase) paths and advances *waveBase by n at its end, so
 // that the same launch sequence (a captured graph) replays wave after wave.
+//
+// finishFrom < maxDepth: the bounces from finishFrom on run as one kWfFinish
+// launch over the paths still live then.
 template <class Src, class Mode>
 int runWave(const Src& src, const Mode& mode, WfBuffers* b, uint64_t base, uint32_t n, uint32_t maxDepth,
-            uint32_t nKeys, cudaStream_t stream, uint64_t* waveBase = nullptr, uint64_t total = 0) {
+            uint32_t nKeys, cudaStream_t stream, uint64_t* waveBase = nullptr, uint64_t total = 0,
+            uint32_t finishFrom = 0xffffffffu) {
     const WfState st{b->ro, b->rd, b->beta, b->rad, b->meta, b->inc, b->hit, b->aux, b->item};
     kWfInit<Src><<<blocks(n), kWfThreads, 0, stream>>>(src, st, base, n, waveBase, total);
     CR_LAUNCH_CHECK();
@@ -571,7 +634,8 @@ int runWave(const Src& src, const Mode& mode, WfBuffers* b, uint64_t base, uint3
     CR_LAUNCH_CHECK();
     uint32_t* live = b->qa;
     uint32_t* nextQ = b->qb;
-    for (uint32_t depth = 0; depth < maxDepth; depth++) {
+    const uint32_t bounces = std::min(maxDepth, finishFrom);
+    for (uint32_t depth = 0; depth < bounces; depth++) {
         kWfExtend<Src><<<std::min(blocks(n), wfExtendBlocks<Src>()), kWfThreads, 0, stream>>>(src, st, live,
                                                                                               b->counts, b->keys);
         CR_LAUNCH_CHECK();
@@ -587,6 +651,10 @@ int runWave(const Src& src, const Mode& mode, WfBuffers* b, uint64_t base, uint3
         kWfAdvance<<<1, 256, 0, stream>>>(b->counts, b->hist, nKeys);
         CR_LAUNCH_CHECK();
         std::swap(live, nextQ);
+    }
+    if (bounces < maxDepth) {
+        kWfFinish<Src, Mode><<<blocks(n), kWfThreads, 0, stream>>>(src, st, mode, live, b->counts, bounces);
+        CR_LAUNCH_CHECK();
     }
     if (waveBase) {
         kWfNextWave<<<1, 1, 0, stream>>>(waveBase, n);

@@ -476,7 +476,7 @@ int cr_render_cached(cr_scene* scene, const cr_integrator_config* cfg,
  *   - persistent megakernel (wave_log2 = 0): one persistent launch whose
  *     blocks take work items (scene, pixel tile, run of spp_per_item sample
  *     indices) from one queue, largest scenes first;
- *   - wavefront (wave_log2 = 16..23): the paths of all scenes form one
+ *   - wavefront (wave_log2 = 16..25): the paths of all scenes form one
  *     sequence, rendered in waves of 2^wave_log2 paths; every bounce sorts
  *     the live paths by (scene, material), so a wave mixes scenes and the
  *     small ones fill the GPU beside the large ones.  One captured graph of
@@ -497,7 +497,7 @@ typedef struct {
     uint32_t tile;          /* persistent: 8 or 16 pixels square */
     uint32_t spp_per_item;  /* persistent: sample indices per work item */
     uint32_t blocks_per_sm; /* persistent: 0 = as many as fit */
-    uint32_t wave_log2;     /* 0 = persistent megakernel; 16..23 = wavefront waves of 2^wave_log2 paths */
+    uint32_t wave_log2;     /* 0 = persistent megakernel; 16..25 = wavefront waves of 2^wave_log2 paths */
 } cr_batch_tuning;
 typedef struct {
     cr_batch_tuning tuning;

@@ -63,7 +63,7 @@ def test_autotune_times_every_tuning_and_clears(gpu_lib, tmp_path):
     params, scs, integs = make_batch(4)
     b = BatchRenderer(scs, integs, [p["spp"] for p in params])
     out = b.autotune(json_path=str(tmp_path / "tuning.json"))
-    assert len(out["timings_ms"]) == 14
+    assert len(out["timings_ms"]) == 15
     best = min(out["timings_ms"], key=lambda r: r["ms"])
     assert out["best"] == {"tile": best["tile"], "spp_per_item": best["spp_per_item"], "wave_log2": best["wave_log2"]}
     assert b.tuning()["wave_log2"] == best["wave_log2"]

@@ -52,10 +52,10 @@ def test_wavefront_spheres_textures_environment(gpu_lib):
 
 
 def test_wavefront_several_waves_and_depth_zero(gpu_lib):
-    data, cam = scenes.cornell_box(seed=7, width=512, height=512)
+    data, cam = scenes.cornell_box(seed=7, width=2048, height=2048)
     sc = Scene(data)
     sc.setCamera(cam)
-    compare(sc, spp=9)  # 2.36 M paths: two waves
+    compare(sc, spp=9)  # 37.7 M paths: two waves of at most 2^25
     rgb, w, rays = compare(sc, depth=0, spp=2)
     assert rays == 0 and w.sum() > 0 and not rgb.any()
 
