@@ -168,10 +168,10 @@ __global__ void __launch_bounds__(256) kRenderCached(const SceneView sc, const C
 
 // SensorData::addSample (Core/Sensor.cu:19-43) of each pixel's final sample.
 __global__ void kSplatCached(const SampleRec* __restrict__ samples, const float* __restrict__ qBeta,
-                             const float* __restrict__ qOut, uint32_t W, uint32_t H, float* __restrict__ filmRgb,
-                             float* __restrict__ filmW) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= W * H) return;
+                             const float* __restrict__ qOut, uint64_t count, uint32_t W, uint32_t H,
+                             float* __restrict__ filmRgb, float* __restrict__ filmW) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
     const SampleRec s = samples[i];
     Spec L = sp(s.a.x, s.a.y, s.a.z);
     const uint32_t q = __float_as_uint(s.b.y);
@@ -218,7 +218,9 @@ struct WfCacheHooks {
 struct CachedMode {
     using Hooks = WfCacheHooks;
     CacheParams cp;
-    uint32_t width;
+    uint32_t width, height;
+    uint32_t first;    // sample index of the wave's first frame
+
     float* qIn;
     float* qBeta;
     uint32_t* qCount;
@@ -245,7 +247,7 @@ struct CachedMode {
         SampleRec rec;
         rec.a = make_float4(L.r, L.g, L.b, pix.x);
         rec.b = make_float4(pix.y, __uint_as_float(h.q), 0.0f, 0.0f);
-        samples[(size_t)meta.y * width + meta.x] = rec;
+        samples[((size_t)(meta.z - first) * height + meta.y) * width + meta.x] = rec;
         if (!h.train || h.slot >= slotCap) return;
         const size_t r0 = (size_t)h.slot * kMaxRecords;
         for (uint32_t r = 0; r < h.nRec; r++) {
@@ -305,6 +307,7 @@ __device__ __forceinline__ bool WfCacheHooks::atVertex(uint32_t depth, const Ise
 // Per-scene buffers of the cached integrator (sized for the film).
 struct CacheBuffers {
     uint64_t pixels = 0;
+    uint32_t frames = 0;  // frames per wave the per-path buffers hold
     uint32_t trainCap = 0;
     SampleRec* samples = nullptr;
     float* qIn = nullptr;
@@ -335,23 +338,28 @@ void freeCacheBuffers(void* p) {
 
 namespace {
 
-int ensureCacheBuffers(cr_scene* s, uint32_t trainCap, uint32_t slotCap, CacheBuffers** out) {
+// frames: frames per wave; the sample and query buffers hold px x frames
+// entries, the training buffers trainCap records (all frames of a wave).
+int ensureCacheBuffers(cr_scene* s, uint32_t frames, uint32_t trainCap, uint32_t slotCap, CacheBuffers** out) {
     const uint64_t px = (uint64_t)s->cam.width * s->cam.height;
     CacheBuffers* b = static_cast<CacheBuffers*>(s->cacheBuffers);
-    if (b && b->pixels == px && b->trainCap >= trainCap && b->slotCap >= slotCap) {
+    if (b && b->pixels == px && b->frames >= frames && b->trainCap >= trainCap && b->slotCap >= slotCap) {
         *out = b;
         return CR_OK;
     }
+    CR_CUDA(cudaDeviceSynchronize());  // earlier renders may still use the old buffers
     freeCacheBuffers(b);
     s->cacheBuffers = nullptr;
     b = new CacheBuffers();
     s->cacheBuffers = b;
     b->pixels = px;
+    b->frames = frames;
     b->trainCap = trainCap;
-    CR_CUDA(cudaMalloc(&b->samples, px * sizeof(SampleRec)));
-    CR_CUDA(cudaMalloc(&b->qIn, px * kMlpInputs * sizeof(float)));
-    CR_CUDA(cudaMalloc(&b->qBeta, px * 3 * sizeof(float)));
-    CR_CUDA(cudaMalloc(&b->qOut, px * 3 * sizeof(float)));
+    const uint64_t n = px * frames;
+    CR_CUDA(cudaMalloc(&b->samples, n * sizeof(SampleRec)));
+    CR_CUDA(cudaMalloc(&b->qIn, n * kMlpInputs * sizeof(float)));
+    CR_CUDA(cudaMalloc(&b->qBeta, n * 3 * sizeof(float)));
+    CR_CUDA(cudaMalloc(&b->qOut, n * 3 * sizeof(float)));
     CR_CUDA(cudaMalloc(&b->tIn, (size_t)trainCap * kMlpInputs * sizeof(float)));
     CR_CUDA(cudaMalloc(&b->tTarget, (size_t)trainCap * 3 * sizeof(float)));
     CR_CUDA(cudaMalloc(&b->counters, 3 * sizeof(uint32_t)));
@@ -398,18 +406,29 @@ int renderCached(cr_scene* s, const cr_integrator_config* cfg, const cr_cache_co
     // training paths of a frame: px / trainEvery on average (the hash picks
     // them); room for four times that at the smallest spacing, beyond which a
     // path keeps no records
-    const uint32_t slotCap = wavefront ? (uint32_t)std::min<uint64_t>(px, 4 * (px / teMin) + 4096) : 0u;
-    CacheBuffers* b = nullptr;
-    int rc = ensureCacheBuffers(s, trainCap, slotCap, &b);
-    if (rc) return rc;
-    if (adaptive && b->teStart == te0 && b->teAdapted) cp.trainEvery = b->teAdapted;
+    //
+    // Frames per wave (wavefront form).  After the query vertex only the
+    // training paths are live, and kWfFinish runs their remaining bounces as
+    // one serial chain per path, which a frame alone would wait for; a wave
+    // of several frames waits for it once.  Up to 8 frames, or 2^23 paths.
+    // Each frame of a wave still gets its own Adam steps, on its share of the
+    // wave's records; the frames of a wave share the network they start with.
     WfBuffers* wb = nullptr;
     uint32_t waveCap = 0;
+    uint32_t F = 1;
     if (wavefront) {
-        rc = ensureWavefrontWave(s->wfBuffers, px, s->nMats + 2, wb, waveCap);
-        if (rc) return rc;
+        F = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(std::min<uint64_t>(8, frames), (1ull << 23) / px));
+        int rcw = ensureWavefrontWave(s->wfBuffers, px * F, s->nMats + 2, wb, waveCap);
+        if (rcw) return rcw;
         clearError();
+        F = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(F, waveCap / px));
     }
+    const uint32_t slotCap =
+        wavefront ? (uint32_t)std::min<uint64_t>(px * F, 4 * (px * F / teMin) + 4096) : 0u;
+    CacheBuffers* b = nullptr;
+    int rc = ensureCacheBuffers(s, F, trainCap * F, slotCap, &b);
+    if (rc) return rc;
+    if (adaptive && b->teStart == te0 && b->teAdapted) cp.trainEvery = b->teAdapted;
     Params p;
     p.maxDepth = cfg->max_depth;
     p.rrThreshold = cfg->rr_threshold;
@@ -422,17 +441,22 @@ int renderCached(cr_scene* s, const cr_integrator_config* cfg, const cr_cache_co
     dim3 grid((W + 15) / 16, (H + 15) / 16), block(16, 16);
     const uint32_t steps = cc->train_steps ? cc->train_steps : 1u;
     uint32_t lastTrain = 0;
-    for (uint32_t f = 0; f < frames; f++) {
+    for (uint32_t f = 0; f < frames;) {
+        const uint32_t fw = std::min(F, frames - f);  // frames in this wave
         p.first = first + f;
+        p.spp = fw;
+        cp.trainCap = trainCap * fw;
         CR_CUDA(cudaMemsetAsync(b->counters, 0, 3 * sizeof(uint32_t), st));
         if (wavefront) {
-            const CachedMode mode{cp,         W,         b->qIn,    b->qBeta,     b->counters, b->recIn,
-                                  b->recBeta, b->recBefore, b->counters + 2, slotCap, b->tIn, b->tTarget,
-                                  b->counters + 1, b->samples};
-            for (uint64_t base = 0; base < px; base += waveCap) {
+            const CachedMode mode{cp,          W,          H,         p.first,        b->qIn,
+                                  b->qBeta,    b->counters, b->recIn, b->recBeta,     b->recBefore,
+                                  b->counters + 2, slotCap, b->tIn,   b->tTarget,     b->counters + 1,
+                                  b->samples};
+            const uint64_t paths = px * fw;
+            for (uint64_t base = 0; base < paths; base += waveCap) {
                 // after the query vertex only training paths are live: one
                 // launch finishes them
-                rc = runWave(oneScene(s, p), mode, wb, base, (uint32_t)std::min<uint64_t>(waveCap, px - base),
+                rc = runWave(oneScene(s, p), mode, wb, base, (uint32_t)std::min<uint64_t>(waveCap, paths - base),
                              p.maxDepth, s->nMats + 2, st, nullptr, 0, cp.queryVertex + 1);
                 if (rc) return rc;
             }
@@ -444,10 +468,10 @@ int renderCached(cr_scene* s, const cr_integrator_config* cfg, const cr_cache_co
         uint32_t cnt[2];
         CR_CUDA(cudaMemcpyAsync(cnt, b->counters, sizeof(cnt), cudaMemcpyDeviceToHost, st));
         CR_CUDA(cudaStreamSynchronize(st));
-        const uint32_t nq = cnt[0], nt = std::min(cnt[1], trainCap);
+        const uint32_t nq = cnt[0], nt = std::min(cnt[1], trainCap * fw);
         const uint32_t teUsed = cp.trainEvery;
         if (adaptive) {
-            const double ratio = std::min(2.0, std::max(0.5, (double)cnt[1] / (double)trainCap));
+            const double ratio = std::min(2.0, std::max(0.5, (double)cnt[1] / ((double)trainCap * fw)));
             const double te = std::min((double)teMax, std::max((double)teMin, (double)cp.trainEvery * ratio));
             cp.trainEvery = (uint32_t)(te + 0.5);
             b->teStart = te0;
@@ -455,24 +479,32 @@ int renderCached(cr_scene* s, const cr_integrator_config* cfg, const cr_cache_co
         }
         rc = mlpInferDevice(mlp, b->qIn, nq, b->qOut, true, st);
         if (rc) return rc;
-        kSplatCached<<<(unsigned)((W * H + 255) / 256), 256, 0, st>>>(b->samples, b->qBeta, b->qOut, W, H,
-                                                                    s->filmRgb, s->filmW);
+        const uint64_t nSamples = px * fw;
+        kSplatCached<<<(unsigned)((nSamples + 255) / 256), 256, 0, st>>>(b->samples, b->qBeta, b->qOut, nSamples, W,
+                                                                       H, s->filmRgb, s->filmW);
         CR_LAUNCH_CHECK();
         if (nt > 0 && !cc->freeze) {
-            lastTrain = nt;
-            for (uint32_t k = 0; k < steps; k++) {
-                rc = mlpGradDevice(mlp, b->tIn, b->tTarget, nt, st);
-                if (rc) return rc;
-                rc = mlpAdamDevice(mlp, st);
-                if (rc) return rc;
+            // train_steps Adam steps per frame, each frame on its share of the
+            // wave's records
+            for (uint32_t k = 0; k < fw; k++) {
+                const uint32_t r0 = (uint32_t)((uint64_t)nt * k / fw), r1 = (uint32_t)((uint64_t)nt * (k + 1) / fw);
+                if (r1 <= r0) continue;
+                lastTrain = r1 - r0;
+                for (uint32_t j = 0; j < steps; j++) {
+                    rc = mlpGradDevice(mlp, b->tIn + (size_t)r0 * kMlpInputs, b->tTarget + (size_t)r0 * 3, r1 - r0, st);
+                    if (rc) return rc;
+                    rc = mlpAdamDevice(mlp, st);
+                    if (rc) return rc;
+                }
             }
         }
         if (stats) {
             stats->queries += nq;
             stats->train_records += nt;
-            stats->frames++;
+            stats->frames += fw;
             stats->last_train_every = teUsed;
         }
+        f += fw;
     }
     rc = mlpCheck(mlp);
     if (rc) return rc;
