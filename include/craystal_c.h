@@ -444,9 +444,12 @@ int cr_mlp_train_step_device(cr_mlp* mlp, const float* inputs, const float* targ
  * (a hash of pixel and sample index) traces its whole path with the plain
  * estimator, adds that unbiased sample to the film, and turns every vertex
  * v >= 1 into a training record (inputs at v, target = radiance gathered from
- * v on / throughput at v).  After each frame the network takes train_steps
+ * v on / throughput at v).  For each frame the network takes train_steps
  * Adam steps on at most train_samples records (none when freeze is set).
- * Frames use sample indices first_sample, first_sample + 1, ... */
+ * Frames use sample indices first_sample, first_sample + 1, ...  On the
+ * wavefront schedule (the default) up to 8 frames (2^23 paths) render as
+ * one wave, and the steps of its frames follow the wave, each frame's on its
+ * share of the wave's records. */
 typedef struct {
     uint32_t query_vertex;   /* 1 */
     uint32_t train_every;    /* 0 = adaptive: the spacing that yields about
