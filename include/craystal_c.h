@@ -479,17 +479,20 @@ int cr_render_cached(cr_scene* scene, const cr_integrator_config* cfg,
  *   - persistent megakernel (wave_log2 = 0): one persistent launch whose
  *     blocks take work items (scene, pixel tile, run of spp_per_item sample
  *     indices) from one queue, largest scenes first;
- *   - wavefront (wave_log2 = 16..25): the paths of all scenes form one
- *     sequence, rendered in waves of 2^wave_log2 paths; every bounce sorts
- *     the live paths by (scene, material), so a wave mixes scenes and the
- *     small ones fill the GPU beside the large ones.  One captured graph of
- *     a wave is replayed wave after wave.
+ *   - wavefront (wave_log2 = 16..25): the paths of all scenes with fewer
+ *     than 2^wave_log2 paths form one sequence, rendered in waves of
+ *     2^wave_log2 paths; every bounce sorts the live paths by (scene,
+ *     material), so a wave mixes scenes and the small ones fill the GPU
+ *     together.  One captured graph of a wave is replayed wave after wave.
+ *     A scene with at least one whole wave of paths renders on its own
+ *     single-scene wavefront, as cr_render does.
  * Each scene's film receives exactly the samples cr_render(scene, config,
  * spp, first_sample) would add; the k-th cr_batch_render of a batch uses
  * sample indices first_sample + k*spp.  cr_batch_autotune times every
- * (tile 8|16) x (spp_per_item 1,2,4,8,16) and every wave size 2^19..2^22
- * on the batch itself, keeps the fastest and clears the films it rendered
- * into.  The scenes must outlive the batch and keep their camera size. */
+ * (tile 8|16) x (spp_per_item 1,2,4,8,16) and the wave sizes 2^20 and
+ * 2^22..2^25 on the batch itself, keeps the fastest and clears the films it
+ * rendered into.  The scenes must outlive the batch and keep their camera
+ * size. */
 typedef struct cr_batch cr_batch;
 typedef struct {
     cr_integrator_config config;
