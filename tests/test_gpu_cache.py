@@ -67,6 +67,29 @@ def test_wavefront_form_equals_megakernel_form(gpu_lib, train_every):
     np.testing.assert_allclose(r1, r0, rtol=1e-4, atol=1e-5)
 
 
+def test_multi_frame_waves_equal_single_frames(gpu_lib):
+    """On the wavefront form up to 8 frames render as one wave (here 11
+    frames: a wave of 8 and one of 3).  With a frozen network that gives the
+    film, queries, records and rays of 11 single-frame calls."""
+    from craystal_gb300.api import RadianceCache
+    sc, cam = cornell(64)
+    cache = RadianceCache()
+    waves = CachedPathTraceIntegrator(CFG, train_every=4, cache=cache)
+    sc.film_clear()
+    waves.dispatch(sc, 11, first_sample=21, freeze=True)
+    a = (cam.sensor.data.copy(), cam.sensor.weight.copy(), sc.render_ray_count())
+    single = CachedPathTraceIntegrator(CFG, train_every=4, cache=cache)
+    sc.film_clear()
+    for k in range(11):
+        single.dispatch(sc, 1, first_sample=21 + k, freeze=True, readback=(k == 10))
+    b = (cam.sensor.data.copy(), cam.sensor.weight.copy(), sc.render_ray_count())
+    assert (waves.stats.frames, waves.stats.queries, waves.stats.train_records) == \
+        (single.stats.frames, single.stats.queries, single.stats.train_records)
+    assert a[2] == b[2]
+    np.testing.assert_allclose(a[1], b[1], rtol=1e-5)
+    np.testing.assert_allclose(a[0], b[0], rtol=1e-4, atol=1e-5)
+
+
 def test_cache_bookkeeping_and_finite(gpu_lib):
     sc, cam = cornell(128)
     integ = CachedPathTraceIntegrator(CFG, train_every=8)
