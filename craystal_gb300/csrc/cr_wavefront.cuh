@@ -91,13 +91,13 @@ inline int ensureWavefrontBuffers(void*& slot, uint32_t cap, uint32_t nKeys, WfB
 namespace {
 
 
-// Waves of up to 2^25 paths (4.4 GB of path state).  Every wave ends with a
+// Waves of up to 2^26 paths (8.8 GB of path state).  Every wave ends with a
 // tail of bounces in which few paths are left and most SMs idle, so fewer,
-// larger waves render faster: on GB300, 2^21 / 2^23 / 2^25-path waves take
-// 0.42 / 0.24 / 0.20 s for 1920x1080 at 64 spp (depth 16) and 2.19 / 1.19 /
-// 0.83 s for 3840x2160 at 32 spp.  A render whose path state cannot be
-// allocated halves its wave, down to kWaveCapMin.
-constexpr uint32_t kWaveCap = 1u << 25;
+// larger waves render faster: on GB300, 2^21 / 2^23 / 2^25 / 2^26-path waves
+// take 0.42 / 0.24 / 0.195 / 0.187 s for 1920x1080 at 64 spp (depth 16) and
+// 2.19 / 1.19 / 0.83 / 0.77 s for 3840x2160 at 32 spp.  A render whose path
+// state cannot be allocated halves its wave, down to kWaveCapMin.
+constexpr uint32_t kWaveCap = 1u << 26;
 constexpr uint32_t kWaveCapMin = 1u << 20;
 constexpr int kWfThreads = 128;
 
