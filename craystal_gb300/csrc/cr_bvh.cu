@@ -739,7 +739,8 @@ __global__ void kLeafFlags(const BuildNode* __restrict__ nodes, uint32_t n, uint
 }
 
 __device__ __forceinline__ uint32_t childRef(const BuildNode* nodes, const uint32_t* leafPrefix, uint32_t c) {
-    return nodes[c].info.z ? (kLeafBit | leafPrefix[c]) : (c - leafPrefix[c]);
+    const BuildNode& n = nodes[c];
+    return n.info.z ? leafRef(leafPrefix[c], n.info.x, n.info.y) : (c - leafPrefix[c]);
 }
 
 __global__ void kLayout(const BuildNode* __restrict__ nodes, uint32_t n, const uint32_t* __restrict__ leafPrefix,
@@ -999,6 +1000,8 @@ int buildGeneric(uint32_t N, Prep prep, BuiltBvh& out) {
     CR_CUDA(cub::DeviceScan::ExclusiveSum(scanTemp.p, scanBytes, isLeaf.p, leafPrefix.p, (int)nNodes));
     countLaunch(1);
     const uint32_t nLeaves = hc.leafCount;
+    if (nLeaves > ~(kLeafBit | kInlineLeafBit))  // leaf-table refs have 30 index bits
+        return fail(CR_ERR_UNSUPPORTED, "BVH has %u leaves; the limit is 2^30-1", nLeaves);
     const uint32_t nPairs = nNodes - nLeaves;
     DevBuf<NodePair> pairs;
     DevBuf<uint2> leaves;

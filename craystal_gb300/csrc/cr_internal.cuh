@@ -72,8 +72,9 @@ constexpr uint32_t kErrStackOverflow = 1u;
 //   p1 = (L.max.y, L.max.z, R.min.x, R.min.y)
 //   p2 = (R.min.z, R.max.x, R.max.y, R.max.z)
 //   ref = (L.ref, R.ref, flags, 0).  A child ref with bit 31 clear is the
-//         pair index of an interior child; with bit 31 set, bits 0-30 index
-//         the leaf table (first leaf slot, triangle count).  flags bits 0-2
+//         pair index of an interior child; with bit 31 set it is a leaf,
+//         whose slot range is in the ref itself or in the leaf table
+//         (kInlineLeafBit, below).  flags bits 0-2
 //         (left) and 3-5 (right) mark box axes thinner than FLT_EPSILON,
 //         which take the degenerate-slab branch of Math/AABB.cu:10-19.
 struct __align__(64) NodePair {
@@ -134,8 +135,23 @@ struct CameraGpu {
     uint32_t width, height;
 };
 
-// Everything a traversal or render kernel reads, passed by value.
+// Child refs.  Bit 31 clear: the pair index of an interior child.  Bit 31
+// set: a leaf.  A leaf of 1 to 7 slots that start below 2^27 carries its
+// range in the ref itself (bit 30 set, count in bits 27-29, first slot in
+// bits 0-26), so that opening it needs no load; any other leaf has bit 30
+// clear and bits 0-29 index the leaf table (first slot, count).
 constexpr uint32_t kLeafBit = 0x80000000u;
+constexpr uint32_t kInlineLeafBit = 0x40000000u;
+constexpr uint32_t kInlineSlotMask = (1u << 27) - 1u;
+constexpr uint32_t kInlineMaxCount = 7u;
+
+__host__ __device__ __forceinline__ uint32_t leafRef(uint32_t tableIndex, uint32_t first, uint32_t count) {
+    if (count >= 1u && count <= kInlineMaxCount && first <= kInlineSlotMask)
+        return kLeafBit | kInlineLeafBit | (count << 27) | first;
+    return kLeafBit | tableIndex;
+}
+
+// Everything a traversal or render kernel reads, passed by value.
 
 struct SceneView {
     const NodePair* pairs;

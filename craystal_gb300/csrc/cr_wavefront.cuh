@@ -344,7 +344,7 @@ __global__ void __launch_bounds__(kWfThreads) kWfExtend(const __grid_constant__ 
             if (active) {
                 const SceneView& sc = src.sceneOf(item);
                 const BvhView bv{sc.pairs, sc.leaves, sc.rootRef, sc.rootFlags, sc.rootMin, sc.rootMax, sc.hasRoot};
-                const TriLeaf<false> leaf{sc.leaves, sc.tris};
+                const TriLeaf<false> leaf{sc.tris};
                 if (!travStep<false>(cur, stack, bv, sc.errFlags, leaf, r, h)) {
                     finish();
                     active = false;
