@@ -83,6 +83,44 @@ def test_closest_hits_bit_exact(gpu_lib):
     assert_same_hits(gh, oh, ties)
 
 
+def _star_cluster(n, centre, rng):
+    """n triangles of random orientations and sizes that share one centroid:
+    no split separates them, so the builder makes one leaf of n.  Vertex
+    offsets are multiples of 2^-7, so ((v0 + v1) + v2) / 3 is the same float
+    for every triangle."""
+    a = rng.integers(-12, 13, (n, 3)).astype(np.float32) / 128.0
+    b = rng.integers(-12, 13, (n, 3)).astype(np.float32) / 128.0
+    c = np.asarray(centre, np.float32)
+    tri = np.stack([c + a, c + b, c - a - b], axis=1)
+    return tri.reshape(-1, 3).astype(np.float32)
+
+
+@pytest.mark.parametrize("with_others", [False, True])
+def test_closest_hits_large_leaves(gpu_lib, with_others):
+    """Leaves of more than 7 slots keep their range in the leaf table rather
+    than in the child ref: a 150-triangle leaf as the root, and the same leaf
+    below interior nodes among 3000 other triangles, hit bit-exactly."""
+    from craystal_gb300.api import MaterialData, MeshData, SceneData
+    rng = np.random.default_rng(31)
+    pos = _star_cluster(150, (0.5, 0.5, 0.5), rng)
+    if with_others:
+        pos = np.concatenate([pos, scenes.random_triangles(3000, seed=32)[0]]).astype(np.float32)
+    data = SceneData(meshes=[MeshData(position=pos, index=np.arange(len(pos), dtype=np.uint32))],
+                     materials=[MaterialData()])
+    g, o = both(data)
+    assert_same_tree(g, o)
+    st = g.bvh_stats()
+    assert st["max_leaf_size"] >= 150
+    assert (st["leaf_count"] == 1) == (not with_others)
+    rays = scenes.random_rays(200000, seed=33)
+    gh = g.trace_closest(rays)
+    oh, ties = o.trace_closest(rays)
+    cluster = (oh["prim"] != MISS) & (oh["prim"] < 150)
+    assert cluster.sum() > 1000
+    assert_same_hits(gh, oh, ties, max_tie_frac=1e-3)
+    assert np.array_equal(g.trace_occluded(rays), o.trace_occluded(rays))
+
+
 def test_device_and_host_entry_points_agree(gpu_lib):
     import torch
     g, _ = both(scenes.random_triangle_scene(20000, seed=23))
