@@ -1,6 +1,8 @@
 // cr_trace.cu -- batched closest-hit and occlusion queries
 // (SceneView::intersect / intersectOcclusion, Scene/Scene.cu:5-29).
 
+#include <cuda.h>
+
 #include "cr_internal.cuh"
 #include "cr_math.cuh"
 #include "cr_traverse.cuh"
@@ -188,10 +190,17 @@ namespace {
 
 constexpr uint64_t kChunk = 1ull << 21;  // rays per pipelined chunk (64 MiB of rays)
 
+int ensureStreams(cr_scene* s) {
+    for (int k = 0; k < 2; k++)
+        if (!s->streams[k]) CR_CUDA(cudaStreamCreateWithFlags(&s->streams[k], cudaStreamNonBlocking));
+    return CR_OK;
+}
+
 int ensureStaging(cr_scene* s) {
     if (s->stageCap) return CR_OK;
+    int rc = ensureStreams(s);
+    if (rc) return rc;
     for (int k = 0; k < 2; k++) {
-        CR_CUDA(cudaStreamCreateWithFlags(&s->streams[k], cudaStreamNonBlocking));
         CR_CUDA(cudaMalloc(&s->stageRays[k], kChunk * sizeof(cr_ray)));
         CR_CUDA(cudaMalloc(&s->stageHits[k], kChunk * sizeof(cr_hit)));
         CR_CUDA(cudaMalloc(&s->stageOcc[k], kChunk));
@@ -200,17 +209,83 @@ int ensureStaging(cr_scene* s) {
     return CR_OK;
 }
 
-// Host-buffer query: chunks alternate between two streams so that the
-// copy-in of one chunk overlaps the traversal and copy-out of the other.
+// cuPointerGetAttribute from the driver the runtime uses (no link to libcuda).
+typedef CUresult (*PointerAttributeFn)(void*, CUpointer_attribute, CUdeviceptr);
+
+PointerAttributeFn pointerAttributeFn() {
+    static const PointerAttributeFn fn = [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuPointerGetAttribute", &f, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            f = nullptr;
+        }
+        return reinterpret_cast<PointerAttributeFn>(f);
+    }();
+    return fn;
+}
+
+// The device address of host range [p, p + bytes) when the GPU can use it in
+// place: page-locked host memory (cudaHostAlloc, cudaHostRegister, a pinned
+// torch tensor) of the scene's device, mapped, with the whole range inside
+// one allocation.  Anything else (pageable memory, a range that runs past its
+// allocation, a driver that cannot say) gives nullptr and the staged path.
+void* mappedDevicePtr(const cr_scene* s, const void* p, size_t bytes) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type != cudaMemoryTypeHost || !a.devicePointer || a.device != s->device) return nullptr;
+    const PointerAttributeFn fn = pointerAttributeFn();
+    if (!fn) return nullptr;
+    unsigned long long start = 0, size = 0, mapped = 0;
+    const CUdeviceptr q = (CUdeviceptr)reinterpret_cast<uintptr_t>(p);
+    if (fn(&start, CU_POINTER_ATTRIBUTE_RANGE_START_ADDR, q) != CUDA_SUCCESS ||
+        fn(&size, CU_POINTER_ATTRIBUTE_RANGE_SIZE, q) != CUDA_SUCCESS ||
+        fn(&mapped, CU_POINTER_ATTRIBUTE_MAPPED, q) != CUDA_SUCCESS || !mapped)
+        return nullptr;
+    const uintptr_t lo = reinterpret_cast<uintptr_t>(p);
+    if (lo < start || bytes > size || lo - start > size - bytes) return nullptr;
+    return a.devicePointer;
+}
+
+// In-place query on mapped host buffers.  On GB300 the GPU reads the rays and
+// writes the results over NVLink-C2C as the traversal goes: 16M rays in
+// 13.97 ms against 13.87 ms on device buffers, where staging copies take
+// 14.96 ms.  false: the buffers do not qualify.
+template <bool kOcc>
+bool traceMapped(cr_scene* s, const cr_ray* rays, uint64_t n, void* out, int& rc) {
+    const cr_ray* dr = static_cast<const cr_ray*>(mappedDevicePtr(s, rays, n * sizeof(cr_ray)));
+    void* dout = mappedDevicePtr(s, out, n * (kOcc ? 1 : sizeof(cr_hit)));
+    if (!dr || !dout) return false;
+    if (reinterpret_cast<uintptr_t>(dr) & 15u) return false;
+    if (!kOcc && (reinterpret_cast<uintptr_t>(dout) & 15u)) return false;
+    rc = ensureStreams(s);
+    if (rc) return true;
+    cudaStream_t st = s->streams[0];
+    rc = kOcc ? traceOccludedDevice(s, dr, n, static_cast<uint8_t*>(dout), st)
+              : traceClosestDevice(s, dr, n, static_cast<cr_hit*>(dout), st);
+    return true;
+}
+
+// Host-buffer query.  Mapped host buffers are used in place (traceMapped);
+// otherwise chunks alternate between two streams so that the copy-in of one
+// chunk overlaps the traversal and copy-out of the other.
 template <bool kOcc>
 int traceHost(cr_scene* s, const cr_ray* rays, uint64_t n, void* out) {
     if (!s) return fail(CR_ERR_INVALID_ARGUMENT, "scene is NULL");
     if (n == 0) return CR_OK;
     if (!rays || !out) return fail(CR_ERR_INVALID_ARGUMENT, "rays / output is NULL");
     CR_CUDA(cudaSetDevice(s->device));
-    int rc = ensureStaging(s);
+    int rc = CR_OK;
+    const bool inPlace = traceMapped<kOcc>(s, rays, n, out, rc);
     if (rc) return rc;
-    for (uint64_t off = 0, k = 0; off < n; off += kChunk, k++) {
+    if (!inPlace) rc = ensureStaging(s);
+    if (rc) return rc;
+    for (uint64_t off = 0, k = 0; !inPlace && off < n; off += kChunk, k++) {
         const int b = (int)(k & 1);
         const uint64_t m = std::min(kChunk, n - off);
         cudaStream_t st = s->streams[b];

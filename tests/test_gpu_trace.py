@@ -135,6 +135,38 @@ def test_device_and_host_entry_points_agree(gpu_lib):
     assert np.array_equal(dev.view(np.uint32), host.view(np.uint32))
 
 
+def test_pinned_host_buffers_used_in_place(gpu_lib):
+    """Page-locked host buffers (a pinned torch tensor) are read and written
+    by the GPU in place; pageable ones go through staging copies.  Both give
+    the device path's hits and occlusion flags, also for a range that starts
+    inside its allocation and for a ray count that spans several chunks."""
+    import ctypes
+    import torch
+    from craystal_gb300._lib import check, load
+    lib = load()
+    g, o = both(scenes.random_triangle_scene(20000, seed=41))
+    n = (1 << 21) + 1000  # more than one 2^21-ray staging chunk
+    rays = scenes.random_rays(n, seed=42)
+    rays["tmax"][::3] = np.float32(1.5)
+    host = g.trace_closest(rays)  # pageable: staged
+    occ_host = g.trace_occluded(rays)
+    pin_r = torch.empty(n * 32 + 64, dtype=torch.uint8).pin_memory()
+    pin_h = torch.empty(n * 16 + 64, dtype=torch.uint8).pin_memory()
+    pin_o = torch.empty(n + 64, dtype=torch.uint8).pin_memory()
+    for off in (0, 32):  # 16-byte aligned starts inside the allocation
+        pin_r.numpy()[off:off + n * 32] = rays.view(np.uint8)
+        pin_h.zero_()
+        rp = ctypes.c_void_p(pin_r.data_ptr() + off)
+        check(lib.cr_trace_closest(g.handle, rp, n, ctypes.c_void_p(pin_h.data_ptr() + off)))
+        got = pin_h.numpy()[off:off + n * 16].copy().view(host.dtype)
+        assert np.array_equal(got.view(np.uint32), host.view(np.uint32))
+        pin_o.fill_(7)
+        check(lib.cr_trace_occluded(g.handle, rp, n, ctypes.c_void_p(pin_o.data_ptr() + off)))
+        assert np.array_equal(pin_o.numpy()[off:off + n], occ_host)
+    oh, ties = o.trace_closest(rays[:200000])
+    assert_same_hits(host[:200000], oh, ties)
+
+
 def test_occlusion_exact(gpu_lib):
     g, o = both(scenes.random_triangle_scene(50000, seed=25))
     rays = scenes.random_rays(300000, seed=26)
