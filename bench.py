@@ -753,7 +753,8 @@ def run_ours(args):
     value = N_RAYS * args.steps * world / (ms * 1e-3) / 1e6
     kernel_ms = ms / args.steps  # one launch per step
 
-    # e2e: host buffers through the C ABI, copies inside the timed region
+    # e2e: host buffers through the C ABI, host<->device transfers inside the timed region
+    # (pinned arrays: the library has the GPU read and write them in place)
     pin_r = torch.empty(N_RAYS * 32, dtype=torch.uint8).pin_memory()
     pin_r.numpy()[:] = rays.view(np.uint8)
     pin_h = torch.empty(N_RAYS * 16, dtype=torch.uint8).pin_memory()

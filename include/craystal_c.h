@@ -338,8 +338,13 @@ int cr_render_ray_count(cr_scene* scene, uint64_t* rays);
 /* SceneView::intersect (Scene/Scene.cu:5-14) on a batch of rays: closest
  * hit with the reference's traversal order (Core/BVH.cu:13-84) and
  * intersection arithmetic (Scene/Triangle.cu:40-75), so that prim, t, u and
- * v equal the reference's bit for bit.  Host arrays; copies in and out are
- * pipelined with the traversal. */
+ * v equal the reference's bit for bit.  Host arrays.  When both arrays lie
+ * in page-locked host memory of the scene's device (cudaHostAlloc,
+ * cudaHostRegister, a pinned torch tensor), each inside one mapped
+ * allocation and 16-byte aligned, the GPU reads the rays and writes the hits
+ * there in place (over NVLink-C2C on GB300); otherwise copies in and out go
+ * through device staging buffers, pipelined with the traversal.  The call
+ * returns when the hits are written.  cr_trace_occluded does the same. */
 int cr_trace_closest(cr_scene* scene, const cr_ray* rays, uint64_t n,
                      cr_hit* hits);
 /* The same on device buffers, ordered on `stream` (NULL = the default
