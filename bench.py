@@ -9,7 +9,8 @@ step = one closest-hit pass over the 16M rays.
   value : Mrays/s with rays and hits resident in HBM (cr_trace_closest_device),
           CUDA events on the launching stream.
   e2e   : Mrays/s through cr_trace_closest with pinned host buffers; every step
-          copies the 512 MiB of rays in and the 256 MiB of hits out.
+          moves the 512 MiB of rays in and the 256 MiB of hits out (the
+          library has the GPU read and write pinned arrays in place).
   roofline : algorithmic bytes per ray counted by the oracle on the
           reference BVH (32 B ray + 16 B hit + 24 B per child box tested +
           48 B per triangle tested + 4 B per leaf-map read) over the kernel's

@@ -106,11 +106,11 @@ __device__ __forceinline__ bool occluded(PathCtx& c, float3 o, float3 d, float t
 }
 
 // The shadow and MIS rays' queries, inline (kOutOfLine = false) or as calls
-// to one out-of-line copy.  The wavefront's shade stage calls them out of
-// line: its code then holds no traversal, and on GB300 that removes most
-// of its instruction-fetch stalls (1.6x faster shading on a small scene, no
-// loss on a traversal-heavy one); the megakernel, which also inlines the
-// extension ray's traversal, keeps them inline.
+// to one out-of-line copy.  The megakernel and the wavefront's shade stage
+// inline them.  With the earlier whole-leaf traversal step, calls made
+// wavefront shading 1.6x faster on a small scene (fewer instruction-fetch
+// stalls); with the one-slot step, inline is 1-4 % faster on every scene
+// measured.  kWfFinish, which runs few paths, keeps the calls.
 static __device__ __noinline__ bool closestOutOfLine(PathCtx* c, float3 o, float3 d, THit* h) {
     return closest(*c, o, d, *h);
 }

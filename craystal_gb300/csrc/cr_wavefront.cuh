@@ -492,7 +492,7 @@ __global__ void __launch_bounds__(kWfThreads, Src::kShadeMinBlocks) kWfShade(con
         h.u = hv.z;
         h.v = hv.w;
         typename Mode::Hooks hk = mode.hooks(st, k, meta);
-        const bool alive = shadeBounce<typename Mode::Hooks, true>(c, p, smp, depth, h, ro, rd, beta, radiance, hk);
+        const bool alive = shadeBounce<typename Mode::Hooks, false>(c, p, smp, depth, h, ro, rd, beta, radiance, hk);
         if (alive && depth + 1 < p.maxDepth) {
             push = true;
             st.ro[k] = make_float4(ro.x, ro.y, ro.z, o.w);
