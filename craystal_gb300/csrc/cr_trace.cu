@@ -258,6 +258,7 @@ void* mappedDevicePtr(const cr_scene* s, const void* p, size_t bytes) {
 // 14.96 ms.  false: the buffers do not qualify.
 template <bool kOcc>
 bool traceMapped(cr_scene* s, const cr_ray* rays, uint64_t n, void* out, int& rc) {
+    if (n > (~0ull >> 6)) return false;  // the byte counts below stay far from overflow
     const cr_ray* dr = static_cast<const cr_ray*>(mappedDevicePtr(s, rays, n * sizeof(cr_ray)));
     void* dout = mappedDevicePtr(s, out, n * (kOcc ? 1 : sizeof(cr_hit)));
     if (!dr || !dout) return false;

@@ -95,14 +95,16 @@ def _star_cluster(n, centre, rng):
     return tri.reshape(-1, 3).astype(np.float32)
 
 
+@pytest.mark.parametrize("size", [7, 8, 150])
 @pytest.mark.parametrize("with_others", [False, True])
-def test_closest_hits_large_leaves(gpu_lib, with_others):
-    """Leaves of more than 7 slots keep their range in the leaf table rather
-    than in the child ref: a 150-triangle leaf as the root, and the same leaf
-    below interior nodes among 3000 other triangles, hit bit-exactly."""
+def test_closest_hits_large_leaves(gpu_lib, with_others, size):
+    """A leaf of up to 7 slots carries its range in the child ref; a larger one
+    keeps it in the leaf table.  Leaves of 7, 8 and 150 coincident-centroid
+    triangles, as the root and below interior nodes among 3000 other
+    triangles, hit bit-exactly."""
     from craystal_gb300.api import MaterialData, MeshData, SceneData
     rng = np.random.default_rng(31)
-    pos = _star_cluster(150, (0.5, 0.5, 0.5), rng)
+    pos = _star_cluster(size, (0.5, 0.5, 0.5), rng)
     if with_others:
         pos = np.concatenate([pos, scenes.random_triangles(3000, seed=32)[0]]).astype(np.float32)
     data = SceneData(meshes=[MeshData(position=pos, index=np.arange(len(pos), dtype=np.uint32))],
@@ -110,13 +112,13 @@ def test_closest_hits_large_leaves(gpu_lib, with_others):
     g, o = both(data)
     assert_same_tree(g, o)
     st = g.bvh_stats()
-    assert st["max_leaf_size"] >= 150
+    assert st["max_leaf_size"] == size
     assert (st["leaf_count"] == 1) == (not with_others)
     rays = scenes.random_rays(200000, seed=33)
     gh = g.trace_closest(rays)
     oh, ties = o.trace_closest(rays)
-    cluster = (oh["prim"] != MISS) & (oh["prim"] < 150)
-    assert cluster.sum() > 1000
+    cluster = (oh["prim"] != MISS) & (oh["prim"] < size)
+    assert cluster.sum() > 100
     assert_same_hits(gh, oh, ties, max_tie_frac=1e-3)
     assert np.array_equal(g.trace_occluded(rays), o.trace_occluded(rays))
 
