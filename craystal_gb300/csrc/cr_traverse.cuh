@@ -4,11 +4,13 @@
 // Scene/Triangle.cu:40-75 (Moller-Trumbore with the absolute 1e-6
 // determinant cull), Scene/Shape.h:16-37 (closest-hit update rule) and
 // Core/BVH.cu:13-84 (near-first binary traversal with per-entry culling).
-// Only the memory layout differs: both children's boxes sit in one 64-byte
-// NodePair, the inverse direction is computed once per ray (the value
-// 1/d the reference recomputes per box is the same float), and each leaf
-// slot holds a pre-gathered 48-byte triangle block (v0, e1, e2) whose
-// edges are the differences the reference forms per test.
+// What differs is the memory layout and the unit of work: both children's
+// boxes sit in one 64-byte NodePair (read as two 32-byte loads), small
+// leaves carry their slot range in the child ref, the inverse direction is
+// computed once per ray (the value 1/d the reference recomputes per box is
+// the same float), each leaf slot holds a pre-gathered 48-byte triangle
+// block (v0, e1, e2) whose edges are the differences the reference forms
+// per test, and a traversal step is one node or one leaf slot (travStep).
 //
 // Visiting order.  The reference pushes the far child, then the near child,
 // and pops the near child at once; here the near child becomes the current
