@@ -309,6 +309,107 @@ def cornell_extra(torch):
     return out
 
 
+def rel_mse(img, ref):
+    """mean((I - R)^2 / (R^2 + 1e-2)) over pixels and channels, in FP64."""
+    img = np.nan_to_num(np.asarray(img, np.float64))
+    ref = np.nan_to_num(np.asarray(ref, np.float64))
+    return float(np.mean((img - ref) ** 2 / (ref ** 2 + 1e-2)))
+
+
+def gpu_film_1spp(integ, sc):
+    """The GPU film of one sample per pixel at sample index 0."""
+    sc.film_clear()
+    integ.dispatch(sc, 1, first_sample=0, readback=False)
+    return sc.film_read()
+
+
+def crop_parity(integ, sc, orgb, ow, rows, film=None):
+    """Equal-seed comparison of a full GPU render at 1 spp (sample index 0)
+    with the oracle's 1-spp render of rows [rows) (FP64 film): relMSE on the
+    rows whose filter footprint lies inside the band, and the two films'
+    mean radiance there."""
+    r0, r1 = rows
+    rgb, w = film if film is not None else gpu_film_1spp(integ, sc)
+    band = slice(r0 + 1, r1 - 1)
+    g = rgb[band] / w[band][..., None]
+    o = orgb[band] / ow[band][..., None]
+    return {"rows": [r0 + 1, r1 - 1], "spp": 1, "relmse_vs_oracle_equal_seed": rel_mse(g, o),
+            "mean_gpu": [round(float(x), 5) for x in np.nanmean(g, axis=(0, 1))],
+            "mean_oracle": [round(float(x), 5) for x in np.nanmean(o, axis=(0, 1))],
+            "weight_max_rel_diff": float(np.max(np.abs(w[band] - ow[band]) / np.maximum(ow[band], 1e-12)))}
+
+
+def c1_parity_extra(torch, chunks=128, chunk_spp=512, crop=(120, 136), crop_spp=4096):
+    """Parity of the plain path tracer at the C1 configuration (Cornell box,
+    256x256, 16 spp, max depth 8, rr 0.05, NEE + MIS):
+      - equal seed: the GPU's 16-spp image against the oracle's (same sample
+        indices 0..15), RGB and spectral;
+      - a 65,536-spp reference from the GPU plain tracer, `chunks` renders of
+        `chunk_spp` spp whose films are summed in FP64 on the host (sample
+        indices from 1,000,000 on, disjoint from the images compared with it),
+        spot-checked on rows [crop) against the oracle at `crop_spp` spp with
+        its FP64 film;
+      - the relMSE of the GPU's and the oracle's 16-spp images against that
+        reference."""
+    import oracle
+    from craystal_gb300 import scenes
+    from craystal_gb300.api import PathTraceIntegrator, Scene, flatten_scene
+    data, cam = scenes.cornell_box(seed=0, width=256, height=256)
+    sc = Scene(data)
+    sc.setCamera(cam)
+    cfg = PathTraceIntegrator.Configs(maxDepth=8, rrThreshold=0.05, useMIS=True)
+    threads = oracle.hardware_threads()
+    osc = oracle.OracleScene(flatten_scene(data))
+    oc = oracle.make_camera(cam.posW, cam.target, cam.up, cam.fovY, 256, 256)
+    out = {"config": "cornell 256x256, 16 spp, max depth 8, rr 0.05, NEE+MIS; relMSE = mean((I-R)^2/(R^2+1e-2))"}
+    imgs = {}
+    for label, spectral in (("rgb", False), ("spectral", True)):
+        integ = PathTraceIntegrator(cfg, compat=False, spectral=spectral)
+        sc.film_clear()
+        integ.dispatch(sc, 16, readback=False)
+        rgb, w = sc.film_read()
+        img = rgb / w[..., None]
+        (orgb, ow), _ = osc.render(oc, 8, 0.05, True, spp=16, threads=threads, spectral=spectral)
+        oimg = orgb / ow[..., None]
+        imgs[label] = (img, oimg)
+        out[f"equal_seed_relmse_{label}"] = rel_mse(img, oimg)
+    # the 65,536-spp reference: FP64 sum of the GPU films
+    integ = PathTraceIntegrator(cfg, compat=False)
+    acc = np.zeros((256, 256, 3))
+    accw = np.zeros((256, 256))
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for k in range(chunks):
+        sc.film_clear()
+        integ.dispatch(sc, chunk_spp, first_sample=1_000_000 + chunk_spp * k, readback=False)
+        rgb, w = sc.film_read()
+        acc += rgb
+        accw += w
+    ref_s = time.perf_counter() - t
+    ref = acc / accw[..., None]
+    # spot check: the oracle's own FP64 film at crop_spp on a band of rows
+    r0, r1 = crop
+    t = time.perf_counter()
+    (orgb, ow), _ = osc.render(oc, 8, 0.05, True, spp=crop_spp, first_sample=50_000_000, rows=(r0, r1),
+                               threads=threads)
+    crop_s = time.perf_counter() - t
+    band = slice(r0 + 1, r1 - 1)  # rows whose filter footprint lies inside the rendered band
+    ocrop = orgb[band] / ow[band][..., None]
+    img, oimg = imgs["rgb"]
+    out["reference"] = {"spp": chunks * chunk_spp, "film": "FP64 sum of GPU plain-tracer films",
+                        "render_s": round(ref_s, 2)}
+    out["reference_spot_check"] = {
+        "rows": [r0 + 1, r1 - 1], "oracle_spp": crop_spp, "oracle_s": round(crop_s, 2),
+        "relmse_reference_vs_oracle": rel_mse(ref[band], ocrop),
+        "relmse_oracle_16spp_vs_oracle": rel_mse(oimg[band], ocrop),
+        "note": "the oracle band's own noise at its spp is about 16/oracle_spp of its 16-spp error"}
+    out["relmse_vs_reference_16spp"] = {"gpu": rel_mse(img, ref), "oracle": rel_mse(oimg, ref),
+                                        "gpu_spectral": rel_mse(imgs["spectral"][0], ref),
+                                        "oracle_spectral": rel_mse(imgs["spectral"][1], ref)}
+    sc.close()
+    return out
+
+
 def c3_extra(torch, res=(1920, 1080), budgets=(16, 64)):
     """The radiance-cache config: 8 displaced icospheres (2.6M triangles),
     Principled materials, constant environment 0.5 and one sphere light, max
@@ -348,13 +449,17 @@ def c3_extra(torch, res=(1920, 1080), budgets=(16, 64)):
     osc.set_lights(env, sph)
     oc = oracle.make_camera(cam.posW, cam.target, cam.up, cam.fovY, 1920, 1080)
     t = time.perf_counter()
-    _, orays = osc.render(oc, 16, 0.05, True, spp=1, rows=(508, 572), threads=threads)
+    (orgb, ow), orays = osc.render(oc, 16, 0.05, True, spp=1, rows=(508, 572), threads=threads)
     cpu_s = time.perf_counter() - t
     cpu_rate = 1920 * 64 / cpu_s
     out["cpu_oracle"] = {"Mpaths_s": round(cpu_rate / 1e6, 4), "Mrays_s": round(orays / cpu_s / 1e6, 4),
                          "threads": threads, "sample": "rows 508-571 at 1 spp",
                          "projected_1080p_64spp_s": round(1920 * 1080 * 64 / cpu_rate, 1)}
     del osc
+    # parity at this configuration: the GPU's 1-spp render at the same sample
+    # index (0) against the oracle's band, on the rows whose filter footprint
+    # lies inside it
+    out["parity"] = crop_parity(plain, sc, orgb, ow, (508, 572))
     w, h = res
     cam.setSensor(type(cam.sensor)((w, h)))
     sc.setCamera(cam)
@@ -497,6 +602,9 @@ def large_scene_extra(torch, spp=32):
     free1, _ = torch.cuda.mem_get_info()
     rays = sc.render_ray_count()
     rgb, w = sc.film_read()
+    # for parity below: the 1-spp film at sample index 0 and the GPU's tree
+    film1 = gpu_film_1spp(integ, sc)
+    gnodes, gmap = sc.bvh_export()
     paths = 3840 * 2160 * spp
     out = {"config": "terrain 4096^2 (fBm, 6 octaves) + 10k boxes, 3840x2160, 32 spp, depth 12, sun + sky",
            "triangles": int(n_tris), "host_generation_s": round(gen_s, 2), "scene_create_s": round(create_s, 2),
@@ -514,10 +622,12 @@ def large_scene_extra(torch, spp=32):
     osc = oracle.OracleScene(flat)
     build_s = time.perf_counter() - t
     del flat
+    out["tree_vs_oracle"] = compare_trees(gnodes, gmap, *osc.bvh_export())
+    del gnodes, gmap
     osc.set_lights(env, sun)
     oc = oracle.make_camera(cam.posW, cam.target, cam.up, cam.fovY, 3840, 2160)
     t = time.perf_counter()
-    _, orays = osc.render(oc, 12, 0.05, True, spp=1, rows=(1072, 1088), threads=threads)
+    (orgb, ow), orays = osc.render(oc, 12, 0.05, True, spp=1, rows=(1072, 1088), threads=threads)
     cpu_s = time.perf_counter() - t
     cpu_rate = 3840 * 16 / cpu_s
     out["cpu_oracle"] = {"bvh_build_s": round(build_s, 1), "Mpaths_s": round(cpu_rate / 1e6, 4),
@@ -525,6 +635,35 @@ def large_scene_extra(torch, spp=32):
                          "sample": "rows 1072-1087 at 1 spp",
                          "projected_render_s": round(paths / cpu_rate, 1)}
     del osc
+    out["parity"] = crop_parity(None, None, orgb, ow, (1072, 1088), film=film1)
+    return out
+
+
+def compare_trees(gnodes, gmap, onodes, omap):
+    """The GPU's tree against the oracle's (the reference's host build), both
+    in the reference layout: node count, every box as bits, topology, and
+    the set of triangles in every leaf (slot order inside a leaf may differ,
+    since the builders partition in different orders)."""
+    out = {"nodes_gpu": int(len(gnodes)), "nodes_oracle": int(len(onodes))}
+    same_size = len(gnodes) == len(onodes) and len(gmap) == len(omap)
+    boxes = same_size and (np.array_equal(gnodes["bmin"].view(np.uint32), onodes["bmin"].view(np.uint32)) and
+                           np.array_equal(gnodes["bmax"].view(np.uint32), onodes["bmax"].view(np.uint32)))
+    topo = same_size and (np.array_equal(gnodes["is_leaf"], onodes["is_leaf"]) and
+                          np.array_equal(gnodes["a"], onodes["a"]) and np.array_equal(gnodes["b"], onodes["b"]))
+    leaves_same = False
+    if topo:
+        lf = gnodes[gnodes["is_leaf"] == 1]
+        starts, counts = lf["a"].astype(np.int64), lf["b"].astype(np.int64)
+        # the slots of every leaf, leaf after leaf, tagged with the leaf's number
+        within = np.arange(counts.sum()) - np.repeat(np.cumsum(counts) - counts, counts)
+        slots = np.repeat(starts, counts) + within
+        leaf = np.repeat(np.arange(len(lf), dtype=np.int64), counts)
+        if len(slots) == len(gmap) and len(np.unique(slots)) == len(gmap):
+            g = np.sort(leaf << 32 | gmap[slots].astype(np.int64))
+            o = np.sort(leaf << 32 | omap[slots].astype(np.int64))
+            leaves_same = bool(np.array_equal(g, o))
+    out.update({"boxes_bit_equal": bool(boxes), "topology_equal": bool(topo), "leaf_sets_equal": leaves_same,
+                "tree_equal": bool(boxes and topo and leaves_same)})
     return out
 
 
@@ -786,6 +925,7 @@ def run_ours(args):
         extra["restated_reference_kernel"] = restated_reference_extra(torch, sc, flatten_scene(data), d_rays, N_RAYS,
                                                                       d_hits)
         extra["path_tracer"] = cornell_extra(torch)
+        extra["c1_parity"] = c1_parity_extra(torch)
         extra["wavefront_vs_megakernel"] = wavefront_extra(torch)
         extra["radiance_cache_network"] = mlp_extra(torch)
         extra["radiance_cache_equal_time"] = cache_extra(torch, args.cache_res)
@@ -846,6 +986,8 @@ def run_only(args):
     cg.load().cr_set_device(0)
     if args.only == "path_tracer":
         r = cornell_extra(torch)
+    elif args.only == "c1_parity":
+        r = c1_parity_extra(torch)
     elif args.only == "wavefront":
         r = wavefront_extra(torch)
     elif args.only == "radiance_cache":
@@ -873,7 +1015,7 @@ def main():
     ap.add_argument("--skip-extra", action="store_true", help="omit the path-tracer figures")
     ap.add_argument("--rays", type=int, default=N_RAYS, help="rays per step (profiling a smaller case)")
     ap.add_argument("--tris", type=int, default=N_TRIS, help="triangles (profiling a smaller case)")
-    ap.add_argument("--only", choices=["path_tracer", "wavefront", "radiance_cache", "cache_frames", "batched_scenes",
+    ap.add_argument("--only", choices=["path_tracer", "c1_parity", "wavefront", "radiance_cache", "cache_frames", "batched_scenes",
                                        "large_scene", "radiance_cache_scene", "radiance_cache_network"],
                     help="run one secondary workload alone and print its figures (profiling)")
     ap.add_argument("--cache-res", type=int, default=512, help="radiance-cache workload resolution")

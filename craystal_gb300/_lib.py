@@ -17,6 +17,7 @@ CR_ERR_CUDA = 2
 CR_ERR_OUT_OF_MEMORY = 3
 CR_ERR_DEVICE = 4
 CR_ERR_UNSUPPORTED = 5
+CR_DEVICE_ERROR_STACK_OVERFLOW = 1
 CR_MISS = 0xFFFFFFFF
 CR_NOALLOC_MAX_RAYS = 65536
 CR_NO_TEXTURE = 0xFFFFFFFF
@@ -126,6 +127,9 @@ SIGNATURES = [
     ("cr_scene_destroy", ctypes.c_int, [_P]),
     ("cr_scene_bvh_stats", ctypes.c_int, [_P, ctypes.POINTER(CrBvhStats)]),
     ("cr_scene_bvh_export", ctypes.c_int, [_P, _P, _P]),
+    ("cr_scene_bvh_import", ctypes.c_int, [_P, _P, _U32, _P]),
+    ("cr_scene_check_errors", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint32)]),
+    ("cr_scene_set_error_flags", ctypes.c_int, [_P, _U32]),
     ("cr_scene_set_camera", ctypes.c_int, [_P, ctypes.POINTER(CrCamera)]),
     ("cr_scene_set_environment", ctypes.c_int, [_P, _P]),
     ("cr_scene_set_sphere_lights", ctypes.c_int, [_P, _P, _U32]),

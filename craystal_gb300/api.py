@@ -303,6 +303,23 @@ class Scene:
         check(load().cr_scene_bvh_export(self._h, ptr(nodes), ptr(pmap)))
         return nodes, pmap
 
+    def bvh_import(self, nodes: np.ndarray, prim_map: np.ndarray):
+        """Replaces the tree with one in the reference layout (nodes with the
+        root last, leaf (first slot, count) into prim_map), e.g. the tree the
+        reference's host builder makes (Core/BVH.cu:303-338)."""
+        nodes = np.ascontiguousarray(nodes, BVH_NODE_DTYPE)
+        prim_map = np.ascontiguousarray(prim_map, np.uint32)
+        if len(prim_map) != self.n_tris:
+            raise ValueError(f"prim_map has {len(prim_map)} entries; the scene has {self.n_tris} triangles")
+        check(load().cr_scene_bvh_import(self._h, ptr(nodes), len(nodes), ptr(prim_map)))
+
+    def check_errors(self) -> int:
+        """Waits for the device, then reports (CrayError, code CR_ERR_DEVICE)
+        and clears the errors kernels raised on this scene; returns 0."""
+        flags = ctypes.c_uint32()
+        check(load().cr_scene_check_errors(self._h, ctypes.byref(flags)))
+        return flags.value
+
     # --- ray queries (SceneView::intersect / intersectOcclusion) ---
     def trace_closest(self, rays: np.ndarray) -> np.ndarray:
         rays = np.ascontiguousarray(rays, RAY_DTYPE)

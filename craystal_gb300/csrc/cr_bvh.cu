@@ -738,9 +738,25 @@ __global__ void kLeafFlags(const BuildNode* __restrict__ nodes, uint32_t n, uint
     if (i < n) isLeaf[i] = nodes[i].info.z;
 }
 
-__device__ __forceinline__ uint32_t childRef(const BuildNode* nodes, const uint32_t* leafPrefix, uint32_t c) {
+__host__ __device__ __forceinline__ uint32_t childRef(const BuildNode* nodes, const uint32_t* leafPrefix, uint32_t c) {
     const BuildNode& n = nodes[c];
     return n.info.z ? leafRef(leafPrefix[c], n.info.x, n.info.y) : (c - leafPrefix[c]);
+}
+
+// The NodePair of interior node i: both children's boxes, refs and
+// degenerate-axis flags.  Interior node i becomes pair i - leafPrefix[i].
+__host__ __device__ __forceinline__ NodePair pairOf(const BuildNode* nodes, const uint32_t* leafPrefix, uint32_t i) {
+    const BuildNode& nd = nodes[i];
+    const BuildNode& L = nodes[nd.info.x];
+    const BuildNode& R = nodes[nd.info.y];
+    NodePair p;
+    p.p0 = make_float4(L.lo.x, L.lo.y, L.lo.z, L.hi.x);
+    p.p1 = make_float4(L.hi.y, L.hi.z, R.lo.x, R.lo.y);
+    p.p2 = make_float4(R.lo.z, R.hi.x, R.hi.y, R.hi.z);
+    uint32_t fl = degenerateFlags(mk3(L.lo.x, L.lo.y, L.lo.z), mk3(L.hi.x, L.hi.y, L.hi.z)) |
+                  (degenerateFlags(mk3(R.lo.x, R.lo.y, R.lo.z), mk3(R.hi.x, R.hi.y, R.hi.z)) << 3);
+    p.ref = make_uint4(childRef(nodes, leafPrefix, nd.info.x), childRef(nodes, leafPrefix, nd.info.y), fl, 0u);
+    return p;
 }
 
 __global__ void kLayout(const BuildNode* __restrict__ nodes, uint32_t n, const uint32_t* __restrict__ leafPrefix,
@@ -752,15 +768,7 @@ __global__ void kLayout(const BuildNode* __restrict__ nodes, uint32_t n, const u
         leaves[leafPrefix[i]] = make_uint2(nd.info.x, nd.info.y);
         return;
     }
-    const BuildNode L = nodes[nd.info.x], R = nodes[nd.info.y];
-    NodePair p;
-    p.p0 = make_float4(L.lo.x, L.lo.y, L.lo.z, L.hi.x);
-    p.p1 = make_float4(L.hi.y, L.hi.z, R.lo.x, R.lo.y);
-    p.p2 = make_float4(R.lo.z, R.hi.x, R.hi.y, R.hi.z);
-    uint32_t fl = degenerateFlags(mk3(L.lo.x, L.lo.y, L.lo.z), mk3(L.hi.x, L.hi.y, L.hi.z)) |
-                  (degenerateFlags(mk3(R.lo.x, R.lo.y, R.lo.z), mk3(R.hi.x, R.hi.y, R.hi.z)) << 3);
-    p.ref = make_uint4(childRef(nodes, leafPrefix, nd.info.x), childRef(nodes, leafPrefix, nd.info.y), fl, 0u);
-    pairs[i - leafPrefix[i]] = p;
+    pairs[i - leafPrefix[i]] = pairOf(nodes, leafPrefix, i);
 }
 
 __global__ void kTriBlocks(const float3* __restrict__ pos, const uint32_t* __restrict__ idx,
@@ -1178,6 +1186,144 @@ int exportBvh(const cr_scene* s, cr_bvh_node* out, uint32_t* primMap) {
         o.a = n.info.z ? n.info.x : post[n.info.x];
         o.b = n.info.z ? n.info.y : post[n.info.y];
     }
+    return CR_OK;
+}
+
+}  // namespace cr
+
+namespace cr {
+
+// Replaces the scene's triangle BVH with a tree given in the reference's
+// layout (BVHData, Core/BVH.h:17-30, as BVH::createFinalBVH fills it,
+// Core/BVH.cu:303-338): nodes in any order with the root last, interior
+// children by index, leaves as (first slot, count) ranges of primMap, which
+// maps each of the n_tris leaf slots to a triangle.  The tree is checked
+// (every index in range, every node reached once from the root, depth within
+// the traversal stack), renumbered breadth-first and laid out as NodePairs
+// and triangle blocks like a built tree; traversal then visits it in the
+// reference's order with the reference's culling.
+int importBvh(cr_scene* s, const cr_bvh_node* in, uint32_t nodeCount, const uint32_t* primMap) {
+    if (s->nt == 0) {
+        if (nodeCount) return fail(CR_ERR_INVALID_ARGUMENT, "the scene has no triangles; pass node_count 0");
+        return CR_OK;
+    }
+    if (!in || nodeCount == 0 || !primMap) return fail(CR_ERR_INVALID_ARGUMENT, "nodes / prim_map is NULL or empty");
+    const uint64_t nSlots = s->nt;
+    for (uint64_t i = 0; i < nSlots; i++)
+        if (primMap[i] >= s->nt)
+            return fail(CR_ERR_INVALID_ARGUMENT, "prim_map[%llu] = %u is not a triangle", (unsigned long long)i,
+                        primMap[i]);
+    // breadth-first renumbering from the root (the last node), with checks
+    std::vector<uint32_t> order;  // new index -> input index
+    std::vector<uint32_t> depth;
+    std::vector<uint8_t> seen(nodeCount, 0);
+    order.reserve(nodeCount);
+    order.push_back(nodeCount - 1);
+    depth.push_back(0);
+    seen[nodeCount - 1] = 1;
+    uint32_t maxDepth = 0, maxLeafDepth = 0, maxLeafSize = 0, nLeaves = 0;
+    for (size_t k = 0; k < order.size(); k++) {
+        const cr_bvh_node& n = in[order[k]];
+        if (n.is_leaf > 1) return fail(CR_ERR_INVALID_ARGUMENT, "node %u: is_leaf = %u", order[k], n.is_leaf);
+        if (n.is_leaf) {
+            if ((uint64_t)n.a + n.b > nSlots)
+                return fail(CR_ERR_INVALID_ARGUMENT, "leaf %u: slots %u + %u run past the %llu slots", order[k], n.a,
+                            n.b, (unsigned long long)nSlots);
+            nLeaves++;
+            maxLeafSize = std::max(maxLeafSize, n.b);
+            maxLeafDepth = std::max(maxLeafDepth, depth[k]);
+            continue;
+        }
+        maxDepth = std::max(maxDepth, depth[k]);
+        // a near-first traversal holds at most one pushed entry per level
+        // above the current node, so pushing at an interior node of depth d
+        // needs d + 1 stack entries
+        if (depth[k] + 1 > (uint32_t)kStackSize)
+            return fail(CR_ERR_UNSUPPORTED,
+                        "node %u is an interior node at depth %u; the %d-entry traversal stack holds depths up to %d",
+                        order[k], depth[k], kStackSize, kStackSize - 1);
+        for (uint32_t c : {n.a, n.b}) {
+            if (c >= nodeCount) return fail(CR_ERR_INVALID_ARGUMENT, "node %u: child %u of %u", order[k], c, nodeCount);
+            if (seen[c]) return fail(CR_ERR_INVALID_ARGUMENT, "node %u is reached twice (not a tree)", c);
+            seen[c] = 1;
+            order.push_back(c);
+            depth.push_back(depth[k] + 1);
+        }
+    }
+    if (order.size() != nodeCount)
+        return fail(CR_ERR_INVALID_ARGUMENT, "%u of %u nodes are not reached from the root (node %u)",
+                    (uint32_t)(nodeCount - order.size()), nodeCount, nodeCount - 1);
+    if (nLeaves > ~(kLeafBit | kInlineLeafBit)) return fail(CR_ERR_UNSUPPORTED, "%u leaves", nLeaves);
+    std::vector<uint32_t> newIndex(nodeCount);
+    for (uint32_t k = 0; k < nodeCount; k++) newIndex[order[k]] = k;
+    std::vector<BuildNode> nodes(nodeCount);
+    std::vector<uint32_t> leafPrefix(nodeCount);
+    uint32_t leavesBefore = 0;
+    for (uint32_t k = 0; k < nodeCount; k++) {
+        const cr_bvh_node& n = in[order[k]];
+        BuildNode& b = nodes[k];
+        b.lo = make_float4(n.bmin[0], n.bmin[1], n.bmin[2], 0.0f);
+        b.hi = make_float4(n.bmax[0], n.bmax[1], n.bmax[2], 0.0f);
+        b.info = n.is_leaf ? make_uint4(n.a, n.b, 1u, depth[k]) : make_uint4(newIndex[n.a], newIndex[n.b], 0u, depth[k]);
+        leafPrefix[k] = leavesBefore;
+        leavesBefore += n.is_leaf;
+    }
+    const uint32_t nPairs = nodeCount - nLeaves;
+    std::vector<NodePair> pairs(std::max<uint32_t>(nPairs, 1));
+    std::vector<uint2> leaves(std::max<uint32_t>(nLeaves, 1));
+    for (uint32_t k = 0; k < nodeCount; k++) {
+        if (nodes[k].info.z) leaves[leafPrefix[k]] = make_uint2(nodes[k].info.x, nodes[k].info.y);
+        else pairs[k - leafPrefix[k]] = pairOf(nodes.data(), leafPrefix.data(), k);
+    }
+    DevBuf<NodePair> dPairs;
+    DevBuf<uint2> dLeaves;
+    DevBuf<BuildNode> dNodes;
+    DevBuf<uint32_t> dOrder;
+    DevBuf<TriBlock> dTris;
+    CR_CUDA(dPairs.alloc(nPairs));
+    CR_CUDA(dLeaves.alloc(nLeaves));
+    CR_CUDA(dNodes.alloc(nodeCount));
+    CR_CUDA(dOrder.alloc(nSlots));
+    CR_CUDA(dTris.alloc(nSlots));
+    CR_CUDA(cudaMemcpy(dPairs.p, pairs.data(), (size_t)nPairs * sizeof(NodePair), cudaMemcpyHostToDevice));
+    CR_CUDA(cudaMemcpy(dLeaves.p, leaves.data(), (size_t)nLeaves * sizeof(uint2), cudaMemcpyHostToDevice));
+    CR_CUDA(cudaMemcpy(dNodes.p, nodes.data(), (size_t)nodeCount * sizeof(BuildNode), cudaMemcpyHostToDevice));
+    CR_CUDA(cudaMemcpy(dOrder.p, primMap, nSlots * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    kTriBlocks<<<blocksFor(nSlots, 256), 256>>>(s->pos, s->idx, dOrder.p, (uint32_t)nSlots, dTris.p);
+    CR_LAUNCH_CHECK();
+    CR_CUDA(cudaDeviceSynchronize());
+    // the new tree is complete: drop the old one (cudaFree waits for queries still using it)
+    void* old[] = {s->pairs, s->leaves, s->tris, s->slotToPrim, s->buildNodes};
+    for (void* p : old)
+        if (p) cudaFree(p);
+    const BuildNode& root = nodes[0];
+    s->pairs = dPairs.release();
+    s->nPairs = nPairs;
+    s->leaves = dLeaves.release();
+    s->nLeaves = nLeaves;
+    s->tris = dTris.release();
+    s->slotToPrim = dOrder.release();
+    s->buildNodes = dNodes.release();
+    s->nBuildNodes = nodeCount;
+    s->rootMin = mk3(root.lo.x, root.lo.y, root.lo.z);
+    s->rootMax = mk3(root.hi.x, root.hi.y, root.hi.z);
+    s->rootFlags = degenerateFlags(s->rootMin, s->rootMax);
+    s->rootRef = root.info.z ? kLeafBit : 0u;
+    s->hasRoot = 1;
+    cr_bvh_stats& st = s->stats;
+    st = cr_bvh_stats{};
+    st.node_count = nodeCount;
+    st.leaf_count = nLeaves;
+    st.max_depth = maxDepth;
+    st.max_leaf_size = maxLeafSize;
+    st.max_leaf_depth = maxLeafDepth;
+    st.levels = 0;
+    for (int k = 0; k < 3; k++) {
+        st.root_min[k] = k == 0 ? root.lo.x : (k == 1 ? root.lo.y : root.lo.z);
+        st.root_max[k] = k == 0 ? root.hi.x : (k == 1 ? root.hi.y : root.hi.z);
+    }
+    st.build_ms = 0.0;
+    st.device_bytes = (uint64_t)nPairs * sizeof(NodePair) + (uint64_t)nLeaves * sizeof(uint2) + nSlots * sizeof(TriBlock);
     return CR_OK;
 }
 

@@ -36,6 +36,18 @@ int fail(int code, const char* fmt, ...) {
 
 void countLaunch(uint64_t n) { gLaunches.fetch_add(n, std::memory_order_relaxed); }
 
+// Reads the scene's device error word and, when a bit is set, clears it and
+// returns CR_ERR_DEVICE: each error a kernel raises is reported by exactly
+// one call.  The caller has waited for the work whose errors it reports.
+int takeDeviceErrors(cr_scene* s, const char* what) {
+    uint32_t err = 0;
+    CR_CUDA(cudaMemcpy(&err, s->errFlags, sizeof(err), cudaMemcpyDeviceToHost));
+    if (!err) return CR_OK;
+    CR_CUDA(cudaMemset(s->errFlags, 0, sizeof(err)));
+    return fail(CR_ERR_DEVICE, "%s: device error flags 0x%x%s", what, err,
+                (err & kErrStackOverflow) ? " (traversal stack overflow)" : "");
+}
+
 namespace {
 
 // MaterialData::finalize (Core/Material.h:57-65) and the per-material part
@@ -222,6 +234,13 @@ int cr_scene_bvh_export(const cr_scene* scene, cr_bvh_node* nodes, uint32_t* pri
     return exportBvh(scene, nodes, prim_map);
 }
 
+int cr_scene_bvh_import(cr_scene* scene, const cr_bvh_node* nodes, uint32_t node_count, const uint32_t* prim_map) {
+    clearError();
+    if (!scene) return fail(CR_ERR_INVALID_ARGUMENT, "scene is NULL");
+    CR_CUDA(cudaSetDevice(scene->device));
+    return importBvh(scene, nodes, node_count, prim_map);
+}
+
 int cr_scene_set_camera(cr_scene* scene, const cr_camera* cam) {
     clearError();
     if (!scene || !cam) return fail(CR_ERR_INVALID_ARGUMENT, "NULL argument");
@@ -396,9 +415,30 @@ int cr_film_read(cr_scene* scene, float* rgb, float* weight) {
     const size_t px = (size_t)scene->cam.width * scene->cam.height;
     if (rgb) CR_CUDA(cudaMemcpy(rgb, scene->filmRgb, px * 3 * sizeof(float), cudaMemcpyDeviceToHost));
     if (weight) CR_CUDA(cudaMemcpy(weight, scene->filmW, px * sizeof(float), cudaMemcpyDeviceToHost));
+    return takeDeviceErrors(scene, "render");
+}
+
+int cr_scene_check_errors(cr_scene* scene, uint32_t* flags) {
+    clearError();
+    if (flags) *flags = 0;
+    if (!scene) return fail(CR_ERR_INVALID_ARGUMENT, "scene is NULL");
+    CR_CUDA(cudaSetDevice(scene->device));
+    CR_CUDA(cudaDeviceSynchronize());
     uint32_t err = 0;
-    CR_CUDA(cudaMemcpy(&err, scene->errFlags, 4, cudaMemcpyDeviceToHost));
-    if (err) return fail(CR_ERR_DEVICE, "render reported device error flags 0x%x", err);
+    CR_CUDA(cudaMemcpy(&err, scene->errFlags, sizeof(err), cudaMemcpyDeviceToHost));
+    if (flags) *flags = err;
+    return takeDeviceErrors(scene, "scene");
+}
+
+int cr_scene_set_error_flags(cr_scene* scene, uint32_t flags) {
+    clearError();
+    if (!scene) return fail(CR_ERR_INVALID_ARGUMENT, "scene is NULL");
+    CR_CUDA(cudaSetDevice(scene->device));
+    CR_CUDA(cudaDeviceSynchronize());
+    uint32_t err = 0;
+    CR_CUDA(cudaMemcpy(&err, scene->errFlags, sizeof(err), cudaMemcpyDeviceToHost));
+    err |= flags;
+    CR_CUDA(cudaMemcpy(scene->errFlags, &err, sizeof(err), cudaMemcpyHostToDevice));
     return CR_OK;
 }
 

@@ -295,10 +295,13 @@ struct cr_scene {
 
 namespace cr {
 
+// implemented in cr_core.cu: reports and clears the scene's device error word
+int takeDeviceErrors(cr_scene* s, const char* what);
 // implemented in cr_bvh.cu
 int buildBvh(cr_scene* s);
 int buildSphereBvh(cr_scene* s);
 int exportBvh(const cr_scene* s, cr_bvh_node* nodes, uint32_t* primMap);
+int importBvh(cr_scene* s, const cr_bvh_node* nodes, uint32_t nodeCount, const uint32_t* primMap);
 // implemented in cr_trace.cu
 // mayAllocate = false: no device allocation (the no-allocation entry point)
 int traceClosestDevice(cr_scene* s, const cr_ray* rays, uint64_t n, cr_hit* hits, cudaStream_t st,

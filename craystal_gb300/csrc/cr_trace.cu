@@ -125,18 +125,25 @@ __global__ void __launch_bounds__(kTraceThreads) kTraceDyn(const SceneView sc, c
     }
 }
 
+// Resident blocks per SM of each kernel, per device ordinal (0 = not yet
+// asked).  Host threads may call at once: each entry is an atomic, and two
+// threads that both ask store the same value.
+constexpr int kOccDevices = 64;
+std::atomic<int> gOccupancy[kOccDevices][2];
+
 int traceDynBlocks(bool anyHit, uint64_t n) {
-    static int occClosest = 0, occAny = 0;
-    int& occ = anyHit ? occAny : occClosest;
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int occ = 0;
+    if (dev >= 0 && dev < kOccDevices) occ = gOccupancy[dev][anyHit ? 1 : 0].load(std::memory_order_relaxed);
     if (!occ) {
         int b = 0;
         if (anyHit) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kTraceDyn<true>, kTraceThreads, 0);
         else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kTraceDyn<false>, kTraceThreads, 0);
         occ = b > 0 ? b : 1;
+        if (dev >= 0 && dev < kOccDevices) gOccupancy[dev][anyHit ? 1 : 0].store(occ, std::memory_order_relaxed);
     }
-    int dev = 0, sms = 1;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const uint64_t perThread = (n + kTraceThreads - 1) / kTraceThreads;
     return (int)std::min<uint64_t>((uint64_t)sms * occ, std::max<uint64_t>(1, perThread));
 }
@@ -304,10 +311,7 @@ int traceHost(cr_scene* s, const cr_ray* rays, uint64_t n, void* out) {
     }
     CR_CUDA(cudaStreamSynchronize(s->streams[0]));
     CR_CUDA(cudaStreamSynchronize(s->streams[1]));
-    uint32_t err = 0;
-    CR_CUDA(cudaMemcpy(&err, s->errFlags, 4, cudaMemcpyDeviceToHost));
-    if (err) return fail(CR_ERR_DEVICE, "traversal reported device error flags 0x%x", err);
-    return CR_OK;
+    return takeDeviceErrors(s, "traversal");
 }
 
 }  // namespace

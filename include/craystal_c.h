@@ -180,6 +180,39 @@ int cr_scene_bvh_stats(const cr_scene* scene, cr_bvh_stats* out);
 int cr_scene_bvh_export(const cr_scene* scene, cr_bvh_node* nodes,
                         uint32_t* prim_map);
 
+/* Replaces the scene's triangle BVH with a tree in the same layout, e.g. one
+ * built by the reference's host builder (BVH::build + createFinalBVH,
+ * Core/BVH.cu:88-116 and :303-338; BVHData, Core/BVH.h:17-30): node_count
+ * nodes with the root last, interior (a, b) = child indices, leaf (a, b) =
+ * (first slot, count) into prim_map, which has n_tris entries, each a
+ * triangle index.  Node order need not be post-order, but every node must be
+ * reached exactly once from the root.  Queries and renders then traverse this
+ * tree in the reference's order, so hits equal the reference's on the same
+ * tree bit for bit, ties included.  Rejected: indices out of range, a node
+ * reached twice or not at all (CR_ERR_INVALID_ARGUMENT), an interior node
+ * deeper than 31 levels, which the 32-entry traversal stack cannot hold
+ * (CR_ERR_UNSUPPORTED; the reference builder stops at depth 20).  The
+ * scene's statistics describe the imported tree (build_ms 0).  Waits for
+ * work that uses the old tree. */
+int cr_scene_bvh_import(cr_scene* scene, const cr_bvh_node* nodes,
+                        uint32_t node_count, const uint32_t* prim_map);
+
+/* Errors that kernels detect (a traversal stack that would overflow) set
+ * bits of the scene's device error word.  cr_trace_closest,
+ * cr_trace_occluded, cr_trace_closest_noalloc and cr_film_read read it when
+ * they finish and return CR_ERR_DEVICE when a bit is set; the "_device" entry
+ * points and cr_render return before their kernels run, so their errors are
+ * reported by the next of those calls or by cr_scene_check_errors.  The word
+ * is cleared when it is reported: each error is reported once.
+ * cr_scene_check_errors waits for the device, stores the word in *flags (may
+ * be NULL), clears it and returns CR_ERR_DEVICE when it was set.
+ * cr_scene_set_error_flags ORs bits into the word from the host, as a kernel
+ * that detected an error does, so that callers can test their handling of
+ * CR_ERR_DEVICE without a failing kernel. */
+#define CR_DEVICE_ERROR_STACK_OVERFLOW 1u
+int cr_scene_check_errors(cr_scene* scene, uint32_t* flags);
+int cr_scene_set_error_flags(cr_scene* scene, uint32_t flags);
+
 /* Scene::setCamera + Camera::calculateCameraData + Sensor(size)
  * (Scene/Scene.h:56-58, Core/Camera.cu:35-39, Core/Sensor.cu:46-60).  A
  * sensor of a new size gets a new film, cleared to zero. */
@@ -389,15 +422,22 @@ int cr_bsdf_sample(const cr_material* mat, const float* n, const float* wo,
  * not stall on the device synchronisation cudaMalloc / cudaFree imply, or a
  * plugin whose host forbids allocation after start-up.  Rays and hits pass
  * through a fixed staging area inside the library's device image
- * (CR_NOALLOC_MAX_RAYS rays and hits, 3 MiB, held by every GPU that loads the
- * library until the process exits); n above CR_NOALLOC_MAX_RAYS is rejected
- * with CR_ERR_INVALID_ARGUMENT.  The staging area is shared by all calls on a
- * device: calls whose work overlaps on the GPU race on it, so callers
- * serialise them.  The first call on a device looks up the staging area's
- * device address (set-up, done once per device); make that first call before
- * any stream capture begins.  Results equal cr_trace_closest's.  Returns when
- * the hits are in the host array; the copies and the traversal run on
- * `stream` (NULL = legacy default stream). */
+ * (CR_NOALLOC_MAX_RAYS rays and hits, 3 MiB); n above CR_NOALLOC_MAX_RAYS is
+ * rejected with CR_ERR_INVALID_ARGUMENT.  The staging area is shared by all
+ * calls on a device: calls whose work overlaps on the GPU race on it, so
+ * callers serialise them.
+ * First call on a device: under CUDA's default lazy module loading it makes
+ * the driver load the staging area (3 MiB of device memory, which then stays
+ * resident on that device until the process exits) and the traversal
+ * kernel's code; make that call at start-up, before the caller commits its
+ * memory budget (or set CUDA_MODULE_LOADING=EAGER), and before any stream
+ * capture begins.  It also looks up the staging area's device address, again
+ * whenever the device's context has changed (after cudaDeviceReset).
+ * Results equal cr_trace_closest's.  The scene's device error word is shared
+ * by all its queries: a call reports (and clears) every error set when it
+ * finishes, including errors of earlier "_device" queries on the scene.
+ * Returns when the hits are in the host array; the copies and the traversal
+ * run on `stream` (NULL = legacy default stream). */
 #define CR_NOALLOC_MAX_RAYS 65536u
 int cr_trace_closest_noalloc(cr_scene* scene, const cr_ray* rays, uint64_t n,
                              cr_hit* hits, void* stream);

@@ -188,3 +188,27 @@ def test_film_accumulates_and_clears(gpu_lib):
     assert not rgb.any() and not w.any()
     resolved = g.film_resolve()
     assert np.isnan(resolved).all()  # 0 / 0, as Sensor::createImage without a guard
+
+
+@pytest.mark.parametrize("spectral", [False, True])
+@pytest.mark.parametrize("wavefront", [True, False])
+def test_c1_config_equal_seed(gpu_lib, spectral, wavefront):
+    """The plain-method configuration the benchmark renders, exactly: the
+    procedural Cornell box (seed 0), 256 x 256, 16 spp, max depth 8, rr 0.05,
+    NEE + MIS, RGB and hero-wavelength spectral, on both schedules, against
+    the oracle at the same seed.  Equal seeds give the same paths until an
+    ulp difference of a transcendental flips a branch, so relMSE stays near
+    zero (bars as the smaller equal-seed tests: 1e-3 RGB, 2e-3 spectral);
+    ray counts agree within 2 % and film weights (the same jittered filter
+    positions) within float summation order."""
+    g, o, oc, cam = _cornell(256, 256, seed=0)
+    integ = PathTraceIntegrator(PathTraceIntegrator.Configs(maxDepth=8, rrThreshold=0.05, useMIS=True),
+                                compat=False, spectral=spectral, wavefront=wavefront)
+    integ.dispatch(g, 16)
+    img = cam.sensor.createImage()
+    (rgb, w), orays = o.render(oc, 8, 0.05, True, spp=16, spectral=spectral)
+    err = rel_mse(img, rgb / w[..., None])
+    assert err < (2e-3 if spectral else 1e-3), err
+    grays = g.render_ray_count()
+    assert abs(grays - orays) <= 0.02 * orays, (grays, orays)
+    np.testing.assert_allclose(cam.sensor.weight, w, rtol=1e-5)
