@@ -169,6 +169,7 @@ SIGNATURES = [
     ("cr_batch_autotune", ctypes.c_int, [_P, ctypes.POINTER(CrBatchTuning), _P, _U32,
                                          ctypes.POINTER(ctypes.c_uint32)]),
     ("cr_kernel_launch_count", ctypes.c_uint64, []),
+    ("cr_device_read_bandwidth", ctypes.c_int, [_U64, _U32, ctypes.POINTER(ctypes.c_double)]),
     ("cr_import_xml", ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p)]),
     ("cr_import_get", ctypes.c_int, [_P, ctypes.POINTER(CrImportView)]),
     ("cr_import_material_name", ctypes.c_char_p, [_P, _U32]),

@@ -23,7 +23,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off",
                      "-Xptxas", "-warn-spills", "-I", INCLUDE, "-I", CSRC]
 SOURCES = ["cr_core.cu", "cr_bvh.cu", "cr_trace.cu", "cr_render.cu", "cr_noalloc.cu", "cr_mlp.cu", "cr_cache.cu", "cr_batch.cu",
-           "cr_wavefront.cu", "cr_image.cpp", "cr_import.cpp"]
+           "cr_wavefront.cu", "cr_diag.cu", "cr_image.cpp", "cr_import.cpp"]
 
 
 def nvcc() -> str:

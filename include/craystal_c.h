@@ -565,6 +565,14 @@ int cr_batch_autotune(cr_batch* batch, cr_batch_tuning* best,
                       cr_batch_tuning_result* results, uint32_t max_results,
                       uint32_t* n_results);
 
+/* Read bandwidth (GB/s) of the memory level a buffer of `bytes` lives in:
+ * the buffer is read `passes` times by persistent blocks with 16-byte loads
+ * cached in L2 only, after one untimed pass; CUDA events time the passes.
+ * Below the L2 size this is the L2 read bandwidth, the peak the ray queries
+ * on L2-resident scenes are measured against; far above it, HBM's.  No
+ * counterpart in the reference (a measurement aid for the roofline). */
+int cr_device_read_bandwidth(uint64_t bytes, uint32_t passes, double* gbs);
+
 /* Number of kernel launches this library issued since the process started
  * (all entry points); for launch accounting in benchmarks. */
 uint64_t cr_kernel_launch_count(void);
