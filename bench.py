@@ -621,7 +621,8 @@ def mlp_extra(torch):
                            "frac": round(tr_tf / peak, 4)},
             "peak_tflops": peak, "peak_source": f"{src} dense bf16 (burst)",
             "instruction": {"inference": "tcgen05.mma kind::f16, M128, TMEM accumulators, weights by cp.async.bulk",
-                            "training": "mma.sync m16n8k16 FP16 with FP32 accumulation"}}
+                            "training": "tcgen05.mma kind::f16, M128: forward, backward data gradients and "
+                                        "MN-major weight gradients accumulated in TMEM over each CTA's tiles"}}
 
 
 def wavefront_extra(torch):
@@ -657,7 +658,7 @@ def wavefront_extra(torch):
     return out
 
 
-def large_scene_extra(torch, spp=32):
+def large_scene_extra(torch, spp=32, with_cache=True):
     """The large workload: a 4096 x 4096 fBm heightfield (33.5M triangles)
     plus 10k boxes, Principled materials, a sun sphere light and a constant
     sky, rendered at 3840 x 2160, 32 spp, max depth 12, NEE + MIS, on the
@@ -696,6 +697,7 @@ def large_scene_extra(torch, spp=32):
     # for parity below: the 1-spp film at sample index 0 and the GPU's tree
     film1 = gpu_film_1spp(integ, sc)
     gnodes, gmap = sc.bvh_export()
+    cached = c5_cache_equal_time(torch, sc, integ) if with_cache else None
     paths = 3840 * 2160 * spp
     out = {"config": "terrain 4096^2 (fBm, 6 octaves) + 10k boxes, 3840x2160, 32 spp, depth 12, sun + sky",
            "triangles": int(n_tris), "host_generation_s": round(gen_s, 2), "scene_create_s": round(create_s, 2),
@@ -727,7 +729,55 @@ def large_scene_extra(torch, spp=32):
                          "projected_render_s": round(paths / cpu_rate, 1)}
     del osc
     out["parity"] = crop_parity(None, None, orgb, ow, (1072, 1088), film=film1)
+    if cached is not None:
+        out["radiance_cache_equal_time"] = cached
     return out
+
+
+def c5_cache_equal_time(torch, sc, plain, rows=(824, 1336), ref_chunks=16, ref_spp=32, budgets=(32,), trials=3):
+    """The radiance cache on the large scene at full resolution (3840x2160,
+    depth 12): at equal time with the plain tracer's 32-spp render, relMSE
+    on a 512-row band at the image centre against a plain reference of
+    ref_chunks x ref_spp spp (FP64 film sum), whose own noise is estimated
+    from its two halves.  The cache trains from scratch inside its time on
+    2^16 path-suffix records per frame."""
+    from craystal_gb300.api import CachedPathTraceIntegrator, RadianceCache
+    cfg = plain.configs
+    r0, r1 = rows
+    halves = [[0.0, 0.0], [0.0, 0.0]]
+    for k in range(ref_chunks):
+        sc.film_clear()
+        plain.dispatch(sc, ref_spp, first_sample=1_000_000 + ref_spp * k, readback=False)
+        rgb, w = sc.film_read()
+        h = halves[k % 2]
+        h[0] = h[0] + rgb[r0:r1].astype(np.float64)
+        h[1] = h[1] + w[r0:r1].astype(np.float64)
+    ref = (halves[0][0] + halves[1][0]) / (halves[0][1] + halves[1][1])[..., None]
+    ha = halves[0][0] / halves[0][1][..., None]
+    hb = halves[1][0] / halves[1][1][..., None]
+    ref_noise = 0.25 * float(np.mean((ha - hb) ** 2 / (ref ** 2 + 1e-2)))
+
+    def crop_rel_mse(rgb, w):
+        img = np.nan_to_num((rgb[r0:r1] / w[r0:r1][..., None]).astype(np.float64))
+        return float(np.mean((img - ref) ** 2 / (ref ** 2 + 1e-2)))
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        fn()
+        torch.cuda.synchronize()
+        return time.perf_counter() - t
+
+    samples = 1 << 16
+    probe = CachedPathTraceIntegrator(cfg, train_samples=samples, cache=RadianceCache(seed=1))
+    probe.dispatch(sc, 8, first_sample=2_000_000, readback=False)
+    t_frame = timed(lambda: probe.dispatch(sc, 16, first_sample=3_000_000, readback=False)) / 16
+    rows_out = equal_time_trials(sc, cfg, plain, crop_rel_mse, timed, t_frame, budgets, trials=trials,
+                                 train_samples=samples)
+    return {"resolution": [3840, 2160], "crop_rows": [r0, r1], "reference_spp": ref_chunks * ref_spp,
+            "reference_noise_relmse": round(ref_noise, 6), "train_samples_per_frame": samples,
+            "ms_per_cached_frame": round(t_frame * 1e3, 3), "train_every_reached": int(probe.stats.last_train_every),
+            "budgets": rows_out}
 
 
 def compare_trees(gnodes, gmap, onodes, omap):

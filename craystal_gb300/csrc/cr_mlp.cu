@@ -18,15 +18,14 @@
 //              the next layer's FP16 operand.  Three tiles in flight per SM
 //              overlap one warpgroup's encoding and epilogue with another's
 //              MMAs.
-//   kTrainFwdBwd  training forward (mma.sync m16n8k16; one warp carries 16
-//              rows, activations in registers, every layer's input stored),
-//              then the loss gradient and the backward pass for the data
-//              gradients, storing every layer's output gradient dY.
-//   kWeightGrad   dW_l = X_l^T dY_l over the batch (split over CTAs,
-//              accumulated with atomics in FP32).
-//   kAdam      Adam on FP32 master weights; kPackWeights refreshes the three
-//              FP16 copies (n-major and k-major for training, core-matrix
-//              tiles for the tensor-core inference).
+//   kTrainTc   one training pass on the 5th-generation tensor cores: a
+//              persistent CTA per SM carries tiles of 128 records through the
+//              forward, the loss gradient, the backward data gradients and
+//              the weight gradients (the last accumulated in TMEM over all
+//              the CTA's tiles); kReduceGrad sums the CTAs' partials.
+//   kAdam      Adam on FP32 master weights; kPackWeights refreshes the FP16
+//              core-matrix tiles of the weights (W_l for the forward, W_l^T
+//              for the backward data gradients).
 
 #include <cstring>
 #include <vector>
@@ -47,7 +46,6 @@ constexpr int kFreq = 12;       // frequencies per input
 constexpr int kFeat = 176;      // encoded features: 7 * 12 * 2 = 168, padded
 constexpr int kHid = 64;
 constexpr int kLayers = 6;      // 5 hidden + output
-constexpr int kOutPad = 8;      // 3 outputs padded to one n8 tile
 // (K, N) of each layer's weight matrix
 __host__ __device__ constexpr int layerK(int l) { return l == 0 ? kFeat : kHid; }
 __host__ __device__ constexpr int layerN(int l) { return l == kLayers - 1 ? 3 : kHid; }
@@ -55,39 +53,7 @@ __host__ __device__ constexpr int layerN(int l) { return l == kLayers - 1 ? 3 : 
 __host__ __device__ constexpr int paramOffset(int l) { return l == 0 ? 0 : kFeat * kHid + (l - 1) * kHid * kHid; }
 constexpr int kParams = kFeat * kHid + 4 * kHid * kHid + kHid * 3;  // 27,840
 
-// FP16 forward copy (n-major, padded rows): WT_l[n][k], row stride K + 8
-// halves (the pad spreads the 8 rows a fragment load touches over distinct
-// shared-memory banks).  The output layer has 8 rows (3 real).
-__host__ __device__ constexpr int fwdStride(int l) { return layerK(l) + 8; }
-__host__ __device__ constexpr int fwdRows(int l) { return l == kLayers - 1 ? kOutPad : kHid; }
-__host__ __device__ constexpr int fwdOffset(int l) {
-    int o = 0;
-    for (int i = 0; i < l; i++) o += fwdRows(i) * fwdStride(i);
-    return o;
-}
-constexpr int kFwdHalves = fwdOffset(kLayers);
-// FP16 backward copy (k-major): W_l[k][n], row stride Npad + 8 with the
-// output layer's N padded to 16 (it is the K dimension of the backward MMA).
-__host__ __device__ constexpr int bwdCols(int l) { return l == kLayers - 1 ? 16 : kHid; }
-__host__ __device__ constexpr int bwdStride(int l) { return bwdCols(l) + 8; }
-__host__ __device__ constexpr int bwdOffset(int l) {
-    int o = 0;
-    for (int i = 0; i < l; i++) o += layerK(i) * bwdStride(i);
-    return o;
-}
-constexpr int kBwdHalves = bwdOffset(kLayers);
-
-constexpr int kWarps = 4;
 constexpr float kGradClip = 256.0f;  // |dL/dy| per sample and channel
-constexpr int kThreads = kWarps * 32;
-
-__device__ __forceinline__ void mma16816(float c[4], const uint32_t a[4], uint32_t b0, uint32_t b1) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-}
 
 __device__ __forceinline__ uint32_t pack2(float lo, float hi) {
     __half2 h = __floats2half2_rn(lo, hi);
@@ -115,291 +81,6 @@ __device__ __forceinline__ void doubleAngle(float& s, float& c) {
     const float c2 = (c - s) * (c + s);
     s = s2;
     c = c2;
-}
-
-// Encoded features j, j+1 (j even) of one query row.
-__device__ __forceinline__ uint32_t featurePair(const float* x, int j) {
-    if (j >= kIn * kFreq * 2) return 0u;
-    const int d = j / (kFreq * 2), f = (j % (kFreq * 2)) >> 1;
-    float s, c;
-    sincosBase(x[d], f & ~3, s, c);
-    for (int r = 0; r < (f & 3); r++) doubleAngle(s, c);
-    return pack2(s, c);
-}
-
-// A fragments of the encoded input for the 16 rows of a warp tile.
-__device__ __forceinline__ void encodeTile(const float xr0[kIn], const float xr1[kIn], uint32_t a[11][4]) {
-    const int tig = threadIdx.x & 3;
-#pragma unroll
-    for (int kt = 0; kt < 11; kt++) {
-        const int c = kt * 16 + tig * 2;
-        a[kt][0] = featurePair(xr0, c);
-        a[kt][1] = featurePair(xr1, c);
-        a[kt][2] = featurePair(xr0, c + 8);
-        a[kt][3] = featurePair(xr1, c + 8);
-    }
-}
-
-// One hidden / output layer: acc[nt] += A(16 x K) * W(K x N) for nTiles n-tiles.
-template <int KT, int NT>
-__device__ __forceinline__ void layerFwd(const __half* wt, int stride, const uint32_t (*a)[4], float acc[][4]) {
-    const int g = (threadIdx.x & 31) >> 2, tig = threadIdx.x & 3;
-#pragma unroll
-    for (int nt = 0; nt < NT; nt++) {
-        acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
-        const __half* row = wt + (nt * 8 + g) * stride + tig * 2;
-#pragma unroll
-        for (int kt = 0; kt < KT; kt++) {
-            const uint32_t b0 = *reinterpret_cast<const uint32_t*>(row + kt * 16);
-            const uint32_t b1 = *reinterpret_cast<const uint32_t*>(row + kt * 16 + 8);
-            mma16816(acc[nt], a[kt], b0, b1);
-        }
-    }
-}
-
-// ReLU of 8 n-tiles of accumulators into the A fragments of 4 k-tiles.
-__device__ __forceinline__ void reluToA(const float acc[8][4], uint32_t a[4][4]) {
-#pragma unroll
-    for (int kt = 0; kt < 4; kt++) {
-        a[kt][0] = pack2(fmaxf(acc[2 * kt][0], 0.0f), fmaxf(acc[2 * kt][1], 0.0f));
-        a[kt][1] = pack2(fmaxf(acc[2 * kt][2], 0.0f), fmaxf(acc[2 * kt][3], 0.0f));
-        a[kt][2] = pack2(fmaxf(acc[2 * kt + 1][0], 0.0f), fmaxf(acc[2 * kt + 1][1], 0.0f));
-        a[kt][3] = pack2(fmaxf(acc[2 * kt + 1][2], 0.0f), fmaxf(acc[2 * kt + 1][3], 0.0f));
-    }
-}
-
-__device__ void loadFwdWeights(const __half* __restrict__ g, __half* s) {
-    const int n = kFwdHalves / 8;  // 16-byte chunks
-    for (int i = threadIdx.x; i < n; i += blockDim.x)
-        reinterpret_cast<uint4*>(s)[i] = reinterpret_cast<const uint4*>(g)[i];
-}
-
-// Stores the A fragments of a layer input (16 rows x 16*KT halves) at rows
-// [row0, row0+16) of a row-major FP16 matrix with the given stride.
-template <int KT>
-__device__ __forceinline__ void storeA(const uint32_t (*a)[4], __half* m, int stride, uint64_t row0, uint64_t n) {
-    const int g = (threadIdx.x & 31) >> 2, tig = threadIdx.x & 3;
-    const uint64_t r0 = row0 + g, r1 = row0 + g + 8;
-#pragma unroll
-    for (int kt = 0; kt < KT; kt++) {
-        const int c = kt * 16 + tig * 2;
-        if (r0 < n) {
-            *reinterpret_cast<uint32_t*>(m + r0 * stride + c) = a[kt][0];
-            *reinterpret_cast<uint32_t*>(m + r0 * stride + c + 8) = a[kt][2];
-        }
-        if (r1 < n) {
-            *reinterpret_cast<uint32_t*>(m + r1 * stride + c) = a[kt][1];
-            *reinterpret_cast<uint32_t*>(m + r1 * stride + c + 8) = a[kt][3];
-        }
-    }
-}
-
-__device__ __forceinline__ void loadInputs(const float* __restrict__ in, uint64_t n, uint64_t row, float x[kIn]) {
-#pragma unroll
-    for (int d = 0; d < kIn; d++) x[d] = row < n ? in[row * kIn + d] : 0.0f;
-}
-
-// Full forward for the warp's 16 rows; returns the output accumulators
-// (16 x 8; columns 0..2 are RGB).  When act != nullptr the input of every
-// layer is stored (layer 0: kFeat halves per row, others kHid).
-__device__ void forwardTile(const __half* sw, const float* __restrict__ in, uint64_t n, uint64_t row0,
-                            float out[4], __half* const* act) {
-    const int g = (threadIdx.x & 31) >> 2;
-    float x0[kIn], x1[kIn];
-    loadInputs(in, n, row0 + g, x0);
-    loadInputs(in, n, row0 + g + 8, x1);
-    uint32_t a0[11][4];
-    encodeTile(x0, x1, a0);
-    if (act) storeA<11>(a0, act[0], kFeat, row0, n);
-    float acc[8][4];
-    layerFwd<11, 8>(sw + fwdOffset(0), fwdStride(0), a0, acc);
-    uint32_t a[4][4];
-    reluToA(acc, a);
-#pragma unroll 1
-    for (int l = 1; l < kLayers - 1; l++) {
-        if (act) storeA<4>(a, act[l], kHid, row0, n);
-        layerFwd<4, 8>(sw + fwdOffset(l), fwdStride(l), a, acc);
-        reluToA(acc, a);
-    }
-    if (act) storeA<4>(a, act[kLayers - 1], kHid, row0, n);
-    float o[1][4];
-    layerFwd<4, 1>(sw + fwdOffset(kLayers - 1), fwdStride(kLayers - 1), a, o);
-    out[0] = o[0][0];
-    out[1] = o[0][1];
-    out[2] = o[0][2];
-    out[3] = o[0][3];
-}
-
-struct Acts {
-    __half* act[kLayers];   // inputs of each layer: [n][K_l]
-    __half* dy[kLayers];    // output gradients of each layer: [n][Npad_l] (Npad = 64, or 16 for the output)
-};
-
-// dX (16 x K) = dY (16 x N) * W^T, with W k-major [K][Npad] in shared memory;
-// KT_N = k-tiles over N, NT_K = n-tiles over K.
-template <int KT_N, int NT_K>
-__device__ __forceinline__ void layerBwd(const __half* wk, int stride, const uint32_t (*dy)[4], float acc[][4]) {
-    const int g = (threadIdx.x & 31) >> 2, tig = threadIdx.x & 3;
-#pragma unroll
-    for (int nt = 0; nt < NT_K; nt++) {
-        acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
-        const __half* row = wk + (nt * 8 + g) * stride + tig * 2;
-#pragma unroll
-        for (int kt = 0; kt < KT_N; kt++) {
-            const uint32_t b0 = *reinterpret_cast<const uint32_t*>(row + kt * 16);
-            const uint32_t b1 = *reinterpret_cast<const uint32_t*>(row + kt * 16 + 8);
-            mma16816(acc[nt], dy[kt], b0, b1);
-        }
-    }
-}
-
-// Loads the A fragments (16 rows x 64) of a stored activation.
-__device__ __forceinline__ void loadA4(const __half* m, uint64_t row0, uint64_t n, uint32_t a[4][4]) {
-    const int g = (threadIdx.x & 31) >> 2, tig = threadIdx.x & 3;
-    const uint64_t r0 = row0 + g, r1 = row0 + g + 8;
-#pragma unroll
-    for (int kt = 0; kt < 4; kt++) {
-        const int c = kt * 16 + tig * 2;
-        a[kt][0] = r0 < n ? *reinterpret_cast<const uint32_t*>(m + r0 * kHid + c) : 0u;
-        a[kt][2] = r0 < n ? *reinterpret_cast<const uint32_t*>(m + r0 * kHid + c + 8) : 0u;
-        a[kt][1] = r1 < n ? *reinterpret_cast<const uint32_t*>(m + r1 * kHid + c) : 0u;
-        a[kt][3] = r1 < n ? *reinterpret_cast<const uint32_t*>(m + r1 * kHid + c + 8) : 0u;
-    }
-}
-
-// dY of the layer below: dX masked by the ReLU of that layer's output (the
-// stored input of this layer), packed as A fragments.
-__device__ __forceinline__ void maskToA(const float acc[8][4], const uint32_t act[4][4], uint32_t dy[4][4]) {
-#pragma unroll
-    for (int kt = 0; kt < 4; kt++) {
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            const float2 av = unpack2(act[kt][q]);
-            const int nt = 2 * kt + (q >> 1), e = (q & 1) * 2;
-            dy[kt][q] = pack2(av.x > 0.0f ? acc[nt][e] : 0.0f, av.y > 0.0f ? acc[nt][e + 1] : 0.0f);
-        }
-    }
-}
-
-__global__ void __launch_bounds__(kThreads) kTrainFwdBwd(const __half* __restrict__ wFwd,
-                                                         const __half* __restrict__ wBwd,
-                                                         const float* __restrict__ in,
-                                                         const float* __restrict__ target, uint64_t n, Acts acts,
-                                                         float* __restrict__ lossSum) {
-    extern __shared__ __align__(16) __half smem[];
-    __half* sf = smem;
-    __half* sb = smem + kFwdHalves;
-    loadFwdWeights(wFwd, sf);
-    for (int i = threadIdx.x; i < kBwdHalves / 8; i += blockDim.x)
-        reinterpret_cast<uint4*>(sb)[i] = reinterpret_cast<const uint4*>(wBwd)[i];
-    __syncthreads();
-    const int g = (threadIdx.x & 31) >> 2, tig = threadIdx.x & 3;
-    const uint64_t warpsTotal = (uint64_t)gridDim.x * kWarps;
-    const uint64_t w = (uint64_t)blockIdx.x * kWarps + (threadIdx.x >> 5);
-    float lossLocal = 0.0f;
-    for (uint64_t row0 = w * 16; row0 < n; row0 += warpsTotal * 16) {
-        float o[4];
-        forwardTile(sf, in, n, row0, o, acts.act);
-        // relative L2 loss (y - t)^2 / (sg(y)^2 + 0.01) and its gradient
-        // 2 (y - t) / (y^2 + 0.01); the 1 / (3 n) of the mean is applied to dW
-        uint32_t dy[1][4];
-        float d[4];
-        for (int q = 0; q < 4; q++) {
-            const uint64_t r = row0 + g + (q >= 2 ? 8 : 0);
-            const int col = tig * 2 + (q & 1);
-            d[q] = 0.0f;
-            if (r < n && col < 3) {
-                const float y = o[q], t = target[r * 3 + col];
-                const float den = y * y + 0.01f;
-                // per-sample gradient clipped to +-kGradClip: the relative loss
-                // gradient of a far-off prediction (y ~ 0, t large) would
-                // otherwise overflow the FP16 gradient path
-                d[q] = fminf(fmaxf(2.0f * (y - t) / den, -kGradClip), kGradClip);
-                lossLocal += (y - t) * (y - t) / den;
-            }
-        }
-        // output dY (16 x 8) as the A fragment of a 16 x 16 k-tile (cols 8..15 zero)
-        dy[0][0] = pack2(d[0], d[1]);
-        dy[0][1] = pack2(d[2], d[3]);
-        dy[0][2] = 0u;
-        dy[0][3] = 0u;
-        {
-            const uint64_t r0 = row0 + g, r1 = row0 + g + 8;
-            if (r0 < n) *reinterpret_cast<uint32_t*>(acts.dy[kLayers - 1] + r0 * 16 + tig * 2) = dy[0][0];
-            if (r1 < n) *reinterpret_cast<uint32_t*>(acts.dy[kLayers - 1] + r1 * 16 + tig * 2) = dy[0][1];
-            if (r0 < n) *reinterpret_cast<uint32_t*>(acts.dy[kLayers - 1] + r0 * 16 + 8 + tig * 2) = 0u;
-            if (r1 < n) *reinterpret_cast<uint32_t*>(acts.dy[kLayers - 1] + r1 * 16 + 8 + tig * 2) = 0u;
-        }
-        float acc[8][4];
-        layerBwd<1, 8>(sb + bwdOffset(kLayers - 1), bwdStride(kLayers - 1), dy, acc);
-        uint32_t a[4][4], g4[4][4];
-        loadA4(acts.act[kLayers - 1], row0, n, a);
-        maskToA(acc, a, g4);
-#pragma unroll 1
-        for (int l = kLayers - 2; l >= 1; l--) {
-            storeA<4>(g4, acts.dy[l], kHid, row0, n);
-            layerBwd<4, 8>(sb + bwdOffset(l), bwdStride(l), g4, acc);
-            loadA4(acts.act[l], row0, n, a);
-            maskToA(acc, a, g4);
-        }
-        storeA<4>(g4, acts.dy[0], kHid, row0, n);
-    }
-    for (int o = 16; o > 0; o >>= 1) lossLocal += __shfl_xor_sync(0xffffffffu, lossLocal, o);
-    if ((threadIdx.x & 31) == 0) atomicAdd(lossSum, lossLocal);
-}
-
-// dW_l[k][n] += scale * sum_b act_l[b][k] * dY_l[b][n] over a chunk of rows.
-constexpr int kGradRows = 64;
-template <int K, int NP>
-__global__ void __launch_bounds__(256) kWeightGrad(const __half* __restrict__ act, const __half* __restrict__ dy,
-                                                   uint64_t n, int nReal, float scale, float* __restrict__ dW) {
-    __shared__ __align__(16) __half sa[kGradRows][K + 8];
-    __shared__ __align__(16) __half sd[kGradRows][NP + 8];
-    const uint64_t row0 = (uint64_t)blockIdx.x * kGradRows;
-    for (int i = threadIdx.x; i < kGradRows * K / 2; i += blockDim.x) {
-        const int r = i / (K / 2), c = (i % (K / 2)) * 2;
-        const uint64_t gr = row0 + r;
-        *reinterpret_cast<uint32_t*>(&sa[r][c]) = gr < n ? *reinterpret_cast<const uint32_t*>(act + gr * K + c) : 0u;
-    }
-    for (int i = threadIdx.x; i < kGradRows * NP / 2; i += blockDim.x) {
-        const int r = i / (NP / 2), c = (i % (NP / 2)) * 2;
-        const uint64_t gr = row0 + r;
-        *reinterpret_cast<uint32_t*>(&sd[r][c]) = gr < n ? *reinterpret_cast<const uint32_t*>(dy + gr * NP + c) : 0u;
-    }
-    __syncthreads();
-    const int warp = threadIdx.x >> 5, g = (threadIdx.x & 31) >> 2, tig = threadIdx.x & 3;
-    constexpr int MT = K / 16, NT = (NP + 7) / 8;
-    for (int tile = warp; tile < MT * NT; tile += 8) {
-        const int mt = tile / NT, nt = tile % NT;
-        float c[4] = {0, 0, 0, 0};
-        for (int kb = 0; kb < kGradRows; kb += 16) {
-            // A = act^T (m = feature, k = batch row); B = dY (k = batch row, n)
-            uint32_t a[4];
-            const int m0 = mt * 16 + g, kr = kb + tig * 2;
-            auto pk = [&](int m, int r) {
-                __half2 h;
-                h.x = sa[r][m];
-                h.y = sa[r + 1][m];
-                return *reinterpret_cast<uint32_t*>(&h);
-            };
-            a[0] = pk(m0, kr);
-            a[1] = pk(m0 + 8, kr);
-            a[2] = pk(m0, kr + 8);
-            a[3] = pk(m0 + 8, kr + 8);
-            const int nn = nt * 8 + g;
-            __half2 h0, h1;
-            h0.x = sd[kr][nn];
-            h0.y = sd[kr + 1][nn];
-            h1.x = sd[kr + 8][nn];
-            h1.y = sd[kr + 9][nn];
-            mma16816(c, a, *reinterpret_cast<uint32_t*>(&h0), *reinterpret_cast<uint32_t*>(&h1));
-        }
-        // c: rows (m = mt*16 + g, +8), cols (n = nt*8 + tig*2, +1)
-        for (int q = 0; q < 4; q++) {
-            const int m = mt * 16 + g + (q >= 2 ? 8 : 0), col = nt * 8 + tig * 2 + (q & 1);
-            if (col < nReal) atomicAdd(dW + m * nReal + col, c[q] * scale);
-        }
-    }
 }
 
 // ---------------------------------------------------------------------------
@@ -510,6 +191,30 @@ __device__ __forceinline__ bool wgAnd(int g, bool v) {
     return r != 0;
 }
 
+// Encodes row `row` of the inputs (zeros past n) into row lt of a layer-0
+// operand at sA: chunk 3d + q holds f = 4q .. 4q+3 of input d; chunk 21
+// (features 168..175) is zero.
+__device__ __forceinline__ void encodeRowTc(const float* __restrict__ in, uint64_t n, uint64_t row, uint32_t sA,
+                                            int lt) {
+#pragma unroll 1
+    for (int d = 0; d < kIn; d++) {
+        const float xd = row < n ? in[row * kIn + d] : 0.0f;
+#pragma unroll
+        for (int q = 0; q < kFreq / 4; q++) {
+            float sn, cs;
+            sincosBase(xd, 4 * q, sn, cs);
+            uint32_t v[4];
+#pragma unroll
+            for (int r = 0; r < 4; r++) {
+                if (r) doubleAngle(sn, cs);
+                v[r] = pack2(sn, cs);
+            }
+            stShared4(sA + (d * 3 + q) * 2048 + lt * 16, v[0], v[1], v[2], v[3]);
+        }
+    }
+    stShared4(sA + (kFeat / 8 - 1) * 2048 + lt * 16, 0u, 0u, 0u, 0u);
+}
+
 // Persistent: CTA b's warpgroup g takes tiles b * kSlots + g, stepping by
 // gridDim.x * kSlots.  A wait that runs out (it should never) sets bit 0 of
 // *err, ends the warpgroup's loop and still frees the TMEM.
@@ -552,25 +257,8 @@ __global__ void __launch_bounds__(kTile * kSlots, 1) kInferTc(const uint8_t* __r
     uint32_t phase = 0;
     const uint64_t tiles = (n + kTile - 1) / kTile;
     for (uint64_t tile = (uint64_t)blockIdx.x * kSlots + g; ok && tile < tiles; tile += (uint64_t)gridDim.x * kSlots) {
-        // encode this thread's row: chunk 3d + q holds f = 4q .. 4q+3 of input d
         const uint64_t row = tile * kTile + lt;
-#pragma unroll 1
-        for (int d = 0; d < kIn; d++) {
-            const float xd = row < n ? in[row * kIn + d] : 0.0f;
-#pragma unroll
-            for (int q = 0; q < kFreq / 4; q++) {
-                float sn, cs;
-                sincosBase(xd, 4 * q, sn, cs);
-                uint32_t v[4];
-#pragma unroll
-                for (int r = 0; r < 4; r++) {
-                    if (r) doubleAngle(sn, cs);
-                    v[r] = pack2(sn, cs);
-                }
-                stShared4(sA + (d * 3 + q) * 2048 + lt * 16, v[0], v[1], v[2], v[3]);
-            }
-        }
-        stShared4(sA + (kFeat / 8 - 1) * 2048 + lt * 16, 0u, 0u, 0u, 0u);  // features 168..175
+        encodeRowTc(in, n, row, sA, lt);
         proxyFence();
         tcBefore();
         wgSync(g);
@@ -632,6 +320,302 @@ __global__ void __launch_bounds__(kTile * kSlots, 1) kInferTc(const uint8_t* __r
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmemBase), "r"(kTcCols) : "memory");
 }
 
+// ---------------------------------------------------------------------------
+// training on the tensor cores (tcgen05)
+// ---------------------------------------------------------------------------
+// One persistent CTA per SM with one warpgroup; thread t owns record t of
+// the current tile of 128.  Per tile:
+//   forward   Y_l = A_l W_l for l = 0..5 (M 128 records, N 64 / 16, K the
+//             layer's inputs), ReLU into A_{l+1}; all six inputs stay in
+//             shared memory in the inference kernel's core-matrix layout;
+//   loss      dY_5 = clip(2 (y - t) / (y^2 + 0.01)) (FP16, 16 columns);
+//   backward  for l = 5..1: dW_l += A_l^T dY_l and dA_l = dY_l W_l^T, then
+//             dY_{l-1} = dA_l * (A_l > 0) is written over A_l, which the
+//             weight-gradient MMA no longer needs; finally dW_0 += A_0^T dY_0.
+// The weight gradients are MMAs with M = 128 input features (layers with 64
+// read 64 features of the next buffer into rows that are never used), N =
+// the layer's outputs and K = 128 records.  Their operands are the same
+// tiles read MN-major: a core matrix of the record-major layout holds 8
+// records x 8 features, which is the MN-major core matrix of the transpose.
+// For these MN-major operands the descriptor's leading-dimension offset is
+// the stride between core matrices along K (8 records, 128 B) and its
+// stride-dimension offset the stride along M or N (8 features, 2048 B), the
+// same roles the two offsets have for K-major operands (found on GB300: the
+// other assignment gives wrong gradients; both stay inside the allocation).
+// The dW accumulators stay in TMEM across all the CTA's tiles (400 of its
+// 512 columns) and are written once per CTA as FP32 partials; kReduceGrad
+// sums the partials of all CTAs.  Every wait is bounded: one that runs out
+// sets bit 1 of *err, ends the loop, and the TMEM is still freed.
+constexpr int kTrThreads = 128;
+constexpr int kTrChunk = kTile * 16;  // 8 features of 128 records: 2048 B
+// backward-data weights, B = W_l^T as N = 64 inputs x K = outputs (16 for the
+// output layer), K-major core matrices; layer 0 needs none
+__host__ __device__ constexpr int bwdKpad(int l) { return l == kLayers - 1 ? 16 : kHid; }
+__host__ __device__ constexpr int tcBwdBytes(int l) { return l == 0 ? 0 : kHid * bwdKpad(l) * 2; }
+__host__ __device__ constexpr int tcBwdOffset(int l) {
+    int o = 0;
+    for (int i = 1; i < l; i++) o += tcBwdBytes(i);
+    return o;
+}
+constexpr int kTcBwdBytes = tcBwdOffset(kLayers);  // 34,816
+// shared memory: layer inputs (A_0: 22 chunks, A_1..A_5: 8 chunks each), the
+// output layer's dY (2 chunks), forward and backward weights, barriers
+__host__ __device__ constexpr int trA(int l) { return l == 0 ? 0 : (kFeat / 8) * kTrChunk + (l - 1) * 8 * kTrChunk; }
+constexpr int kTrDy5 = trA(kLayers);
+constexpr int kTrWf = kTrDy5 + 2 * kTrChunk;
+constexpr int kTrWb = kTrWf + kTcWeightBytes;
+constexpr int kTrBar = kTrWb + kTcBwdBytes;
+// 4 KB past the barriers, as for inference: operand reads stay inside the
+// allocation under either reading of the descriptors' two strides
+constexpr int kTrSmem = kTrBar + 64 + 4096;
+static_assert(kTrSmem <= 232448, "tensor-core training shared memory");
+// TMEM columns: the forward / backward-data accumulator, then dW per layer
+// (layer 0 in two groups of 128 input features)
+constexpr uint32_t kTrCols = 512;
+__host__ __device__ constexpr uint32_t trDwCol(int l, int grp) {
+    return l == 0 ? 64u + 64u * (uint32_t)grp : (l < kLayers - 1 ? 192u + 64u * (uint32_t)(l - 1) : 448u);
+}
+static_assert(trDwCol(kLayers - 1, 0) + 16 <= kTrCols, "TMEM columns");
+constexpr uint32_t kTcMnA = 1u << 15, kTcMnB = 1u << 16;  // MN-major A / B in the instruction descriptor
+
+__device__ __forceinline__ void ldShared4(uint32_t addr, uint32_t v[4]) {
+    asm volatile("ld.shared.v4.b32 {%0,%1,%2,%3}, [%4];" : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]) : "r"(addr)
+                 : "memory");
+}
+
+__global__ void __launch_bounds__(kTrThreads, 1) kTrainTc(const uint8_t* __restrict__ wTc,
+                                                          const uint8_t* __restrict__ wTcT,
+                                                          const float* __restrict__ in,
+                                                          const float* __restrict__ target, uint64_t n,
+                                                          float* __restrict__ part, float* __restrict__ lossSum,
+                                                          uint32_t* __restrict__ err) {
+    extern __shared__ __align__(1024) uint8_t sm[];
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const uint32_t base = smemAddr(sm);
+    const uint32_t barW = base + kTrBar, barM = barW + 8, slot = barW + 16;
+    if (tid == 0) {
+        mbarInit(barW, 1);
+        mbarInit(barM, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot), "r"(kTrCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tcBefore();
+    __syncthreads();
+    tcAfter();
+    const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(sm + kTrBar + 16);
+    const uint32_t tq = tmem + ((uint32_t)(warp * 32) << 16);  // this warp's lanes (records, or features for dW)
+    if (tid == 0) {
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(barW),
+                     "r"((uint32_t)(kTcWeightBytes + kTcBwdBytes))
+                     : "memory");
+        for (int off = 0; off < kTcWeightBytes; off += 8192) {
+            const uint32_t bytes = (uint32_t)(kTcWeightBytes - off < 8192 ? kTcWeightBytes - off : 8192);
+            asm volatile(
+                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                    base + kTrWf + off),
+                "l"(wTc + off), "r"(bytes), "r"(barW)
+                : "memory");
+        }
+        for (int off = 0; off < kTcBwdBytes; off += 8192) {
+            const uint32_t bytes = (uint32_t)(kTcBwdBytes - off < 8192 ? kTcBwdBytes - off : 8192);
+            asm volatile(
+                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                    base + kTrWb + off),
+                "l"(wTcT + off), "r"(bytes), "r"(barW)
+                : "memory");
+        }
+    }
+    bool ok = __syncthreads_and(mbarWait(barW, 0));
+    uint32_t phase = 0;
+    float lossLocal = 0.0f;
+    // waits for the MMAs committed so far; false when the wait runs out
+    auto waitMma = [&]() {
+        const bool done = __syncthreads_and(mbarWait(barM, phase));
+        phase ^= 1u;
+        tcAfter();
+        return done;
+    };
+    const uint64_t tiles = (n + kTile - 1) / kTile;
+    bool first = true;
+    for (uint64_t tile = blockIdx.x; ok && tile < tiles; tile += gridDim.x) {
+        const uint64_t row = tile * kTile + tid;
+        encodeRowTc(in, n, row, base + trA(0), tid);
+        proxyFence();
+        tcBefore();
+        __syncthreads();
+        // forward
+#pragma unroll 1
+        for (int l = 0; ok && l < kLayers; l++) {
+            if (tid == 0) {
+                tcAfter();
+                const int K = layerK(l), Np = layerNpad(l);
+                const uint32_t idesc = tcInstr(kTile, Np), wl = base + kTrWf + tcOffset(l);
+                for (int k = 0; k < K / 16; k++)
+                    tcMma(tmem, tcDesc(base + trA(l) + k * 2 * kTrChunk, kTrChunk, 128),
+                          tcDesc(wl + k * 2 * (Np * 16), Np * 16, 128), idesc, k > 0 ? 1u : 0u);
+                tcCommit(barM);
+            }
+            ok = waitMma();
+            if (!ok) break;
+            if (l < kLayers - 1) {
+                const uint32_t dst = base + trA(l + 1) + tid * 16;
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    uint32_t v[32];
+                    tcLoad32(tq + h * 32, v);
+                    tcLoadWait();
+#pragma unroll
+                    for (int c = 0; c < 4; c++) {
+                        uint32_t q[4];
+#pragma unroll
+                        for (int e = 0; e < 4; e++)
+                            q[e] = pack2(fmaxf(__uint_as_float(v[c * 8 + 2 * e]), 0.0f),
+                                         fmaxf(__uint_as_float(v[c * 8 + 2 * e + 1]), 0.0f));
+                        stShared4(dst + (h * 4 + c) * kTrChunk, q[0], q[1], q[2], q[3]);
+                    }
+                }
+            } else {
+                // relative L2 loss (y - t)^2 / (sg(y)^2 + 0.01) and its gradient
+                // 2 (y - t) / (y^2 + 0.01), clipped to +-kGradClip so that the FP16
+                // gradient path stays finite; the 1 / (3 n) of the mean is applied
+                // when the partials are summed
+                uint32_t v[4];
+                tcLoad4(tq, v);
+                tcLoadWait();
+                float d[3] = {0.0f, 0.0f, 0.0f};
+                if (row < n) {
+#pragma unroll
+                    for (int c = 0; c < 3; c++) {
+                        const float y = __uint_as_float(v[c]), t = target[row * 3 + c];
+                        const float den = y * y + 0.01f;
+                        d[c] = fminf(fmaxf(2.0f * (y - t) / den, -kGradClip), kGradClip);
+                        lossLocal += (y - t) * (y - t) / den;
+                    }
+                }
+                stShared4(base + kTrDy5 + tid * 16, pack2(d[0], d[1]), pack2(d[2], 0.0f), 0u, 0u);
+                stShared4(base + kTrDy5 + kTrChunk + tid * 16, 0u, 0u, 0u, 0u);
+            }
+            proxyFence();
+            tcBefore();
+            __syncthreads();
+        }
+        // backward: weight and data gradients, layers 5..1
+#pragma unroll 1
+        for (int l = kLayers - 1; ok && l >= 1; l--) {
+            const uint32_t dy = l == kLayers - 1 ? base + kTrDy5 : base + trA(l + 1);  // dY_l
+            const int Nl = bwdKpad(l);
+            if (tid == 0) {
+                tcAfter();
+                const uint32_t idw = tcInstr(kTile, Nl) | kTcMnA | kTcMnB;
+                for (int k = 0; k < kTile / 16; k++)
+                    tcMma(tmem + trDwCol(l, 0), tcDesc(base + trA(l) + k * 256, 128, kTrChunk),
+                          tcDesc(dy + k * 256, 128, kTrChunk), idw, (first && k == 0) ? 0u : 1u);
+                const uint32_t wb = base + kTrWb + tcBwdOffset(l);
+                for (int k = 0; k < Nl / 16; k++)
+                    tcMma(tmem, tcDesc(dy + k * 2 * kTrChunk, kTrChunk, 128), tcDesc(wb + k * 2 * 1024, 1024, 128),
+                          tcInstr(kTile, kHid), k > 0 ? 1u : 0u);
+                tcCommit(barM);
+            }
+            ok = waitMma();
+            if (!ok) break;
+            const uint32_t a = base + trA(l) + tid * 16;
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                uint32_t v[32];
+                tcLoad32(tq + h * 32, v);
+                tcLoadWait();
+#pragma unroll
+                for (int c = 0; c < 4; c++) {
+                    uint32_t act[4], q[4];
+                    ldShared4(a + (h * 4 + c) * kTrChunk, act);
+#pragma unroll
+                    for (int e = 0; e < 4; e++) {
+                        const float2 av = unpack2(act[e]);
+                        q[e] = pack2(av.x > 0.0f ? __uint_as_float(v[c * 8 + 2 * e]) : 0.0f,
+                                     av.y > 0.0f ? __uint_as_float(v[c * 8 + 2 * e + 1]) : 0.0f);
+                    }
+                    stShared4(a + (h * 4 + c) * kTrChunk, q[0], q[1], q[2], q[3]);
+                }
+            }
+            proxyFence();
+            tcBefore();
+            __syncthreads();
+        }
+        if (!ok) break;
+        // dW_0 += A_0^T dY_0 (dY_0 is over A_1), input features in two groups of 128
+        if (tid == 0) {
+            tcAfter();
+            const uint32_t idw = tcInstr(kTile, kHid) | kTcMnA | kTcMnB;
+            for (int grp = 0; grp < 2; grp++)
+                for (int k = 0; k < kTile / 16; k++)
+                    tcMma(tmem + trDwCol(0, grp), tcDesc(base + trA(0) + grp * 16 * kTrChunk + k * 256, 128, kTrChunk),
+                          tcDesc(base + trA(1) + k * 256, 128, kTrChunk), idw, (first && k == 0) ? 0u : 1u);
+            tcCommit(barM);
+        }
+        ok = waitMma();
+        tcBefore();
+        __syncthreads();
+        first = false;
+    }
+    tcBefore();
+    __syncthreads();
+    tcAfter();
+    // this CTA's dW partials: lane = input feature, column = output
+    if (ok) {
+        float* p = part + (size_t)blockIdx.x * kParams;
+        const int lane = tid & 31;
+#pragma unroll 1
+        for (int l = 0; l < kLayers; l++) {
+            const int groups = l == 0 ? 2 : 1, N = layerN(l);
+            for (int grp = 0; grp < groups; grp++) {
+                const int k = grp * 128 + warp * 32 + lane;
+                const bool valid = k < layerK(l);
+                const uint32_t col = tq + trDwCol(l, grp);
+                if (l < kLayers - 1) {
+#pragma unroll
+                    for (int h = 0; h < 2; h++) {
+                        uint32_t v[32];
+                        tcLoad32(col + h * 32, v);
+                        tcLoadWait();
+                        if (valid) {
+                            float* dst = p + paramOffset(l) + k * N + h * 32;
+#pragma unroll
+                            for (int j = 0; j < 32; j++) dst[j] = __uint_as_float(v[j]);
+                        }
+                    }
+                } else {
+                    uint32_t v[4];
+                    tcLoad4(col, v);
+                    tcLoadWait();
+                    if (valid)
+                        for (int j = 0; j < 3; j++) p[paramOffset(l) + k * 3 + j] = __uint_as_float(v[j]);
+                }
+            }
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) lossLocal += __shfl_xor_sync(0xffffffffu, lossLocal, o);
+    if ((tid & 31) == 0) atomicAdd(lossSum, lossLocal);
+    tcBefore();
+    __syncthreads();
+    tcAfter();
+    if (!ok && tid == 0) atomicOr(err, 2u);
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTrCols) : "memory");
+}
+
+// grad += scale * (sum of the CTAs' partials), one thread per parameter
+__global__ void kReduceGrad(const float* __restrict__ part, int parts, float scale, float* __restrict__ grad) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kParams) return;
+    float s = 0.0f;
+    for (int b = 0; b < parts; b++) s += part[(size_t)b * kParams + i];
+    grad[i] += s * scale;
+}
+
 __global__ void kAdam(float* __restrict__ w, float* __restrict__ m, float* __restrict__ v, float* __restrict__ grad,
                       int count, float lr, float b1, float b2, float eps, float c1, float c2) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -645,11 +629,10 @@ __global__ void kAdam(float* __restrict__ w, float* __restrict__ m, float* __res
     grad[i] = 0.0f;
 }
 
-// Refreshes the FP16 copies: forward (n-major) and backward (k-major) for
-// training, core-matrix tiles for the tensor-core inference (its padding,
-// zeroed once, is never written).
-__global__ void kPackWeights(const float* __restrict__ w, __half* __restrict__ fwd, __half* __restrict__ bwd,
-                             __half* __restrict__ tc) {
+// Refreshes the FP16 core-matrix tiles of the weights: W_l for inference and
+// the training forward, W_l^T for the training backward (the padding, zeroed
+// once, is never written).
+__global__ void kPackWeights(const float* __restrict__ w, __half* __restrict__ tc, __half* __restrict__ tcT) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kParams) return;
     int l = 0;
@@ -657,9 +640,9 @@ __global__ void kPackWeights(const float* __restrict__ w, __half* __restrict__ f
     const int N = layerN(l);
     const int local = i - paramOffset(l), k = local / N, n = local % N;
     const __half h = __float2half_rn(w[i]);
-    fwd[fwdOffset(l) + n * fwdStride(l) + k] = h;
-    bwd[bwdOffset(l) + k * bwdStride(l) + n] = h;
     tc[(tcOffset(l) + ((k >> 3) * (layerNpad(l) >> 3) + (n >> 3)) * 128 + (n & 7) * 16 + (k & 7) * 2) / 2] = h;
+    // backward-data operand W_l^T: N = input k, K = output n
+    if (l > 0) tcT[(tcBwdOffset(l) + ((n >> 3) * (kHid >> 3) + (k >> 3)) * 128 + (k & 7) * 16 + (n & 7) * 2) / 2] = h;
 }
 
 inline unsigned cdiv(uint64_t a, uint64_t b) { return (unsigned)((a + b - 1) / b); }
@@ -677,13 +660,10 @@ struct MlpState {
     float* v = nullptr;
     float* grad = nullptr;
     float* loss = nullptr;
-    __half* wFwd = nullptr;
-    __half* wBwd = nullptr;
-    __half* wTc = nullptr;      // inference operand tiles (kTcWeightBytes)
+    __half* wTc = nullptr;      // inference and training forward operand tiles (kTcWeightBytes)
+    __half* wTcT = nullptr;     // training backward-data operand tiles (kTcBwdBytes)
+    float* part = nullptr;      // per-CTA weight-gradient partials of the training kernel (sms x kParams)
     uint32_t* err = nullptr;    // bit 0: a tensor-core wait ran out
-    uint64_t cap = 0;       // rows of the training buffers
-    __half* act[kLayers] = {};
-    __half* dy[kLayers] = {};
     float* stageIn = nullptr;
     float* stageOut = nullptr;
     uint64_t stageCap = 0;
@@ -692,21 +672,6 @@ struct MlpState {
 };
 
 namespace {
-
-int ensureTrainCap(MlpState* s, uint64_t n) {
-    if (n <= s->cap) return CR_OK;
-    for (int l = 0; l < kLayers; l++) {
-        if (s->act[l]) cudaFree(s->act[l]);
-        if (s->dy[l]) cudaFree(s->dy[l]);
-        s->act[l] = s->dy[l] = nullptr;
-    }
-    for (int l = 0; l < kLayers; l++) {
-        CR_CUDA(cudaMalloc(&s->act[l], n * layerK(l) * sizeof(__half)));
-        CR_CUDA(cudaMalloc(&s->dy[l], n * (l == kLayers - 1 ? 16 : kHid) * sizeof(__half)));
-    }
-    s->cap = n;
-    return CR_OK;
-}
 
 int ensureStage(MlpState* s, uint64_t n) {
     if (n <= s->stageCap) return CR_OK;
@@ -720,12 +685,10 @@ int ensureStage(MlpState* s, uint64_t n) {
 }
 
 int pack(MlpState* s, cudaStream_t st) {
-    kPackWeights<<<cdiv(kParams, 256), 256, 0, st>>>(s->w, s->wFwd, s->wBwd, s->wTc);
+    kPackWeights<<<cdiv(kParams, 256), 256, 0, st>>>(s->w, s->wTc, s->wTcT);
     CR_LAUNCH_CHECK();
     return CR_OK;
 }
-
-constexpr size_t kTrainSmem = (size_t)(kFwdHalves + kBwdHalves) * sizeof(__half);
 
 }  // namespace
 
@@ -739,14 +702,13 @@ int mlpCreate(const cr_mlp_config* cfg, MlpState** out) {
     CR_CUDA(cudaMalloc(&s->v, kParams * sizeof(float)));
     CR_CUDA(cudaMalloc(&s->grad, kParams * sizeof(float)));
     CR_CUDA(cudaMalloc(&s->loss, sizeof(float)));
-    CR_CUDA(cudaMalloc(&s->wFwd, kFwdHalves * sizeof(__half)));
-    CR_CUDA(cudaMalloc(&s->wBwd, kBwdHalves * sizeof(__half)));
     CR_CUDA(cudaMalloc(&s->wTc, kTcWeightBytes));
     CR_CUDA(cudaMemset(s->wTc, 0, kTcWeightBytes));
+    CR_CUDA(cudaMalloc(&s->wTcT, kTcBwdBytes));
+    CR_CUDA(cudaMemset(s->wTcT, 0, kTcBwdBytes));
+    CR_CUDA(cudaMalloc(&s->part, (size_t)s->sms * kParams * sizeof(float)));
     CR_CUDA(cudaMalloc(&s->err, sizeof(uint32_t)));
     CR_CUDA(cudaMemset(s->err, 0, sizeof(uint32_t)));
-    CR_CUDA(cudaMemset(s->wFwd, 0, kFwdHalves * sizeof(__half)));
-    CR_CUDA(cudaMemset(s->wBwd, 0, kBwdHalves * sizeof(__half)));
     CR_CUDA(cudaMemset(s->m, 0, kParams * sizeof(float)));
     CR_CUDA(cudaMemset(s->v, 0, kParams * sizeof(float)));
     CR_CUDA(cudaMemset(s->grad, 0, kParams * sizeof(float)));
@@ -763,7 +725,7 @@ int mlpCreate(const cr_mlp_config* cfg, MlpState** out) {
     }
     CR_CUDA(cudaMemcpy(s->w, w.data(), kParams * sizeof(float), cudaMemcpyHostToDevice));
     CR_CUDA(cudaFuncSetAttribute(kInferTc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem));
-    CR_CUDA(cudaFuncSetAttribute(kTrainFwdBwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTrainSmem));
+    CR_CUDA(cudaFuncSetAttribute(kTrainTc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTrSmem));
     int rc = pack(s, 0);
     if (rc) return rc;
     CR_CUDA(cudaDeviceSynchronize());
@@ -774,13 +736,9 @@ int mlpCreate(const cr_mlp_config* cfg, MlpState** out) {
 void mlpDestroy(MlpState* s) {
     if (!s) return;
     cudaSetDevice(s->device);
-    void* p[] = {s->w, s->m, s->v, s->grad, s->loss, s->wFwd, s->wBwd, s->wTc, s->err, s->stageIn, s->stageOut};
+    void* p[] = {s->w, s->m, s->v, s->grad, s->loss, s->wTc, s->wTcT, s->err, s->part, s->stageIn, s->stageOut};
     for (void* q : p)
         if (q) cudaFree(q);
-    for (int l = 0; l < kLayers; l++) {
-        if (s->act[l]) cudaFree(s->act[l]);
-        if (s->dy[l]) cudaFree(s->dy[l]);
-    }
     delete s;
 }
 
@@ -800,7 +758,8 @@ int mlpCheck(MlpState* s) {
     CR_CUDA(cudaMemcpy(&e, s->err, sizeof(e), cudaMemcpyDeviceToHost));
     if (e) {
         CR_CUDA(cudaMemset(s->err, 0, sizeof(uint32_t)));
-        return fail(CR_ERR_CUDA, "radiance-cache inference: a tensor-core wait timed out");
+        return fail(CR_ERR_CUDA, "radiance-cache network: a tensor-core wait timed out (%s)",
+                    (e & 2u) ? ((e & 1u) ? "inference and training" : "training") : "inference");
     }
     return CR_OK;
 }
@@ -808,27 +767,14 @@ int mlpCheck(MlpState* s) {
 // Accumulates dW of the mean relative L2 loss over n samples into s->grad.
 int mlpGradDevice(MlpState* s, const float* in, const float* target, uint64_t n, cudaStream_t st) {
     if (n == 0) return CR_OK;
-    int rc = ensureTrainCap(s, n);
-    if (rc) return rc;
     CR_CUDA(cudaMemsetAsync(s->loss, 0, sizeof(float), st));
-    Acts acts;
-    for (int l = 0; l < kLayers; l++) {
-        acts.act[l] = s->act[l];
-        acts.dy[l] = s->dy[l];
-    }
-    const unsigned blocks = std::min<unsigned>(cdiv(n, kWarps * 16), (unsigned)s->sms * 2);
-    kTrainFwdBwd<<<blocks, kThreads, kTrainSmem, st>>>(s->wFwd, s->wBwd, in, target, n, acts, s->loss);
+    // one persistent CTA per SM (its shared memory admits one), each with at least one tile
+    const unsigned blocks = std::min<unsigned>(cdiv(n, kTile), (unsigned)s->sms);
+    kTrainTc<<<blocks, kTrThreads, kTrSmem, st>>>(reinterpret_cast<const uint8_t*>(s->wTc),
+                                                 reinterpret_cast<const uint8_t*>(s->wTcT), in, target, n, s->part,
+                                                 s->loss, s->err);
     CR_LAUNCH_CHECK();
-    const float scale = 1.0f / (3.0f * (float)n);
-    const unsigned gb = cdiv(n, kGradRows);
-    kWeightGrad<kFeat, kHid><<<gb, 256, 0, st>>>(s->act[0], s->dy[0], n, kHid, scale, s->grad + paramOffset(0));
-    CR_LAUNCH_CHECK();
-    for (int l = 1; l < kLayers - 1; l++) {
-        kWeightGrad<kHid, kHid><<<gb, 256, 0, st>>>(s->act[l], s->dy[l], n, kHid, scale, s->grad + paramOffset(l));
-        CR_LAUNCH_CHECK();
-    }
-    kWeightGrad<kHid, 16><<<gb, 256, 0, st>>>(s->act[kLayers - 1], s->dy[kLayers - 1], n, 3, scale,
-                                             s->grad + paramOffset(kLayers - 1));
+    kReduceGrad<<<cdiv(kParams, 256), 256, 0, st>>>(s->part, (int)blocks, 1.0f / (3.0f * (float)n), s->grad);
     CR_LAUNCH_CHECK();
     return CR_OK;
 }
@@ -929,7 +875,7 @@ static int gradOrTrain(cr_mlp* m, const float* inputs, const float* targets, uin
         CR_CUDA(cudaMemset(s->grad, 0, kParams * sizeof(float)));
     }
     CR_CUDA(cudaDeviceSynchronize());
-    return CR_OK;
+    return mlpCheck(s);
 }
 
 int cr_mlp_infer_device(cr_mlp* m, const float* inputs, uint64_t n, float* outputs, void* stream) {
