@@ -948,15 +948,57 @@ def batch_extra(torch, n_scenes=64):
         sc.film_clear()
     t_batch = timed(b.render)
     rays = sum(sc.render_ray_count() for sc in scs)
+    # the scenes whose reference is cheap (resolution <= 256) carry the error comparison
+    small = [i for i, p in enumerate(params) if p["res"] <= 256]
+    plain_films = {i: scs[i].film_read() for i in small}
     for sc in scs:
         sc.film_clear()
     t_seq = timed(lambda: [integ.dispatch(sc, p["spp"], readback=False) for sc, integ, p in zip(scs, integs, params)])
     paths = sum(p["res"] ** 2 * p["spp"] for p in params)
-    return {"config": f"{n_scenes} box-clutter scenes from captured CUDA graphs",
-            "triangles": int(sum(sc.n_tris for sc in scs)), "paths": int(paths), "rays": int(rays),
-            "batched_s": round(t_batch, 3), "batched_Mpaths_s": round(paths / t_batch / 1e6, 1),
-            "batched_Mrays_s": round(rays / t_batch / 1e6, 1), "per_scene_dispatch_s": round(t_seq, 3),
-            "speedup_vs_per_scene": round(t_seq / t_batch, 3), "tuning": tune["best"]}
+    out = {"config": f"{n_scenes} box-clutter scenes from captured CUDA graphs",
+           "triangles": int(sum(sc.n_tris for sc in scs)), "paths": int(paths), "rays": int(rays),
+           "batched_s": round(t_batch, 3), "batched_Mpaths_s": round(paths / t_batch / 1e6, 1),
+           "batched_Mrays_s": round(rays / t_batch / 1e6, 1), "per_scene_dispatch_s": round(t_seq, 3),
+           "speedup_vs_per_scene": round(t_seq / t_batch, 3), "tuning": tune["best"]}
+    out["radiance_cache"] = batch_cached_extra(torch, b, scs, integs, params, small, plain_films, timed, t_batch)
+    return out
+
+
+def batch_cached_extra(torch, b, scs, integs, params, small, plain_films, timed, t_plain, ref_mult=8):
+    """The radiance-cache form of the batched workload: every scene renders
+    its spp as cached frames (one sample per pixel each) with a network of
+    its own, trained from scratch during the render, all scenes advancing
+    wave by wave together on their own streams (cr_batch_render_cached).
+    Beside the time, each scene with resolution <= 256 is checked against
+    its own plain reference (ref_mult x its spp, FP64 film): relMSE of its
+    cached film and of its plain batched film at the same spp."""
+    from craystal_gb300.api import RadianceCache
+    caches = [RadianceCache(seed=100 + i) for i in range(len(scs))]
+    for sc in scs:
+        sc.film_clear()
+    t_cached = timed(lambda: b.render_cached(caches))
+    cached_films = {i: scs[i].film_read() for i in small}
+    ratios, rows = [], []
+    for i in small:
+        sc, p = scs[i], params[i]
+        sc.film_clear()
+        integs[i].dispatch(sc, ref_mult * p["spp"], first_sample=1_000_000, readback=False)
+        rgb, w = sc.film_read()
+        ref = rgb.astype(np.float64) / w.astype(np.float64)[..., None]
+        e = {}
+        for label, (frgb, fw) in (("plain", plain_films[i]), ("cached", cached_films[i])):
+            e[label] = rel_mse(frgb / fw[..., None], ref)
+        ratios.append(e["plain"] / e["cached"])
+        rows.append({"scene": i, "res": p["res"], "spp": p["spp"], "plain_relmse": round(e["plain"], 5),
+                     "cached_relmse": round(e["cached"], 5)})
+    for c in caches:
+        c.close()
+    ratios.sort()
+    return {"cached_s": round(t_cached, 3), "plain_batched_s": round(t_plain, 3),
+            "time_ratio_cached_over_plain": round(t_cached / t_plain, 3), "frames_per_scene": "its spp",
+            "checked_scenes": len(small), "reference": f"plain, {ref_mult}x each scene's spp, FP64 film",
+            "median_relmse_ratio_plain_over_cached": round(ratios[len(ratios) // 2], 3) if ratios else None,
+            "scenes": rows}
 
 
 def restated_reference_extra(torch, sc, flat, d_rays, n, d_hits_ours, reps=3):

@@ -166,6 +166,7 @@ SIGNATURES = [
     ("cr_batch_set_tuning", ctypes.c_int, [_P, ctypes.POINTER(CrBatchTuning)]),
     ("cr_batch_get_tuning", ctypes.c_int, [_P, ctypes.POINTER(CrBatchTuning)]),
     ("cr_batch_render", ctypes.c_int, [_P, _P]),
+    ("cr_batch_render_cached", ctypes.c_int, [_P, _P, ctypes.POINTER(CrCacheConfig), _P]),
     ("cr_batch_autotune", ctypes.c_int, [_P, ctypes.POINTER(CrBatchTuning), _P, _U32,
                                          ctypes.POINTER(ctypes.c_uint32)]),
     ("cr_kernel_launch_count", ctypes.c_uint64, []),

@@ -536,6 +536,22 @@ class BatchRenderer:
     def render(self, stream: int = 0):
         check(load().cr_batch_render(self._h, stream or None))
 
+    def render_cached(self, caches, query_vertex=1, train_every=0, train_samples=8192, train_steps=1,
+                      freeze=False):
+        """The batch with the radiance cache: scene i renders its spp cached
+        frames with its own network caches[i] (RadianceCache); returns one
+        stats dict per scene (cr_batch_render_cached)."""
+        from ._lib import CrCacheConfig, CrCacheStats
+        n = len(self.scenes)
+        if len(caches) != n:
+            raise ValueError(f"{len(caches)} networks for {n} scenes")
+        nets = (ctypes.c_void_p * n)(*[c.handle.value for c in caches])
+        cc = CrCacheConfig(query_vertex, train_every, train_samples, train_steps, 1 if freeze else 0)
+        stats = (CrCacheStats * n)()
+        check(load().cr_batch_render_cached(self._h, nets, ctypes.byref(cc), stats))
+        return [{"frames": st.frames, "queries": st.queries, "train_records": st.train_records,
+                 "last_loss": st.last_loss, "last_train_every": st.last_train_every} for st in stats]
+
     def set_tuning(self, tile=16, spp_per_item=4, blocks_per_sm=0, wave_log2=0):
         """wave_log2 = 0: the persistent megakernel with (tile, spp_per_item,
         blocks_per_sm); 16..25: the wavefront in waves of 2^wave_log2 paths."""

@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "cr_internal.cuh"
+#include "cr_mlp.cuh"
 #include "cr_tile.cuh"
 #include "cr_wavefront.cuh"
 
@@ -87,6 +88,9 @@ struct cr_batch {
     cudaGraphExec_t exec = nullptr;
     bool built = false;
     uint64_t replays = 0;
+    // cached renders: one stream per scene and the page-locked counters
+    std::vector<cudaStream_t> sceneStreams;
+    uint32_t* cnt = nullptr;
 };
 
 namespace {
@@ -323,6 +327,8 @@ int cr_batch_destroy(cr_batch* b) {
     if (b->dWaveBase) cudaFree(b->dWaveBase);
     freeWavefrontBuffers(b->wfBuffers);
     if (b->stream) cudaStreamDestroy(b->stream);
+    for (cudaStream_t st : b->sceneStreams) cudaStreamDestroy(st);
+    if (b->cnt) cudaFreeHost(b->cnt);
     delete b;
     return CR_OK;
 }
@@ -354,6 +360,41 @@ int cr_batch_render(cr_batch* b, void* stream) {
     int rc = renderOnce(b, st);
     if (rc) return rc;
     if (!stream) CR_CUDA(cudaStreamSynchronize(st));
+    return CR_OK;
+}
+
+int cr_batch_render_cached(cr_batch* b, cr_mlp* const* mlps, const cr_cache_config* cache, cr_cache_stats* stats) {
+    clearError();
+    if (!b || !mlps || !cache) return fail(CR_ERR_INVALID_ARGUMENT, "NULL argument");
+    const uint32_t n = (uint32_t)b->scenes.size();
+    std::vector<MlpState*> nets(n);
+    std::vector<cr_integrator_config> cfgs(n);
+    std::vector<uint32_t> frames(n), firsts(n);
+    for (uint32_t i = 0; i < n; i++) {
+        if (!mlps[i]) return fail(CR_ERR_INVALID_ARGUMENT, "network %u is NULL", i);
+        for (uint32_t k = 0; k < i; k++)
+            if (mlps[k] == mlps[i]) return fail(CR_ERR_INVALID_ARGUMENT, "scenes %u and %u share a network", k, i);
+        int rc = checkCachedConfig(&b->items[i].config, cache);
+        if (rc) return rc;
+        nets[i] = mlps[i]->s;
+        cfgs[i] = b->items[i].config;
+        frames[i] = b->items[i].spp;
+        firsts[i] = b->items[i].first_sample + (uint32_t)(b->replays * b->items[i].spp);
+    }
+    CR_CUDA(cudaSetDevice(b->device));
+    if (b->sceneStreams.size() != n) {
+        for (uint32_t i = (uint32_t)b->sceneStreams.size(); i < n; i++) {
+            cudaStream_t st = nullptr;
+            CR_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+            b->sceneStreams.push_back(st);
+        }
+    }
+    if (!b->cnt) CR_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&b->cnt), 2 * n * sizeof(uint32_t), cudaHostAllocDefault));
+    CR_CUDA(cudaStreamSynchronize(b->stream));  // plain renders of the batch on its own stream come first
+    int rc = renderCachedMany(b->scenes.data(), cfgs.data(), frames.data(), firsts.data(), nets.data(), cache,
+                              b->sceneStreams.data(), n, stats, b->cnt);
+    if (rc) return rc;
+    b->replays++;
     return CR_OK;
 }
 

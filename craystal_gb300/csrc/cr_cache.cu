@@ -373,13 +373,36 @@ int ensureCacheBuffers(cr_scene* s, uint32_t frames, uint32_t trainCap, uint32_t
     return CR_OK;
 }
 
-}  // namespace
+// One cached render in progress: its configuration and the state kept
+// between waves.
+struct CachedJob {
+    cr_scene* s = nullptr;
+    cr_integrator_config cfg{};
+    cr_cache_config cc{};
+    MlpState* mlp = nullptr;
+    uint32_t frames = 0, first = 0;
+    cr_cache_stats* stats = nullptr;
+    uint32_t* cnt = nullptr;  // the wave's query and record counts, read back (page-locked when batched)
+    // derived by cachedSetup
+    bool wavefront = true, adaptive = true;
+    uint64_t px = 0;
+    uint32_t trainCap = 0, te0 = 0, teMin = 0, teMax = 0, F = 1, waveCap = 0, slotCap = 0, steps = 1;
+    uint32_t lastTrain = 0, f = 0, fw = 0;
+    CacheParams cp{};
+    Params p{};
+    WfBuffers* wb = nullptr;
+    CacheBuffers* b = nullptr;
+};
 
-int renderCached(cr_scene* s, const cr_integrator_config* cfg, const cr_cache_config* cc, MlpState* mlp,
-                 uint32_t frames, uint32_t first, cudaStream_t st, cr_cache_stats* stats) {
-    const uint32_t trainCap = cc->train_samples ? cc->train_samples : 8192u;
-    const bool wavefront = !(cfg->flags & CR_RENDER_MEGAKERNEL);
-    CacheParams cp;
+// Sets up a cached render of j.frames frames: the network input
+// normalisation, the training-path spacing, the frames per wave and the
+// buffers.
+int cachedSetup(CachedJob& j) {
+    cr_scene* s = j.s;
+    const cr_cache_config* cc = &j.cc;
+    j.trainCap = cc->train_samples ? cc->train_samples : 8192u;
+    j.wavefront = !(j.cfg.flags & CR_RENDER_MEGAKERNEL);
+    CacheParams& cp = j.cp;
     float3 mn = s->rootMin, mx = s->rootMax;
     if (cc->scene_max[0] > cc->scene_min[0]) {
         mn = mk3(cc->scene_min[0], cc->scene_min[1], cc->scene_min[2]);
@@ -395,14 +418,13 @@ int renderCached(cr_scene* s, const cr_integrator_config* cfg, const cr_cache_co
     // spacing of the training paths by (records produced / train_samples),
     // by at most 2x per frame and never below half the start.  Training paths
     // run to full depth, so more of them than the batch can use only cost time.
-    const uint64_t px = (uint64_t)s->cam.width * s->cam.height;
-    const bool adaptive = cc->train_every == 0;
-    const uint32_t te0 = adaptive ? (uint32_t)std::max<uint64_t>(1, (px * 3 + trainCap / 2) / trainCap)
-                                  : cc->train_every;
-    const uint32_t teMin = adaptive ? std::max(1u, te0 / 2) : te0;
-    const uint32_t teMax = (uint32_t)std::max<uint64_t>(te0, std::min<uint64_t>(px, 1u << 24));
-    cp.trainEvery = te0;
-    cp.trainCap = trainCap;
+    j.px = (uint64_t)s->cam.width * s->cam.height;
+    j.adaptive = cc->train_every == 0;
+    j.te0 = j.adaptive ? (uint32_t)std::max<uint64_t>(1, (j.px * 3 + j.trainCap / 2) / j.trainCap) : cc->train_every;
+    j.teMin = j.adaptive ? std::max(1u, j.te0 / 2) : j.te0;
+    j.teMax = (uint32_t)std::max<uint64_t>(j.te0, std::min<uint64_t>(j.px, 1u << 24));
+    cp.trainEvery = j.te0;
+    cp.trainCap = j.trainCap;
     // training paths of a frame: px / trainEvery on average (the hash picks
     // them); room for four times that at the smallest spacing, beyond which a
     // path keeps no records
@@ -413,107 +435,214 @@ int renderCached(cr_scene* s, const cr_integrator_config* cfg, const cr_cache_co
     // of several frames waits for it once.  Up to 8 frames, or 2^23 paths.
     // Each frame of a wave still gets its own Adam steps, on its share of the
     // wave's records; the frames of a wave share the network they start with.
-    WfBuffers* wb = nullptr;
-    uint32_t waveCap = 0;
-    uint32_t F = 1;
-    if (wavefront) {
-        F = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(std::min<uint64_t>(8, frames), (1ull << 23) / px));
-        int rcw = ensureWavefrontWave(s->wfBuffers, px * F, s->nMats + 2, wb, waveCap);
+    j.F = 1;
+    if (j.wavefront) {
+        j.F = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(std::min<uint64_t>(8, j.frames), (1ull << 23) / j.px));
+        int rcw = ensureWavefrontWave(s->wfBuffers, j.px * j.F, s->nMats + 2, j.wb, j.waveCap);
         if (rcw) return rcw;
         clearError();
-        F = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(F, waveCap / px));
+        j.F = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(j.F, j.waveCap / j.px));
     }
-    const uint32_t slotCap =
-        wavefront ? (uint32_t)std::min<uint64_t>(px * F, 4 * (px * F / teMin) + 4096) : 0u;
-    CacheBuffers* b = nullptr;
-    int rc = ensureCacheBuffers(s, F, trainCap * F, slotCap, &b);
+    j.slotCap = j.wavefront ? (uint32_t)std::min<uint64_t>(j.px * j.F, 4 * (j.px * j.F / j.teMin) + 4096) : 0u;
+    int rc = ensureCacheBuffers(s, j.F, j.trainCap * j.F, j.slotCap, &j.b);
     if (rc) return rc;
-    if (adaptive && b->teStart == te0 && b->teAdapted) cp.trainEvery = b->teAdapted;
-    Params p;
-    p.maxDepth = cfg->max_depth;
-    p.rrThreshold = cfg->rr_threshold;
-    p.useMIS = cfg->use_mis ? 1u : 0u;
+    if (j.adaptive && j.b->teStart == j.te0 && j.b->teAdapted) cp.trainEvery = j.b->teAdapted;
+    Params& p = j.p;
+    p.maxDepth = j.cfg.max_depth;
+    p.rrThreshold = j.cfg.rr_threshold;
+    p.useMIS = j.cfg.use_mis ? 1u : 0u;
     p.spp = 1;
     p.sppPerBlock = 1;
     p.spectral = 0;
     p.wb = mk3(1.0f, 1.0f, 1.0f);
+    j.steps = cc->train_steps ? cc->train_steps : 1u;
+    j.lastTrain = 0;
+    j.f = 0;
+    return CR_OK;
+}
+
+// Issues the next wave of frames on st (the paths up to their query vertex,
+// the training paths to their end) and the copy of its two record counters
+// to j.cnt; the caller waits for st before cachedFinishWave.
+int cachedIssueWave(CachedJob& j, cudaStream_t st) {
+    cr_scene* s = j.s;
+    CacheBuffers* b = j.b;
+    CacheParams& cp = j.cp;
+    Params& p = j.p;
+    j.fw = std::min(j.F, j.frames - j.f);  // frames in this wave
+    p.first = j.first + j.f;
+    p.spp = j.fw;
+    cp.trainCap = j.trainCap * j.fw;
+    CR_CUDA(cudaMemsetAsync(b->counters, 0, 3 * sizeof(uint32_t), st));
     const uint32_t W = s->cam.width, H = s->cam.height;
-    dim3 grid((W + 15) / 16, (H + 15) / 16), block(16, 16);
-    const uint32_t steps = cc->train_steps ? cc->train_steps : 1u;
-    uint32_t lastTrain = 0;
-    for (uint32_t f = 0; f < frames;) {
-        const uint32_t fw = std::min(F, frames - f);  // frames in this wave
-        p.first = first + f;
-        p.spp = fw;
-        cp.trainCap = trainCap * fw;
-        CR_CUDA(cudaMemsetAsync(b->counters, 0, 3 * sizeof(uint32_t), st));
-        if (wavefront) {
-            const CachedMode mode{cp,          W,          H,         p.first,        b->qIn,
-                                  b->qBeta,    b->counters, b->recIn, b->recBeta,     b->recBefore,
-                                  b->counters + 2, slotCap, b->tIn,   b->tTarget,     b->counters + 1,
-                                  b->samples};
-            const uint64_t paths = px * fw;
-            for (uint64_t base = 0; base < paths; base += waveCap) {
-                // after the query vertex only training paths are live: one
-                // launch finishes them
-                rc = runWave(oneScene(s, p), mode, wb, base, (uint32_t)std::min<uint64_t>(waveCap, paths - base),
+    if (j.wavefront) {
+        const CachedMode mode{cp,          W,          H,         p.first,        b->qIn,
+                              b->qBeta,    b->counters, b->recIn, b->recBeta,     b->recBefore,
+                              b->counters + 2, j.slotCap, b->tIn,   b->tTarget,     b->counters + 1,
+                              b->samples};
+        const uint64_t paths = j.px * j.fw;
+        for (uint64_t base = 0; base < paths; base += j.waveCap) {
+            // after the query vertex only training paths are live: one
+            // launch finishes them
+            int rc = runWave(oneScene(s, p), mode, j.wb, base, (uint32_t)std::min<uint64_t>(j.waveCap, paths - base),
                              p.maxDepth, s->nMats + 2, st, nullptr, 0, cp.queryVertex + 1);
+            if (rc) return rc;
+        }
+    } else {
+        dim3 grid((W + 15) / 16, (H + 15) / 16), block(16, 16);
+        kRenderCached<<<grid, block, 0, st>>>(s->view(), s->cam, p, cp, b->samples, b->qIn, b->qBeta, b->counters,
+                                              b->tIn, b->tTarget, b->counters + 1, s->rayCounter);
+        CR_LAUNCH_CHECK();
+    }
+    CR_CUDA(cudaMemcpyAsync(j.cnt, b->counters, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    return CR_OK;
+}
+
+// After the wave's counters are in j.cnt: adapts the training-path spacing,
+// then issues on st the inference of the wave's queries, the film splat and
+// the frames' training steps.
+int cachedFinishWave(CachedJob& j, cudaStream_t st) {
+    cr_scene* s = j.s;
+    CacheBuffers* b = j.b;
+    CacheParams& cp = j.cp;
+    const uint32_t fw = j.fw;
+    const uint32_t nq = j.cnt[0], nt = std::min(j.cnt[1], j.trainCap * fw);
+    const uint32_t teUsed = cp.trainEvery;
+    if (j.adaptive) {
+        const double ratio = std::min(2.0, std::max(0.5, (double)j.cnt[1] / ((double)j.trainCap * fw)));
+        const double te = std::min((double)j.teMax, std::max((double)j.teMin, (double)cp.trainEvery * ratio));
+        cp.trainEvery = (uint32_t)(te + 0.5);
+        b->teStart = j.te0;
+        b->teAdapted = cp.trainEvery;
+    }
+    int rc = mlpInferDevice(j.mlp, b->qIn, nq, b->qOut, true, st);
+    if (rc) return rc;
+    const uint64_t nSamples = j.px * fw;
+    kSplatCached<<<(unsigned)((nSamples + 255) / 256), 256, 0, st>>>(b->samples, b->qBeta, b->qOut, nSamples,
+                                                                   s->cam.width, s->cam.height, s->filmRgb, s->filmW);
+    CR_LAUNCH_CHECK();
+    if (nt > 0 && !j.cc.freeze) {
+        // train_steps Adam steps per frame, each frame on its share of the
+        // wave's records
+        for (uint32_t k = 0; k < fw; k++) {
+            const uint32_t r0 = (uint32_t)((uint64_t)nt * k / fw), r1 = (uint32_t)((uint64_t)nt * (k + 1) / fw);
+            if (r1 <= r0) continue;
+            j.lastTrain = r1 - r0;
+            for (uint32_t q = 0; q < j.steps; q++) {
+                rc = mlpGradDevice(j.mlp, b->tIn + (size_t)r0 * kMlpInputs, b->tTarget + (size_t)r0 * 3, r1 - r0, st);
+                if (rc) return rc;
+                rc = mlpAdamDevice(j.mlp, st);
                 if (rc) return rc;
             }
-        } else {
-            kRenderCached<<<grid, block, 0, st>>>(s->view(), s->cam, p, cp, b->samples, b->qIn, b->qBeta,
-                                                  b->counters, b->tIn, b->tTarget, b->counters + 1, s->rayCounter);
-            CR_LAUNCH_CHECK();
         }
-        uint32_t cnt[2];
-        CR_CUDA(cudaMemcpyAsync(cnt, b->counters, sizeof(cnt), cudaMemcpyDeviceToHost, st));
-        CR_CUDA(cudaStreamSynchronize(st));
-        const uint32_t nq = cnt[0], nt = std::min(cnt[1], trainCap * fw);
-        const uint32_t teUsed = cp.trainEvery;
-        if (adaptive) {
-            const double ratio = std::min(2.0, std::max(0.5, (double)cnt[1] / ((double)trainCap * fw)));
-            const double te = std::min((double)teMax, std::max((double)teMin, (double)cp.trainEvery * ratio));
-            cp.trainEvery = (uint32_t)(te + 0.5);
-            b->teStart = te0;
-            b->teAdapted = cp.trainEvery;
-        }
-        rc = mlpInferDevice(mlp, b->qIn, nq, b->qOut, true, st);
-        if (rc) return rc;
-        const uint64_t nSamples = px * fw;
-        kSplatCached<<<(unsigned)((nSamples + 255) / 256), 256, 0, st>>>(b->samples, b->qBeta, b->qOut, nSamples, W,
-                                                                       H, s->filmRgb, s->filmW);
-        CR_LAUNCH_CHECK();
-        if (nt > 0 && !cc->freeze) {
-            // train_steps Adam steps per frame, each frame on its share of the
-            // wave's records
-            for (uint32_t k = 0; k < fw; k++) {
-                const uint32_t r0 = (uint32_t)((uint64_t)nt * k / fw), r1 = (uint32_t)((uint64_t)nt * (k + 1) / fw);
-                if (r1 <= r0) continue;
-                lastTrain = r1 - r0;
-                for (uint32_t j = 0; j < steps; j++) {
-                    rc = mlpGradDevice(mlp, b->tIn + (size_t)r0 * kMlpInputs, b->tTarget + (size_t)r0 * 3, r1 - r0, st);
-                    if (rc) return rc;
-                    rc = mlpAdamDevice(mlp, st);
-                    if (rc) return rc;
-                }
-            }
-        }
-        if (stats) {
-            stats->queries += nq;
-            stats->train_records += nt;
-            stats->frames += fw;
-            stats->last_train_every = teUsed;
-        }
-        f += fw;
     }
-    rc = mlpCheck(mlp);
+    if (j.stats) {
+        j.stats->queries += nq;
+        j.stats->train_records += nt;
+        j.stats->frames += fw;
+        j.stats->last_train_every = teUsed;
+    }
+    j.f += fw;
+    return CR_OK;
+}
+
+// Reports a tensor-core wait that ran out and the last training loss
+// (synchronises st).
+int cachedEnd(CachedJob& j, cudaStream_t st) {
+    CR_CUDA(cudaStreamSynchronize(st));
+    int rc = mlpCheck(j.mlp);
     if (rc) return rc;
-    if (stats && lastTrain) {
+    if (j.stats && j.lastTrain) {
         float l = 0;
-        CR_CUDA(cudaMemcpyAsync(&l, mlpLossPtr(mlp), sizeof(float), cudaMemcpyDeviceToHost, st));
+        CR_CUDA(cudaMemcpyAsync(&l, mlpLossPtr(j.mlp), sizeof(float), cudaMemcpyDeviceToHost, st));
         CR_CUDA(cudaStreamSynchronize(st));
-        stats->last_loss = l / (3.0f * (float)lastTrain);
+        j.stats->last_loss = l / (3.0f * (float)j.lastTrain);
     }
+    return CR_OK;
+}
+
+}  // namespace
+
+int renderCached(cr_scene* s, const cr_integrator_config* cfg, const cr_cache_config* cc, MlpState* mlp,
+                 uint32_t frames, uint32_t first, cudaStream_t st, cr_cache_stats* stats) {
+    CachedJob j;
+    j.s = s;
+    j.cfg = *cfg;
+    j.cc = *cc;
+    j.mlp = mlp;
+    j.frames = frames;
+    j.first = first;
+    j.stats = stats;
+    uint32_t cnt[2] = {0, 0};
+    j.cnt = cnt;
+    int rc = cachedSetup(j);
+    if (rc) return rc;
+    while (j.f < j.frames) {
+        rc = cachedIssueWave(j, st);
+        if (rc) return rc;
+        CR_CUDA(cudaStreamSynchronize(st));
+        rc = cachedFinishWave(j, st);
+        if (rc) return rc;
+    }
+    return cachedEnd(j, st);
+}
+
+// Cached renders of n scenes, interleaved wave by wave: every round issues
+// the next wave of each unfinished scene on that scene's stream, then, as
+// each stream's counters arrive, that scene's inference, splat and training.
+// A scene's renders follow the same sequence as renderCached, so its film
+// receives the same samples; the scenes' work overlaps on the GPU.
+// cnt: 2 x n page-locked words for the counters.
+int renderCachedMany(cr_scene* const* scenes, const cr_integrator_config* cfgs, const uint32_t* frames,
+                     const uint32_t* firsts, MlpState* const* mlps, const cr_cache_config* cc,
+                     const cudaStream_t* streams, uint32_t n, cr_cache_stats* stats, uint32_t* cnt) {
+    std::vector<CachedJob> jobs(n);
+    for (uint32_t i = 0; i < n; i++) {
+        CachedJob& j = jobs[i];
+        j.s = scenes[i];
+        j.cfg = cfgs[i];
+        j.cc = *cc;
+        j.mlp = mlps[i];
+        j.frames = frames[i];
+        j.first = firsts[i];
+        j.stats = stats ? stats + i : nullptr;
+        j.cnt = cnt + 2 * i;
+        int rc = cachedSetup(j);
+        if (rc) return rc;
+    }
+    for (bool more = true; more;) {
+        more = false;
+        for (uint32_t i = 0; i < n; i++) {
+            if (jobs[i].f >= jobs[i].frames) continue;
+            int rc = cachedIssueWave(jobs[i], streams[i]);
+            if (rc) return rc;
+            more = true;
+        }
+        for (uint32_t i = 0; more && i < n; i++) {
+            if (jobs[i].f >= jobs[i].frames) continue;
+            CR_CUDA(cudaStreamSynchronize(streams[i]));
+            int rc = cachedFinishWave(jobs[i], streams[i]);
+            if (rc) return rc;
+        }
+    }
+    for (uint32_t i = 0; i < n; i++) {
+        int rc = cachedEnd(jobs[i], streams[i]);
+        if (rc) return rc;
+    }
+    return CR_OK;
+}
+
+// Validates a cached-render configuration (the checks of cr_render_cached).
+int checkCachedConfig(const cr_integrator_config* cfg, const cr_cache_config* cc) {
+    if (cfg->max_depth > 1024) return fail(CR_ERR_INVALID_ARGUMENT, "max_depth %u", cfg->max_depth);
+    if (cfg->flags & CR_RENDER_SPECTRAL)
+        return fail(CR_ERR_UNSUPPORTED, "the radiance cache learns RGB radiance; spectral rendering is not cached");
+    if (cfg->flags & ~(CR_RENDER_WAVEFRONT | CR_RENDER_MEGAKERNEL))
+        return fail(CR_ERR_INVALID_ARGUMENT, "unknown render flags 0x%x", cfg->flags);
+    if ((cfg->flags & CR_RENDER_WAVEFRONT) && (cfg->flags & CR_RENDER_MEGAKERNEL))
+        return fail(CR_ERR_INVALID_ARGUMENT, "CR_RENDER_WAVEFRONT and CR_RENDER_MEGAKERNEL exclude each other");
+    if (cc->query_vertex == 0 || cc->query_vertex >= cfg->max_depth)
+        return fail(CR_ERR_INVALID_ARGUMENT, "query_vertex %u must be in [1, max_depth)", cc->query_vertex);
     return CR_OK;
 }
 
@@ -527,15 +656,8 @@ extern "C" int cr_render_cached(cr_scene* scene, const cr_integrator_config* cfg
     clearError();
     if (!scene || !cfg || !cc || !mlp) return fail(CR_ERR_INVALID_ARGUMENT, "NULL argument");
     if (!scene->hasCamera) return fail(CR_ERR_INVALID_ARGUMENT, "scene has no camera; call cr_scene_set_camera");
-    if (cfg->max_depth > 1024) return fail(CR_ERR_INVALID_ARGUMENT, "max_depth %u", cfg->max_depth);
-    if (cfg->flags & CR_RENDER_SPECTRAL)
-        return fail(CR_ERR_UNSUPPORTED, "the radiance cache learns RGB radiance; spectral rendering is not cached");
-    if (cfg->flags & ~(CR_RENDER_WAVEFRONT | CR_RENDER_MEGAKERNEL))
-        return fail(CR_ERR_INVALID_ARGUMENT, "unknown render flags 0x%x", cfg->flags);
-    if ((cfg->flags & CR_RENDER_WAVEFRONT) && (cfg->flags & CR_RENDER_MEGAKERNEL))
-        return fail(CR_ERR_INVALID_ARGUMENT, "CR_RENDER_WAVEFRONT and CR_RENDER_MEGAKERNEL exclude each other");
-    if (cc->query_vertex == 0 || cc->query_vertex >= cfg->max_depth)
-        return fail(CR_ERR_INVALID_ARGUMENT, "query_vertex %u must be in [1, max_depth)", cc->query_vertex);
+    int rc = checkCachedConfig(cfg, cc);
+    if (rc) return rc;
     CR_CUDA(cudaSetDevice(scene->device));
     return renderCached(scene, cfg, cc, mlp->s, frames, first_sample, static_cast<cudaStream_t>(stream), stats);
 }

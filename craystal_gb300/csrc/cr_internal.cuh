@@ -316,5 +316,10 @@ int renderDevice(cr_scene* s, const cr_integrator_config* cfg, uint32_t spp, uin
 int resolveFilm(cr_scene* s, float* rgbHost);
 // implemented in cr_cache.cu
 void freeCacheBuffers(void* buffers);
+struct MlpState;
+int checkCachedConfig(const cr_integrator_config* cfg, const cr_cache_config* cc);
+int renderCachedMany(cr_scene* const* scenes, const cr_integrator_config* cfgs, const uint32_t* frames,
+                     const uint32_t* firsts, MlpState* const* mlps, const cr_cache_config* cc,
+                     const cudaStream_t* streams, uint32_t n, cr_cache_stats* stats, uint32_t* cnt);
 
 }  // namespace cr

@@ -561,6 +561,17 @@ int cr_batch_set_tuning(cr_batch* batch, const cr_batch_tuning* tuning);
 int cr_batch_get_tuning(const cr_batch* batch, cr_batch_tuning* tuning);
 /* stream NULL: the batch's own stream, waited for before returning */
 int cr_batch_render(cr_batch* batch, void* stream);
+/* The batch rendered with the radiance cache (cr_render_cached per scene):
+ * scene i renders items[i].spp cached frames (one sample per pixel each, the
+ * k-th render of the batch starting at sample index first_sample + k*spp)
+ * with its own network mlps[i], all with the cache settings `cache`; the
+ * scenes' configs must allow caching (RGB, query_vertex < max_depth).  The
+ * scenes advance wave by wave together, each on a stream of its own, so that
+ * the small scenes' waves, inference and training overlap the large ones'.
+ * Each scene's film receives the samples cr_render_cached would add.  stats
+ * (may be NULL) is an array of n entries, added to.  Returns when done. */
+int cr_batch_render_cached(cr_batch* batch, cr_mlp* const* mlps,
+                           const cr_cache_config* cache, cr_cache_stats* stats);
 int cr_batch_autotune(cr_batch* batch, cr_batch_tuning* best,
                       cr_batch_tuning_result* results, uint32_t max_results,
                       uint32_t* n_results);

@@ -71,3 +71,57 @@ def test_autotune_times_every_tuning_and_clears(gpu_lib, tmp_path):
         rgb, w = sc.film_read()
         assert not w.any() and sc.render_ray_count() == 0
     assert (tmp_path / "tuning.json").exists()
+
+
+def make_cached_batch(n=4):
+    """RGB scenes (the cache learns RGB) of uneven size, depth and spp."""
+    params, scs, integs = make_batch(n)
+    integs = [PathTraceIntegrator(PathTraceIntegrator.Configs(maxDepth=p["depth"], rrThreshold=0.05), compat=False)
+              for p in params]
+    return params, scs, integs
+
+
+@pytest.mark.parametrize("freeze", [True, False])
+def test_batch_cached_equals_per_scene_cached(gpu_lib, freeze):
+    """cr_batch_render_cached against cr_render_cached scene by scene, each
+    scene with its own network of the same seed: frozen networks give the
+    same films, queries and records (float-atomic order aside); trained ones
+    the same training sequence, so films agree to the float-order noise the
+    updates pick up (relMSE < 1e-3)."""
+    from craystal_gb300.api import CachedPathTraceIntegrator, RadianceCache
+    params, scs, integs = make_cached_batch()
+    spp = [p["spp"] + 2 for p in params]
+    b = BatchRenderer(scs, integs, spp, first_sample=[7] * len(params))
+    stats = b.render_cached([RadianceCache(seed=40 + i) for i in range(len(scs))], train_every=4, freeze=freeze)
+    batch = [sc.film_read() for sc in scs]
+    for i, (sc, integ, (rgb, w)) in enumerate(zip(scs, integs, batch)):
+        sc.film_clear()
+        single = CachedPathTraceIntegrator(integ.configs, train_every=4, cache=RadianceCache(seed=40 + i))
+        single.dispatch(sc, spp[i], first_sample=7, readback=False, freeze=freeze)
+        rgb2, w2 = sc.film_read()
+        np.testing.assert_allclose(w, w2, rtol=1e-5, atol=1e-6)
+        assert stats[i]["frames"] == spp[i] == single.stats.frames
+        assert stats[i]["queries"] == single.stats.queries and stats[i]["train_records"] == single.stats.train_records
+        if freeze:
+            np.testing.assert_allclose(rgb, rgb2, rtol=1e-4, atol=1e-5)
+        else:
+            a = np.nan_to_num(rgb / w[..., None])
+            c = np.nan_to_num(rgb2 / w2[..., None])
+            assert float(np.mean((a - c) ** 2 / (c ** 2 + 1e-2))) < 1e-3
+
+
+def test_batch_cached_training_paths_equal_plain(gpu_lib):
+    """With every pixel a training path, each scene's cached film is its own
+    plain render (cr_render, the same sample indices)."""
+    from craystal_gb300.api import RadianceCache
+    params, scs, integs = make_cached_batch(3)
+    b = BatchRenderer(scs, integs, [p["spp"] for p in params], first_sample=[3] * len(params))
+    stats = b.render_cached([RadianceCache(seed=i) for i in range(len(scs))], train_every=1)
+    batch = [sc.film_read() for sc in scs]
+    for sc, integ, p, (rgb, w), st in zip(scs, integs, params, batch, stats):
+        sc.film_clear()
+        integ.dispatch(sc, p["spp"], first_sample=3, readback=False)
+        rgb2, w2 = sc.film_read()
+        np.testing.assert_allclose(w, w2, rtol=1e-5, atol=1e-6)
+        np.testing.assert_allclose(rgb, rgb2, rtol=1e-4, atol=1e-5)
+        assert st["queries"] == 0 and st["train_records"] > 0
