@@ -951,6 +951,10 @@ def batch_extra(torch, n_scenes=64):
     # the scenes whose reference is cheap (resolution <= 256) carry the error comparison
     small = [i for i, p in enumerate(params) if p["res"] <= 256]
     plain_films = {i: scs[i].film_read() for i in small}
+    # one untimed sample per scene first, so that per-scene dispatch is timed
+    # with its path-state buffers already allocated, as the batch's are
+    for sc, integ in zip(scs, integs):
+        integ.dispatch(sc, 1, first_sample=1 << 30, readback=False)
     for sc in scs:
         sc.film_clear()
     t_seq = timed(lambda: [integ.dispatch(sc, p["spp"], readback=False) for sc, integ, p in zip(scs, integs, params)])
@@ -961,7 +965,53 @@ def batch_extra(torch, n_scenes=64):
            "batched_Mrays_s": round(rays / t_batch / 1e6, 1), "per_scene_dispatch_s": round(t_seq, 3),
            "speedup_vs_per_scene": round(t_seq / t_batch, 3), "tuning": tune["best"]}
     out["radiance_cache"] = batch_cached_extra(torch, b, scs, integs, params, small, plain_films, timed, t_batch)
+    out["breakdown"] = batch_breakdown(torch, scs, integs, params, tune["best"], t_batch, timed)
     return out
+
+
+def batch_breakdown(torch, scs, integs, params, tuning, t_batch, timed):
+    """Where the batched workload's time goes.  Every scene dispatched alone
+    (synchronised) gives its own time; the scenes with at least one wave of
+    paths (2^wave_log2) render on their own waves inside the batch too, so
+    only the rest can gain from sharing waves, which bounds the batch's
+    speed-up over per-scene dispatch (Amdahl).  The shared part's own
+    speed-up is their summed per-scene time against the batch time left
+    after the own-wave scenes.  Beside it, the reference's dispatch
+    structure (Core/Integrator.cu:246-259: one launch and one device
+    synchronisation per sample per scene) run with this library's kernels."""
+    wave = 1 << tuning["wave_log2"] if tuning.get("wave_log2") else None
+    per = []
+    for sc, integ, p in zip(scs, integs, params):
+        sc.film_clear()
+        per.append(timed(lambda: integ.dispatch(sc, p["spp"], readback=False)))
+    per = np.array(per)
+    paths = np.array([p["res"] ** 2 * p["spp"] for p in params], dtype=np.float64)
+    own = paths >= wave if wave else np.zeros(len(params), bool)
+    t_own, t_shared_seq = float(per[own].sum()), float(per[~own].sum())
+    classes = {}
+    for r in sorted({p["res"] for p in params}):
+        m = np.array([p["res"] == r for p in params])
+        classes[str(r)] = {"scenes": int(m.sum()), "paths_share": round(float(paths[m].sum() / paths.sum()), 4),
+                           "time_share": round(float(per[m].sum() / per.sum()), 4),
+                           "Mpaths_s": round(float(paths[m].sum() / per[m].sum() / 1e6), 1)}
+
+    def per_spp():
+        for sc, integ, p in zip(scs, integs, params):
+            for k in range(p["spp"]):
+                integ.dispatch(sc, 1, first_sample=k, readback=False)
+                torch.cuda.synchronize()
+
+    for sc in scs:
+        sc.film_clear()
+    t_spp = timed(per_spp)
+    t_shared_batch = max(t_batch - t_own, 1e-9)
+    return {"per_scene_sum_s": round(float(per.sum()), 3), "by_resolution": classes,
+            "own_wave_scenes": int(own.sum()), "own_wave_paths_share": round(float(paths[own].sum() / paths.sum()), 4),
+            "own_wave_time_s": round(t_own, 3), "shared_scenes_per_scene_s": round(t_shared_seq, 4),
+            "shared_scenes_in_batch_s": round(t_shared_batch, 4),
+            "shared_part_speedup": round(t_shared_seq / t_shared_batch, 2),
+            "amdahl_bound_vs_per_scene": round(float(per.sum()) / t_own, 3) if t_own > 0 else None,
+            "per_spp_dispatch_s": round(t_spp, 3), "speedup_vs_per_spp_dispatch": round(t_spp / t_batch, 2)}
 
 
 def batch_cached_extra(torch, b, scs, integs, params, small, plain_films, timed, t_plain, ref_mult=8):

@@ -733,34 +733,81 @@ __global__ void __launch_bounds__(kSubtreeWarps * 32) kSubtree(const SmallTask* 
 // ---------------------------------------------------------------------------
 // traversal layout
 // ---------------------------------------------------------------------------
-__global__ void kLeafFlags(const BuildNode* __restrict__ nodes, uint32_t n, uint32_t* __restrict__ isLeaf) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) isLeaf[i] = nodes[i].info.z;
+__host__ __device__ __forceinline__ bool isInterior(const BuildNode* nodes, uint32_t c) { return nodes[c].info.z == 0u; }
+
+// Pairs in node i's group: 1 + its interior children for an interior node at
+// even depth (a group top), 0 for any other node (a leaf, or an interior
+// node at odd depth, whose pair sits in its parent's group).
+__host__ __device__ __forceinline__ uint32_t groupSize(const BuildNode* nodes, uint32_t i) {
+    const BuildNode& nd = nodes[i];
+    if (nd.info.z || (nd.info.w & 1u)) return 0u;
+    return 1u + (isInterior(nodes, nd.info.x) ? 1u : 0u) + (isInterior(nodes, nd.info.y) ? 1u : 0u);
 }
 
-__host__ __device__ __forceinline__ uint32_t childRef(const BuildNode* nodes, const uint32_t* leafPrefix, uint32_t c) {
-    const BuildNode& n = nodes[c];
-    return n.info.z ? leafRef(leafPrefix[c], n.info.x, n.info.y) : (c - leafPrefix[c]);
+// The ref of group top g: its pair index and the flags that say which of
+// its children's pairs follow it.
+__host__ __device__ __forceinline__ uint32_t topRef(const BuildNode* nodes, const uint32_t* groupStart, uint32_t g) {
+    const BuildNode& nd = nodes[g];
+    return groupStart[g] | kGroupTopBit | (isInterior(nodes, nd.info.x) ? kGroupLeftBit : 0u) |
+           (isInterior(nodes, nd.info.y) ? kGroupRightBit : 0u);
 }
 
-// The NodePair of interior node i: both children's boxes, refs and
-// degenerate-axis flags.  Interior node i becomes pair i - leafPrefix[i].
-__host__ __device__ __forceinline__ NodePair pairOf(const BuildNode* nodes, const uint32_t* leafPrefix, uint32_t i) {
+// The NodePair of interior node i at pair index p: both children's boxes,
+// refs and degenerate-axis flags.  The children of a group top (top = true)
+// are the group's second-level pairs at p + 1 and after; the interior
+// children of a second-level node are group tops of their own.
+__host__ __device__ __forceinline__ NodePair groupPair(const BuildNode* nodes, const uint32_t* leafPrefix,
+                                                       const uint32_t* groupStart, uint32_t i, bool top, uint32_t p) {
     const BuildNode& nd = nodes[i];
     const BuildNode& L = nodes[nd.info.x];
     const BuildNode& R = nodes[nd.info.y];
-    NodePair p;
-    p.p0 = make_float4(L.lo.x, L.lo.y, L.lo.z, L.hi.x);
-    p.p1 = make_float4(L.hi.y, L.hi.z, R.lo.x, R.lo.y);
-    p.p2 = make_float4(R.lo.z, R.hi.x, R.hi.y, R.hi.z);
-    uint32_t fl = degenerateFlags(mk3(L.lo.x, L.lo.y, L.lo.z), mk3(L.hi.x, L.hi.y, L.hi.z)) |
-                  (degenerateFlags(mk3(R.lo.x, R.lo.y, R.lo.z), mk3(R.hi.x, R.hi.y, R.hi.z)) << 3);
-    p.ref = make_uint4(childRef(nodes, leafPrefix, nd.info.x), childRef(nodes, leafPrefix, nd.info.y), fl, 0u);
-    return p;
+    NodePair q;
+    q.p0 = make_float4(L.lo.x, L.lo.y, L.lo.z, L.hi.x);
+    q.p1 = make_float4(L.hi.y, L.hi.z, R.lo.x, R.lo.y);
+    q.p2 = make_float4(R.lo.z, R.hi.x, R.hi.y, R.hi.z);
+    const uint32_t fl = degenerateFlags(mk3(L.lo.x, L.lo.y, L.lo.z), mk3(L.hi.x, L.hi.y, L.hi.z)) |
+                        (degenerateFlags(mk3(R.lo.x, R.lo.y, R.lo.z), mk3(R.hi.x, R.hi.y, R.hi.z)) << 3);
+    uint32_t ref[2];
+    uint32_t next = p + 1u;
+    for (int k = 0; k < 2; k++) {
+        const uint32_t c = k == 0 ? nd.info.x : nd.info.y;
+        const BuildNode& n = nodes[c];
+        if (n.info.z) ref[k] = leafRef(leafPrefix[c], n.info.x, n.info.y);
+        else if (top) ref[k] = next++;
+        else ref[k] = topRef(nodes, groupStart, c);
+    }
+    q.ref = make_uint4(ref[0], ref[1], fl, 0u);
+    return q;
+}
+
+// Writes group top i's pair and its second-level pairs (and nothing for
+// other nodes); every pair is written exactly once.
+__host__ __device__ __forceinline__ void writeGroup(const BuildNode* nodes, const uint32_t* leafPrefix,
+                                                    const uint32_t* groupStart, uint32_t i, NodePair* pairs) {
+    if (groupSize(nodes, i) == 0u) return;
+    const BuildNode& nd = nodes[i];
+    const uint32_t p = groupStart[i];
+    pairs[p] = groupPair(nodes, leafPrefix, groupStart, i, true, p);
+    uint32_t q = p + 1u;
+    for (uint32_t c : {nd.info.x, nd.info.y})
+        if (isInterior(nodes, c)) {
+            pairs[q] = groupPair(nodes, leafPrefix, groupStart, c, false, q);
+            q++;
+        }
+}
+
+__global__ void kLeafFlags(const BuildNode* __restrict__ nodes, uint32_t n, uint32_t* __restrict__ isLeaf,
+                           uint32_t* __restrict__ group) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        isLeaf[i] = nodes[i].info.z;
+        group[i] = groupSize(nodes, i);
+    }
 }
 
 __global__ void kLayout(const BuildNode* __restrict__ nodes, uint32_t n, const uint32_t* __restrict__ leafPrefix,
-                        NodePair* __restrict__ pairs, uint2* __restrict__ leaves) {
+                        const uint32_t* __restrict__ groupStart, NodePair* __restrict__ pairs,
+                        uint2* __restrict__ leaves) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const BuildNode nd = nodes[i];
@@ -768,7 +815,7 @@ __global__ void kLayout(const BuildNode* __restrict__ nodes, uint32_t n, const u
         leaves[leafPrefix[i]] = make_uint2(nd.info.x, nd.info.y);
         return;
     }
-    pairs[i - leafPrefix[i]] = pairOf(nodes, leafPrefix, i);
+    writeGroup(nodes, leafPrefix, groupStart, i, pairs);
 }
 
 __global__ void kTriBlocks(const float3* __restrict__ pos, const uint32_t* __restrict__ idx,
@@ -858,6 +905,7 @@ struct BuiltBvh {
     uint32_t levels = 0;
     Counters counters{};
     BuildNode root{};
+    uint32_t rootRef = 0;  // the root's ref (group flags included)
 };
 
 // The GPU binned-SAH build over N primitive records that prep(rec, ctr)
@@ -995,29 +1043,41 @@ int buildGeneric(uint32_t N, Prep prep, BuiltBvh& out) {
     const uint32_t nNodes = hc.nodes;
     if (hc.overflow || nNodes > maxNodes) return fail(CR_ERR_DEVICE, "BVH build: node count %u exceeds %u", nNodes, maxNodes);
 
-    // 3. traversal layout
-    DevBuf<uint32_t> isLeaf, leafPrefix;
+    // 3. traversal layout: leaf-table indices and pair groups by exclusive scans
+    const uint32_t nLeaves = hc.leafCount;
+    if (nLeaves > ~(kLeafBit | kInlineLeafBit))  // leaf-table refs have 30 index bits
+        return fail(CR_ERR_UNSUPPORTED, "BVH has %u leaves; the limit is 2^30-1", nLeaves);
+    const uint32_t nPairs = nNodes - nLeaves;
+    if (nPairs > kMaxPairs)  // interior refs have 28 index bits
+        return fail(CR_ERR_UNSUPPORTED, "BVH has %u interior nodes; the limit is 2^28", nPairs);
+    DevBuf<uint32_t> isLeaf, leafPrefix, group, groupStart;
     CR_CUDA(isLeaf.alloc(nNodes));
     CR_CUDA(leafPrefix.alloc(nNodes));
-    kLeafFlags<<<blocksFor(nNodes, 256), 256>>>(nodes.p, nNodes, isLeaf.p);
+    CR_CUDA(group.alloc(nNodes));
+    CR_CUDA(groupStart.alloc(nNodes));
+    kLeafFlags<<<blocksFor(nNodes, 256), 256>>>(nodes.p, nNodes, isLeaf.p, group.p);
     CR_LAUNCH_CHECK();
     size_t scanBytes = 0;
     cub::DeviceScan::ExclusiveSum(nullptr, scanBytes, isLeaf.p, leafPrefix.p, (int)nNodes);
     DevBuf<uint8_t> scanTemp;
     CR_CUDA(scanTemp.alloc(scanBytes));
     CR_CUDA(cub::DeviceScan::ExclusiveSum(scanTemp.p, scanBytes, isLeaf.p, leafPrefix.p, (int)nNodes));
-    countLaunch(1);
-    const uint32_t nLeaves = hc.leafCount;
-    if (nLeaves > ~(kLeafBit | kInlineLeafBit))  // leaf-table refs have 30 index bits
-        return fail(CR_ERR_UNSUPPORTED, "BVH has %u leaves; the limit is 2^30-1", nLeaves);
-    const uint32_t nPairs = nNodes - nLeaves;
+    CR_CUDA(cub::DeviceScan::ExclusiveSum(scanTemp.p, scanBytes, group.p, groupStart.p, (int)nNodes));
+    countLaunch(2);
     DevBuf<NodePair> pairs;
     DevBuf<uint2> leaves;
     CR_CUDA(pairs.alloc(nPairs));
     CR_CUDA(leaves.alloc(nLeaves));
-    kLayout<<<blocksFor(nNodes, 256), 256>>>(nodes.p, nNodes, leafPrefix.p, pairs.p, leaves.p);
+    kLayout<<<blocksFor(nNodes, 256), 256>>>(nodes.p, nNodes, leafPrefix.p, groupStart.p, pairs.p, leaves.p);
     CR_LAUNCH_CHECK();
     CR_CUDA(cudaMemcpy(&out.root, nodes.p, sizeof(BuildNode), cudaMemcpyDeviceToHost));
+    out.rootRef = kLeafBit;  // a leaf root: leaf-table entry 0
+    if (!out.root.info.z) {  // the root is node 0, the first group top (pair 0)
+        BuildNode ch[2];
+        CR_CUDA(cudaMemcpy(&ch[0], nodes.p + out.root.info.x, sizeof(BuildNode), cudaMemcpyDeviceToHost));
+        CR_CUDA(cudaMemcpy(&ch[1], nodes.p + out.root.info.y, sizeof(BuildNode), cudaMemcpyDeviceToHost));
+        out.rootRef = kGroupTopBit | (ch[0].info.z ? 0u : kGroupLeftBit) | (ch[1].info.z ? 0u : kGroupRightBit);
+    }
     out.pairs = pairs.release();
     out.nPairs = nPairs;
     out.leaves = leaves.release();
@@ -1084,7 +1144,7 @@ int buildBvh(cr_scene* s) {
     s->rootMin = mk3(root.lo.x, root.lo.y, root.lo.z);
     s->rootMax = mk3(root.hi.x, root.hi.y, root.hi.z);
     s->rootFlags = degenerateFlags(s->rootMin, s->rootMax);
-    s->rootRef = root.info.z ? kLeafBit : 0u;
+    s->rootRef = b.rootRef;
 
     const Counters& hc = b.counters;
     cr_bvh_stats& st = s->stats;
@@ -1140,7 +1200,7 @@ int buildSphereBvh(cr_scene* s) {
     s->sphRootMin = mk3(root.lo.x, root.lo.y, root.lo.z);
     s->sphRootMax = mk3(root.hi.x, root.hi.y, root.hi.z);
     s->sphRootFlags = degenerateFlags(s->sphRootMin, s->sphRootMax);
-    s->sphRootRef = root.info.z ? kLeafBit : 0u;
+    s->sphRootRef = b.rootRef;
     s->sphHasRoot = 1;
     return CR_OK;
 }
@@ -1269,11 +1329,18 @@ int importBvh(cr_scene* s, const cr_bvh_node* in, uint32_t nodeCount, const uint
         leavesBefore += n.is_leaf;
     }
     const uint32_t nPairs = nodeCount - nLeaves;
+    if (nPairs > kMaxPairs) return fail(CR_ERR_UNSUPPORTED, "%u interior nodes; the limit is 2^28", nPairs);
+    std::vector<uint32_t> groupStart(nodeCount);
+    uint32_t pairsBefore = 0;
+    for (uint32_t k = 0; k < nodeCount; k++) {
+        groupStart[k] = pairsBefore;
+        pairsBefore += groupSize(nodes.data(), k);
+    }
     std::vector<NodePair> pairs(std::max<uint32_t>(nPairs, 1));
     std::vector<uint2> leaves(std::max<uint32_t>(nLeaves, 1));
     for (uint32_t k = 0; k < nodeCount; k++) {
         if (nodes[k].info.z) leaves[leafPrefix[k]] = make_uint2(nodes[k].info.x, nodes[k].info.y);
-        else pairs[k - leafPrefix[k]] = pairOf(nodes.data(), leafPrefix.data(), k);
+        else writeGroup(nodes.data(), leafPrefix.data(), groupStart.data(), k, pairs.data());
     }
     DevBuf<NodePair> dPairs;
     DevBuf<uint2> dLeaves;
@@ -1308,7 +1375,7 @@ int importBvh(cr_scene* s, const cr_bvh_node* in, uint32_t nodeCount, const uint
     s->rootMin = mk3(root.lo.x, root.lo.y, root.lo.z);
     s->rootMax = mk3(root.hi.x, root.hi.y, root.hi.z);
     s->rootFlags = degenerateFlags(s->rootMin, s->rootMax);
-    s->rootRef = root.info.z ? kLeafBit : 0u;
+    s->rootRef = root.info.z ? kLeafBit : topRef(nodes.data(), groupStart.data(), 0);
     s->hasRoot = 1;
     cr_bvh_stats& st = s->stats;
     st = cr_bvh_stats{};

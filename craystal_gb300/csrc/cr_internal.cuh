@@ -71,9 +71,10 @@ constexpr uint32_t kErrStackOverflow = 1u;
 //   p0 = (L.min.x, L.min.y, L.min.z, L.max.x)
 //   p1 = (L.max.y, L.max.z, R.min.x, R.min.y)
 //   p2 = (R.min.z, R.max.x, R.max.y, R.max.z)
-//   ref = (L.ref, R.ref, flags, 0).  A child ref with bit 31 clear is the
-//         pair index of an interior child; with bit 31 set it is a leaf,
-//         whose slot range is in the ref itself or in the leaf table
+//   ref = (L.ref, R.ref, flags, 0).  A child ref with bit 31 clear points
+//         at the pair of an interior child (its index and the group flags,
+//         kGroupTopBit below); with bit 31 set it is a leaf, whose slot
+//         range is in the ref itself or in the leaf table
 //         (kInlineLeafBit, below).  flags bits 0-2
 //         (left) and 3-5 (right) mark box axes thinner than FLT_EPSILON,
 //         which take the degenerate-slab branch of Math/AABB.cu:10-19.
@@ -135,15 +136,32 @@ struct CameraGpu {
     uint32_t width, height;
 };
 
-// Child refs.  Bit 31 clear: the pair index of an interior child.  Bit 31
-// set: a leaf.  A leaf of 1 to 7 slots that start below 2^27 carries its
-// range in the ref itself (bit 30 set, count in bits 27-29, first slot in
-// bits 0-26), so that opening it needs no load; any other leaf has bit 30
-// clear and bits 0-29 index the leaf table (first slot, count).
+// Child refs.  Bit 31 set: a leaf.  A leaf of 1 to 7 slots that start below
+// 2^27 carries its range in the ref itself (bit 30 set, count in bits 27-29,
+// first slot in bits 0-26), so that opening it needs no load; any other leaf
+// has bit 30 clear and bits 0-29 index the leaf table (first slot, count).
+//
+// Bit 31 clear: an interior child, whose pair index is bits 0-27.  The pairs
+// are laid out in groups (treelets of two levels): the pair of every
+// interior node at even depth (the root's depth is 0) is followed directly
+// by the pairs of its interior children, left before right.  A ref to the
+// top of a group has bit 30 set, bit 29 when the node's left child is
+// interior (its pair is the next one) and bit 28 when its right child is
+// (the pair after that, or the next one when the left child is a leaf).  A
+// ref to the second pair of a group carries no flags.  So a traversal that
+// reaches a group top knows, before any load, where both children's pairs
+// lie: the two levels of a group can be fetched at once.  A traversal that
+// walks one level at a time masks the flags off and sees a plain binary
+// tree.
 constexpr uint32_t kLeafBit = 0x80000000u;
 constexpr uint32_t kInlineLeafBit = 0x40000000u;
 constexpr uint32_t kInlineSlotMask = (1u << 27) - 1u;
 constexpr uint32_t kInlineMaxCount = 7u;
+constexpr uint32_t kGroupTopBit = 0x40000000u;
+constexpr uint32_t kGroupLeftBit = 0x20000000u;
+constexpr uint32_t kGroupRightBit = 0x10000000u;
+constexpr uint32_t kPairIndexMask = 0x0FFFFFFFu;
+constexpr uint32_t kMaxPairs = kPairIndexMask + 1u;
 
 __host__ __device__ __forceinline__ uint32_t leafRef(uint32_t tableIndex, uint32_t first, uint32_t count) {
     if (count >= 1u && count <= kInlineMaxCount && first <= kInlineSlotMask)

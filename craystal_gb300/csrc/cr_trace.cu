@@ -12,41 +12,19 @@ namespace {
 
 constexpr int kTraceThreads = kStackBlock;  // the top of the stack is in shared memory
 
-// One thread per ray: the form for scenes with analytic spheres, which are
-// tested first as SceneView::intersect does (a separate instance keeps the
-// triangle-only kernels free of the sphere code).
-template <bool kAnyHit, bool kSpheres>
-__global__ void __launch_bounds__(kTraceThreads) kTrace(const SceneView sc, const cr_ray* __restrict__ rays,
-                                                        uint64_t n, cr_hit* __restrict__ hits,
-                                                        uint8_t* __restrict__ occ) {
-    __shared__ SharedStackArea stk;
-    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float4* rp = reinterpret_cast<const float4*>(rays + i);
-    const float4 a = __ldg(rp), b = __ldg(rp + 1);
-    const TRay r = makeTRay(mk3(a.x, a.y, a.z), a.w, mk3(b.x, b.y, b.z), b.w);
-    THit h;
-    h.t = INFINITY;
-    h.u = h.v = 0.0f;
-    h.prim = CR_MISS;
-    bool hit = false;
-    if (kSpheres) hit = traverseSpheres<kAnyHit, kSharedStack>(sc, r, h, stk);
-    if (!(kAnyHit && hit)) hit |= traverse<kAnyHit, kSharedStack>(sc, r, h, stk);
-    if (kAnyHit) {
-        occ[i] = hit ? 1 : 0;
-    } else {
-        reinterpret_cast<float4*>(hits)[i] = hit ? make_float4(__uint_as_float(h.prim), h.t, h.u, h.v)
-                                                 : make_float4(__uint_as_float(CR_MISS), INFINITY, 0.0f, 0.0f);
-    }
-}
-
-// Triangle-only scenes: persistent blocks with dynamic ray fetch.  The
-// lanes of a warp take rays from a counter as they finish, at least kRefill
-// lanes at a time, so that a warp keeps most of its lanes busy until the
-// rays run out instead of waiting for its slowest ray (incoherent rays leave
-// a one-ray-per-thread warp with 6 of 32 lanes busy on average).  Every ray
-// is traversed exactly as in kTrace (the same cursor, order and culling);
-// only the lane that carries it changes.
+// Persistent blocks with dynamic ray fetch.  The lanes of a warp take rays
+// from a counter as they finish, at least kRefill lanes at a time, so that a
+// warp keeps most of its lanes busy until the rays run out instead of
+// waiting for its slowest ray (incoherent rays leave a one-ray-per-thread
+// warp with 6 of 32 lanes busy on average).  Every ray is traversed in the
+// reference's order with the reference's culling; only the lane that
+// carries it changes.
+//
+// kSpheres: the scene also holds analytic spheres, which are tested first,
+// as SceneView::intersect does (Scene/Scene.cu:5-14): a lane that takes a
+// ray walks the sphere BVH to the end at once (sphere trees are small), and
+// the triangle traversal then starts from the sphere hit's distance.  A
+// separate instance keeps the triangle-only kernel free of the sphere code.
 //
 // counter != nullptr: one zeroed device counter over all n rays, which
 // keeps every SM busy to the end (12 % faster than one ray per thread on the
@@ -56,7 +34,7 @@ __global__ void __launch_bounds__(kTraceThreads) kTrace(const SceneView sc, cons
 // one-slot-per-step traversal.
 constexpr int kRefill = 4;
 
-template <bool kAnyHit>
+template <bool kAnyHit, bool kSpheres>
 __global__ void __launch_bounds__(kTraceThreads) kTraceDyn(const SceneView sc, const cr_ray* __restrict__ rays,
                                                            uint64_t n, cr_hit* __restrict__ hits,
                                                            uint8_t* __restrict__ occ,
@@ -79,7 +57,7 @@ __global__ void __launch_bounds__(kTraceThreads) kTraceDyn(const SceneView sc, c
     stack.sh = stk;
     TravState cur;
     TRay r;
-    THit h;
+    THit h{INFINITY, 0.0f, 0.0f, CR_MISS};
     uint64_t idx = 0;
     bool active = false, exhausted = false;
     const int lane = threadIdx.x & 31;
@@ -109,8 +87,16 @@ __global__ void __launch_bounds__(kTraceThreads) kTraceDyn(const SceneView sc, c
                     h.t = INFINITY;
                     h.u = h.v = 0.0f;
                     h.prim = CR_MISS;
-                    if (travBegin(cur, bv, r)) active = true;
-                    else finish(false);
+                    bool sphereHit = false;
+                    if (kSpheres) sphereHit = traverseSpheres<kAnyHit, kSharedStack>(sc, r, h, stk);
+                    if (kAnyHit && sphereHit) {
+                        finish(true);
+                    } else if (travBegin(cur, bv, r)) {
+                        cur.isHit = sphereHit;
+                        active = true;
+                    } else {
+                        finish(sphereHit);
+                    }
                 }
             }
         }
@@ -129,20 +115,21 @@ __global__ void __launch_bounds__(kTraceThreads) kTraceDyn(const SceneView sc, c
 // asked).  Host threads may call at once: each entry is an atomic, and two
 // threads that both ask store the same value.
 constexpr int kOccDevices = 64;
-std::atomic<int> gOccupancy[kOccDevices][2];
+std::atomic<int> gOccupancy[kOccDevices][4];
 
-int traceDynBlocks(bool anyHit, uint64_t n) {
+template <bool kAnyHit, bool kSpheres>
+int traceDynBlocks(uint64_t n) {
     int dev = 0, sms = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    constexpr int kKind = (kAnyHit ? 1 : 0) + (kSpheres ? 2 : 0);
     int occ = 0;
-    if (dev >= 0 && dev < kOccDevices) occ = gOccupancy[dev][anyHit ? 1 : 0].load(std::memory_order_relaxed);
+    if (dev >= 0 && dev < kOccDevices) occ = gOccupancy[dev][kKind].load(std::memory_order_relaxed);
     if (!occ) {
         int b = 0;
-        if (anyHit) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kTraceDyn<true>, kTraceThreads, 0);
-        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kTraceDyn<false>, kTraceThreads, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kTraceDyn<kAnyHit, kSpheres>, kTraceThreads, 0);
         occ = b > 0 ? b : 1;
-        if (dev >= 0 && dev < kOccDevices) gOccupancy[dev][anyHit ? 1 : 0].store(occ, std::memory_order_relaxed);
+        if (dev >= 0 && dev < kOccDevices) gOccupancy[dev][kKind].store(occ, std::memory_order_relaxed);
     }
     const uint64_t perThread = (n + kTraceThreads - 1) / kTraceThreads;
     return (int)std::min<uint64_t>((uint64_t)sms * occ, std::max<uint64_t>(1, perThread));
@@ -159,20 +146,17 @@ int launchTrace(cr_scene* s, const cr_ray* rays, uint64_t n, cr_hit* hits, uint8
     const SceneView v = s->view();
     for (uint64_t off = 0; off < n; off += kMaxRaysPerLaunch) {
         const uint64_t m = std::min(n - off, kMaxRaysPerLaunch);
-        const unsigned blocks = (unsigned)((m + kTraceThreads - 1) / kTraceThreads);
-        if (s->sphHasRoot) {
-            kTrace<kAnyHit, true><<<blocks, kTraceThreads, 0, st>>>(v, rays + off, m, hits ? hits + off : nullptr,
-                                                                    occ ? occ + off : nullptr);
-            CR_LAUNCH_CHECK();
-            continue;
-        }
         unsigned long long* counter = nullptr;
         if (mayAllocate) {
             CR_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&counter), sizeof(unsigned long long), st));
             CR_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st));
         }
-        kTraceDyn<kAnyHit><<<traceDynBlocks(kAnyHit, m), kTraceThreads, 0, st>>>(
-            v, rays + off, m, hits ? hits + off : nullptr, occ ? occ + off : nullptr, counter);
+        if (s->sphHasRoot)
+            kTraceDyn<kAnyHit, true><<<traceDynBlocks<kAnyHit, true>(m), kTraceThreads, 0, st>>>(
+                v, rays + off, m, hits ? hits + off : nullptr, occ ? occ + off : nullptr, counter);
+        else
+            kTraceDyn<kAnyHit, false><<<traceDynBlocks<kAnyHit, false>(m), kTraceThreads, 0, st>>>(
+                v, rays + off, m, hits ? hits + off : nullptr, occ ? occ + off : nullptr, counter);
         CR_LAUNCH_CHECK();
         if (counter) CR_CUDA(cudaFreeAsync(counter, st));
     }

@@ -184,6 +184,9 @@ __device__ __forceinline__ Float8 ldg32(const void* p) {
     return r;
 }
 
+// Starts moving the line holding p towards L2 (no register result).
+__device__ __forceinline__ void prefetchL2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
 // The slot range [first, first + count) of a leaf ref: from the ref itself
 // (kInlineLeafBit) or from the leaf table.
 __device__ __forceinline__ void openLeaf(const uint2* leaves, uint32_t ref, uint32_t& ts, uint32_t& te) {
@@ -205,6 +208,12 @@ __device__ __forceinline__ void openLeaf(const uint2* leaves, uint32_t ref, uint
 template <bool kAnyHit>
 struct TriLeaf {
     const TriBlock* tris;
+    // the 128-byte lines of slots [ts, te) towards L2
+    __device__ __forceinline__ void prefetch(uint32_t ts, uint32_t te) const {
+        const uintptr_t a = reinterpret_cast<uintptr_t>(tris + ts) & ~uintptr_t(127);
+        const uintptr_t e = reinterpret_cast<uintptr_t>(tris + te);
+        for (uintptr_t x = a; x < e; x += 128) prefetchL2(reinterpret_cast<const void*>(x));
+    }
     __device__ __forceinline__ bool operator()(const TRay& r, THit& h, bool& isHit, uint32_t slot) const {
         float3 v0, e1, e2;
         uint32_t prim;
@@ -266,6 +275,7 @@ __device__ __forceinline__ float2 sphereUV(float4 s, const TRay& r, float t) {
 template <bool kAnyHit>
 struct SphereLeaf {
     const SphereBlock* blocks;
+    __device__ __forceinline__ void prefetch(uint32_t, uint32_t) const {}
     __device__ __forceinline__ bool operator()(const TRay& r, THit& h, bool& isHit, uint32_t slot) const {
         const float4* p = reinterpret_cast<const float4*>(blocks + slot);
         const float4 g = __ldg(p);
@@ -321,6 +331,32 @@ __device__ __forceinline__ bool travBegin(TravState& s, const BvhView& bv, const
     return bv.hasRoot && boxTest(bv.rootMin, bv.rootMax, bv.rootFlags, r, tr);
 }
 
+// One binary level: both child boxes of the pair (w0, w1), the reference's
+// near-first choice, the far child pushed when both pass.  Returns 1 when
+// s.e is now the near child, 0 when neither child passes (pop), -1 on a
+// stack overflow (reported through errFlags).
+template <class Stack>
+__device__ __forceinline__ int nodeLevel(const Float8& w0, const Float8& w1, TravState& s, Stack& stack,
+                                         uint32_t* errFlags, const TRay& r, float ct) {
+    const float4 p0 = w0.a, p1 = w0.b, p2 = w1.a;
+    const uint4 ref = make_uint4(__float_as_uint(w1.b.x), __float_as_uint(w1.b.y), __float_as_uint(w1.b.z), 0u);
+    float lt = INFINITY, rt = INFINITY;
+    const bool hl = boxTest(mk3(p0.x, p0.y, p0.z), mk3(p0.w, p1.x, p1.y), ref.z & 7u, r, lt);
+    const bool hr = boxTest(mk3(p1.z, p1.w, p2.x), mk3(p2.y, p2.z, p2.w), (ref.z >> 3) & 7u, r, rt);
+    const bool gl = hl && lt < ct, gr = hr && rt < ct;
+    // near = the child the reference pushes last: right when lt > rt
+    const bool rightNear = gl && gr ? lt > rt : gr;
+    if (gl && gr) {
+        if (s.sp >= kStackSize) {  // unreachable for depth <= 20; never overrun
+            atomicOr(errFlags, kErrStackOverflow);
+            return -1;
+        }
+        stack.put(s.sp++, rightNear ? make_uint2(ref.x, __float_as_uint(lt)) : make_uint2(ref.y, __float_as_uint(rt)));
+    }
+    s.e = rightNear ? make_uint2(ref.y, __float_as_uint(rt)) : make_uint2(ref.x, __float_as_uint(lt));
+    return (gl || gr) ? 1 : 0;
+}
+
 // One step; false once the traversal is over (an any-hit query that found
 // a hit stops at once).
 template <bool kAnyHit, class Leaf, class Stack>
@@ -329,32 +365,63 @@ __device__ __forceinline__ bool travStep(TravState& s, Stack& stack, const BvhVi
     bool pop = true;
     const bool culled = __uint_as_float(s.e.y) > h.t;
     if (s.ts < s.te || (s.e.x & kLeafBit) || culled) {
-        if (s.ts >= s.te && (s.e.x & kLeafBit) && !culled) openLeaf(bv.leaves, s.e.x, s.ts, s.te);
+        if (s.ts >= s.te && (s.e.x & kLeafBit) && !culled) {
+            openLeaf(bv.leaves, s.e.x, s.ts, s.te);
+#ifdef CR_EXP_PF_LEAF
+            leaf.prefetch(s.ts, s.te);
+#endif
+        }
         if (s.ts < s.te) {
             if (leaf(r, h, s.isHit, s.ts)) return false;
             pop = ++s.ts >= s.te;
         }
     } else {
-        const NodePair* np = bv.pairs + s.e.x;
+        const uint32_t ref = s.e.x;
+        const NodePair* np = bv.pairs + (ref & kPairIndexMask);
         const Float8 w0 = ldg32(&np->p0), w1 = ldg32(&np->p2);
-        const float4 p0 = w0.a, p1 = w0.b, p2 = w1.a;
-        const uint4 ref = make_uint4(__float_as_uint(w1.b.x), __float_as_uint(w1.b.y), __float_as_uint(w1.b.z), 0u);
-        float lt = INFINITY, rt = INFINITY;
-        const bool hl = boxTest(mk3(p0.x, p0.y, p0.z), mk3(p0.w, p1.x, p1.y), ref.z & 7u, r, lt);
-        const bool hr = boxTest(mk3(p1.z, p1.w, p2.x), mk3(p2.y, p2.z, p2.w), (ref.z >> 3) & 7u, r, rt);
-        const float ct = h.t;
-        const bool gl = hl && lt < ct, gr = hr && rt < ct;
-        // near = the child the reference pushes last: right when lt > rt
-        const bool rightNear = gl && gr ? lt > rt : gr;
-        if (gl && gr) {
-            if (s.sp >= kStackSize) {  // unreachable for depth <= 20; never overrun
-                atomicOr(errFlags, kErrStackOverflow);
-                return false;
-            }
-            stack.put(s.sp++, rightNear ? make_uint2(ref.x, __float_as_uint(lt)) : make_uint2(ref.y, __float_as_uint(rt)));
+#ifdef CR_EXP_WIDE
+        // a group top: both children's pairs follow it; load them with its own
+        const bool top = (ref & kGroupTopBit) != 0u;
+        const NodePair* rp = np + ((ref & kGroupLeftBit) ? 2 : 1);
+        Float8 l0, l1, r0, r1;
+        if (top && (ref & kGroupLeftBit)) {
+            l0 = ldg32(&np[1].p0);
+            l1 = ldg32(&np[1].p2);
         }
-        pop = !(gl || gr);
-        s.e = rightNear ? make_uint2(ref.y, __float_as_uint(rt)) : make_uint2(ref.x, __float_as_uint(lt));
+        if (top && (ref & kGroupRightBit)) {
+            r0 = ldg32(&rp->p0);
+            r1 = ldg32(&rp->p2);
+        }
+#endif
+#ifdef CR_EXP_PF_CHILD
+        if (ref & kGroupTopBit) {
+            if (ref & (kGroupLeftBit | kGroupRightBit)) prefetchL2(np + 1);
+            if ((ref & kGroupLeftBit) && (ref & kGroupRightBit)) prefetchL2(np + 2);
+        }
+#endif
+        const float ct = h.t;
+        int st = nodeLevel(w0, w1, s, stack, errFlags, r, ct);
+        if (st < 0) return false;
+#if defined(CR_EXP_WIDE) || defined(CR_EXP_WIDE_DEP)
+        // the near child is an interior node of this group: its level in the
+        // same step (nothing changes closestT in between, so the reference's
+        // pop-time cull of the near child never fires)
+#ifdef CR_EXP_WIDE_DEP
+        const bool top = (ref & kGroupTopBit) != 0u;
+#endif
+        if (st > 0 && top && !(s.e.x & kLeafBit)) {
+            const bool nearLeft = (ref & kGroupLeftBit) && s.e.x == (ref & kPairIndexMask) + 1u;
+#ifdef CR_EXP_WIDE
+            st = nearLeft ? nodeLevel(l0, l1, s, stack, errFlags, r, ct) : nodeLevel(r0, r1, s, stack, errFlags, r, ct);
+#else
+            const NodePair* cp = bv.pairs + s.e.x;
+            (void)nearLeft;
+            st = nodeLevel(ldg32(&cp->p0), ldg32(&cp->p2), s, stack, errFlags, r, ct);
+#endif
+            if (st < 0) return false;
+        }
+#endif
+        pop = st == 0;
     }
     if (pop) {
         if (s.sp == 0) return false;
