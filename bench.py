@@ -212,6 +212,32 @@ def l2_peak_gbs():
     return l2, hbm
 
 
+def two_level_extra(torch, sc, d_rays, n, ref_hits, one_level_ms, reps=5):
+    """The same cast with the two-level step (cr_scene_set_traversal): two
+    binary levels of a node group per step.  Device time per launch beside
+    the one-level step's, and whether every hit is the same bit for bit."""
+    import craystal_gb300 as cg
+    out_hits = torch.empty(n * 16, dtype=torch.uint8, device=d_rays.device)
+    s = torch.cuda.current_stream()
+    sc.set_traversal("two_level")
+    try:
+        for _ in range(2):
+            sc.trace_closest_device(d_rays.data_ptr(), n, out_hits.data_ptr(), s.cuda_stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for _ in range(reps):
+            sc.trace_closest_device(d_rays.data_ptr(), n, out_hits.data_ptr(), s.cuda_stream)
+        e1.record(s)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+    finally:
+        sc.set_traversal("one_level")
+    hits = out_hits.cpu().numpy().view(cg.HIT_DTYPE)
+    return {"ms_per_launch": round(ms, 3), "Mrays_s": round(n / ms / 1e3, 1),
+            "one_level_ms_per_launch": round(one_level_ms, 3), "two_over_one_time": round(ms / one_level_ms, 3),
+            "hits_equal_one_level": bool(np.array_equal(hits.view(np.uint32), ref_hits.view(np.uint32)))}
+
+
 def hbm_raycast_extra(torch, n_tris=1 << 23, n_rays=1 << 24, reps=5, with_oracle=True):
     """The ray cast on a scene far larger than L2: 8,388,608 random triangles
     (the C2 distribution, seed 2), 16,777,216 rays (seed 3).  Nodes and
@@ -243,6 +269,7 @@ def hbm_raycast_extra(torch, n_tris=1 << 23, n_rays=1 << 24, reps=5, with_oracle
     out = {"config": f"{n_tris} random triangles (C2 distribution), {n_rays} rays, closest hit",
            "bvh_device_mib": round(st["device_bytes"] / 2 ** 20, 1), "ms_per_launch": round(ms, 3),
            "Mrays_s": round(n_rays / ms / 1e3, 1)}
+    out["two_level_traversal"] = two_level_extra(torch, sc, d_rays, n_rays, d_hits.cpu().numpy(), ms)
     if with_oracle:
         import oracle
         threads = oracle.hardware_threads()
@@ -1093,6 +1120,7 @@ def run_ours(args):
     sc = Scene(data)
     build_wall = time.perf_counter() - t0
     st = sc.bvh_stats()
+    sc.set_traversal(args.traversal)
     rays = scenes.random_rays(N_RAYS, RAY_SEED)
     raw = torch.from_numpy(rays.view(np.uint8))
     d_rays = raw.to(f"cuda:{local}")
@@ -1152,6 +1180,8 @@ def run_ours(args):
                      "device_mib": round(st["device_bytes"] / 2 ** 20, 1)},
              "host_path_matches_device_path": same,
              "hit_fraction": round(float((hits_dev["prim"] != cg.CR_MISS).mean()), 4)}
+    if not args.skip_extra and world == 1:
+        extra["two_level_traversal"] = two_level_extra(torch, sc, d_rays, N_RAYS, hits_dev, kernel_ms)
     # the extras are single-GPU configurations (and time the CPU oracle on the
     # host's cores): a replica run under torchrun measures the ray cast only
     if not args.skip_extra and world == 1:
@@ -1263,6 +1293,8 @@ def main():
     ap.add_argument("--rays", type=int, default=N_RAYS, help="rays per step (profiling a smaller case)")
     ap.add_argument("--tris", type=int, default=N_TRIS, help="triangles (profiling a smaller case)")
     ap.add_argument("--hbm-rays", type=int, default=1 << 24, help="rays of the HBM-resident ray cast")
+    ap.add_argument("--traversal", choices=["one_level", "two_level"], default="one_level",
+                    help="traversal step of the headline ray cast (profiling the two-level step)")
     ap.add_argument("--only", choices=["path_tracer", "c1_parity", "hbm_raycast", "wavefront", "radiance_cache", "cache_frames", "batched_scenes",
                                        "large_scene", "radiance_cache_scene", "radiance_cache_network"],
                     help="run one secondary workload alone and print its figures (profiling)")

@@ -21,6 +21,8 @@ CR_DEVICE_ERROR_STACK_OVERFLOW = 1
 CR_MISS = 0xFFFFFFFF
 CR_NOALLOC_MAX_RAYS = 65536
 CR_NO_TEXTURE = 0xFFFFFFFF
+CR_TRAVERSAL_ONE_LEVEL = 0
+CR_TRAVERSAL_TWO_LEVEL = 1
 
 RAY_DTYPE = np.dtype([("o", "<f4", 3), ("tmin", "<f4"), ("d", "<f4", 3), ("tmax", "<f4")])
 HIT_DTYPE = np.dtype([("prim", "<u4"), ("t", "<f4"), ("u", "<f4"), ("v", "<f4")])
@@ -130,6 +132,7 @@ SIGNATURES = [
     ("cr_scene_bvh_import", ctypes.c_int, [_P, _P, _U32, _P]),
     ("cr_scene_check_errors", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint32)]),
     ("cr_scene_set_error_flags", ctypes.c_int, [_P, _U32]),
+    ("cr_scene_set_traversal", ctypes.c_int, [_P, _U32]),
     ("cr_scene_set_camera", ctypes.c_int, [_P, ctypes.POINTER(CrCamera)]),
     ("cr_scene_set_environment", ctypes.c_int, [_P, _P]),
     ("cr_scene_set_sphere_lights", ctypes.c_int, [_P, _P, _U32]),

@@ -313,6 +313,14 @@ class Scene:
             raise ValueError(f"prim_map has {len(prim_map)} entries; the scene has {self.n_tris} triangles")
         check(load().cr_scene_bvh_import(self._h, ptr(nodes), len(nodes), ptr(prim_map)))
 
+    def set_traversal(self, mode: str):
+        """"one_level" (default) or "two_level": how the ray-cast queries step
+        through the BVH (cr_scene_set_traversal).  The hits are the same."""
+        modes = {"one_level": _lib.CR_TRAVERSAL_ONE_LEVEL, "two_level": _lib.CR_TRAVERSAL_TWO_LEVEL}
+        if mode not in modes:
+            raise ValueError(f"traversal mode {mode!r}; one of {sorted(modes)}")
+        check(load().cr_scene_set_traversal(self._h, modes[mode]))
+
     def check_errors(self) -> int:
         """Waits for the device, then reports (CrayError, code CR_ERR_DEVICE)
         and clears the errors kernels raised on this scene; returns 0."""

@@ -733,6 +733,47 @@ __global__ void __launch_bounds__(kSubtreeWarps * 32) kSubtree(const SmallTask* 
 // ---------------------------------------------------------------------------
 // traversal layout
 // ---------------------------------------------------------------------------
+__global__ void kLeafFlags(const BuildNode* __restrict__ nodes, uint32_t n, uint32_t* __restrict__ isLeaf) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) isLeaf[i] = nodes[i].info.z;
+}
+
+__host__ __device__ __forceinline__ uint32_t childRef(const BuildNode* nodes, const uint32_t* leafPrefix, uint32_t c) {
+    const BuildNode& n = nodes[c];
+    return n.info.z ? leafRef(leafPrefix[c], n.info.x, n.info.y) : (c - leafPrefix[c]);
+}
+
+// The NodePair of interior node i: both children's boxes, refs and
+// degenerate-axis flags.  Interior node i becomes pair i - leafPrefix[i].
+__host__ __device__ __forceinline__ NodePair pairOf(const BuildNode* nodes, const uint32_t* leafPrefix, uint32_t i) {
+    const BuildNode& nd = nodes[i];
+    const BuildNode& L = nodes[nd.info.x];
+    const BuildNode& R = nodes[nd.info.y];
+    NodePair p;
+    p.p0 = make_float4(L.lo.x, L.lo.y, L.lo.z, L.hi.x);
+    p.p1 = make_float4(L.hi.y, L.hi.z, R.lo.x, R.lo.y);
+    p.p2 = make_float4(R.lo.z, R.hi.x, R.hi.y, R.hi.z);
+    uint32_t fl = degenerateFlags(mk3(L.lo.x, L.lo.y, L.lo.z), mk3(L.hi.x, L.hi.y, L.hi.z)) |
+                  (degenerateFlags(mk3(R.lo.x, R.lo.y, R.lo.z), mk3(R.hi.x, R.hi.y, R.hi.z)) << 3);
+    p.ref = make_uint4(childRef(nodes, leafPrefix, nd.info.x), childRef(nodes, leafPrefix, nd.info.y), fl, 0u);
+    return p;
+}
+
+__global__ void kLayout(const BuildNode* __restrict__ nodes, uint32_t n, const uint32_t* __restrict__ leafPrefix,
+                        NodePair* __restrict__ pairs, uint2* __restrict__ leaves) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const BuildNode nd = nodes[i];
+    if (nd.info.z) {
+        leaves[leafPrefix[i]] = make_uint2(nd.info.x, nd.info.y);
+        return;
+    }
+    pairs[i - leafPrefix[i]] = pairOf(nodes, leafPrefix, i);
+}
+
+// ---------------------------------------------------------------------------
+// the grouped copy of the pairs, for the two-level traversal step
+// ---------------------------------------------------------------------------
 __host__ __device__ __forceinline__ bool isInterior(const BuildNode* nodes, uint32_t c) { return nodes[c].info.z == 0u; }
 
 // Pairs in node i's group: 1 + its interior children for an interior node at
@@ -752,40 +793,31 @@ __host__ __device__ __forceinline__ uint32_t topRef(const BuildNode* nodes, cons
            (isInterior(nodes, nd.info.y) ? kGroupRightBit : 0u);
 }
 
-// The NodePair of interior node i at pair index p: both children's boxes,
-// refs and degenerate-axis flags.  The children of a group top (top = true)
-// are the group's second-level pairs at p + 1 and after; the interior
-// children of a second-level node are group tops of their own.
+// The NodePair of interior node i at grouped index p.  The children of a
+// group top (top = true) are the group's second-level pairs at p + 1 and
+// after; the interior children of a second-level node are group tops.
 __host__ __device__ __forceinline__ NodePair groupPair(const BuildNode* nodes, const uint32_t* leafPrefix,
                                                        const uint32_t* groupStart, uint32_t i, bool top, uint32_t p) {
+    NodePair q = pairOf(nodes, leafPrefix, i);
     const BuildNode& nd = nodes[i];
-    const BuildNode& L = nodes[nd.info.x];
-    const BuildNode& R = nodes[nd.info.y];
-    NodePair q;
-    q.p0 = make_float4(L.lo.x, L.lo.y, L.lo.z, L.hi.x);
-    q.p1 = make_float4(L.hi.y, L.hi.z, R.lo.x, R.lo.y);
-    q.p2 = make_float4(R.lo.z, R.hi.x, R.hi.y, R.hi.z);
-    const uint32_t fl = degenerateFlags(mk3(L.lo.x, L.lo.y, L.lo.z), mk3(L.hi.x, L.hi.y, L.hi.z)) |
-                        (degenerateFlags(mk3(R.lo.x, R.lo.y, R.lo.z), mk3(R.hi.x, R.hi.y, R.hi.z)) << 3);
-    uint32_t ref[2];
     uint32_t next = p + 1u;
+    uint32_t* ref[2] = {&q.ref.x, &q.ref.y};
     for (int k = 0; k < 2; k++) {
         const uint32_t c = k == 0 ? nd.info.x : nd.info.y;
-        const BuildNode& n = nodes[c];
-        if (n.info.z) ref[k] = leafRef(leafPrefix[c], n.info.x, n.info.y);
-        else if (top) ref[k] = next++;
-        else ref[k] = topRef(nodes, groupStart, c);
+        if (!isInterior(nodes, c)) continue;  // leaf refs are the same in both layouts
+        *ref[k] = top ? next++ : topRef(nodes, groupStart, c);
     }
-    q.ref = make_uint4(ref[0], ref[1], fl, 0u);
     return q;
 }
 
-// Writes group top i's pair and its second-level pairs (and nothing for
-// other nodes); every pair is written exactly once.
-__host__ __device__ __forceinline__ void writeGroup(const BuildNode* nodes, const uint32_t* leafPrefix,
-                                                    const uint32_t* groupStart, uint32_t i, NodePair* pairs) {
-    if (groupSize(nodes, i) == 0u) return;
-    const BuildNode& nd = nodes[i];
+// Group top i: its own pair and its second-level pairs.  Every interior
+// node's pair is written exactly once, by the top of its group.
+__global__ void kGroupLayout(const BuildNode* __restrict__ nodes, uint32_t n, const uint32_t* __restrict__ leafPrefix,
+                             const uint32_t* __restrict__ groupStart, NodePair* __restrict__ pairs,
+                             uint32_t* __restrict__ rootRef) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || groupSize(nodes, i) == 0u) return;
+    const BuildNode nd = nodes[i];
     const uint32_t p = groupStart[i];
     pairs[p] = groupPair(nodes, leafPrefix, groupStart, i, true, p);
     uint32_t q = p + 1u;
@@ -794,28 +826,16 @@ __host__ __device__ __forceinline__ void writeGroup(const BuildNode* nodes, cons
             pairs[q] = groupPair(nodes, leafPrefix, groupStart, c, false, q);
             q++;
         }
+    if (i == 0) *rootRef = topRef(nodes, groupStart, 0);  // node 0 is the root
 }
 
-__global__ void kLeafFlags(const BuildNode* __restrict__ nodes, uint32_t n, uint32_t* __restrict__ isLeaf,
-                           uint32_t* __restrict__ group) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void kGroupFlags(const BuildNode* __restrict__ nodes, uint32_t n, uint32_t* __restrict__ isLeaf,
+                            uint32_t* __restrict__ group) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) {
         isLeaf[i] = nodes[i].info.z;
         group[i] = groupSize(nodes, i);
     }
-}
-
-__global__ void kLayout(const BuildNode* __restrict__ nodes, uint32_t n, const uint32_t* __restrict__ leafPrefix,
-                        const uint32_t* __restrict__ groupStart, NodePair* __restrict__ pairs,
-                        uint2* __restrict__ leaves) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const BuildNode nd = nodes[i];
-    if (nd.info.z) {
-        leaves[leafPrefix[i]] = make_uint2(nd.info.x, nd.info.y);
-        return;
-    }
-    writeGroup(nodes, leafPrefix, groupStart, i, pairs);
 }
 
 __global__ void kTriBlocks(const float3* __restrict__ pos, const uint32_t* __restrict__ idx,
@@ -905,7 +925,6 @@ struct BuiltBvh {
     uint32_t levels = 0;
     Counters counters{};
     BuildNode root{};
-    uint32_t rootRef = 0;  // the root's ref (group flags included)
 };
 
 // The GPU binned-SAH build over N primitive records that prep(rec, ctr)
@@ -1043,41 +1062,29 @@ int buildGeneric(uint32_t N, Prep prep, BuiltBvh& out) {
     const uint32_t nNodes = hc.nodes;
     if (hc.overflow || nNodes > maxNodes) return fail(CR_ERR_DEVICE, "BVH build: node count %u exceeds %u", nNodes, maxNodes);
 
-    // 3. traversal layout: leaf-table indices and pair groups by exclusive scans
-    const uint32_t nLeaves = hc.leafCount;
-    if (nLeaves > ~(kLeafBit | kInlineLeafBit))  // leaf-table refs have 30 index bits
-        return fail(CR_ERR_UNSUPPORTED, "BVH has %u leaves; the limit is 2^30-1", nLeaves);
-    const uint32_t nPairs = nNodes - nLeaves;
-    if (nPairs > kMaxPairs)  // interior refs have 28 index bits
-        return fail(CR_ERR_UNSUPPORTED, "BVH has %u interior nodes; the limit is 2^28", nPairs);
-    DevBuf<uint32_t> isLeaf, leafPrefix, group, groupStart;
+    // 3. traversal layout
+    DevBuf<uint32_t> isLeaf, leafPrefix;
     CR_CUDA(isLeaf.alloc(nNodes));
     CR_CUDA(leafPrefix.alloc(nNodes));
-    CR_CUDA(group.alloc(nNodes));
-    CR_CUDA(groupStart.alloc(nNodes));
-    kLeafFlags<<<blocksFor(nNodes, 256), 256>>>(nodes.p, nNodes, isLeaf.p, group.p);
+    kLeafFlags<<<blocksFor(nNodes, 256), 256>>>(nodes.p, nNodes, isLeaf.p);
     CR_LAUNCH_CHECK();
     size_t scanBytes = 0;
     cub::DeviceScan::ExclusiveSum(nullptr, scanBytes, isLeaf.p, leafPrefix.p, (int)nNodes);
     DevBuf<uint8_t> scanTemp;
     CR_CUDA(scanTemp.alloc(scanBytes));
     CR_CUDA(cub::DeviceScan::ExclusiveSum(scanTemp.p, scanBytes, isLeaf.p, leafPrefix.p, (int)nNodes));
-    CR_CUDA(cub::DeviceScan::ExclusiveSum(scanTemp.p, scanBytes, group.p, groupStart.p, (int)nNodes));
-    countLaunch(2);
+    countLaunch(1);
+    const uint32_t nLeaves = hc.leafCount;
+    if (nLeaves > ~(kLeafBit | kInlineLeafBit))  // leaf-table refs have 30 index bits
+        return fail(CR_ERR_UNSUPPORTED, "BVH has %u leaves; the limit is 2^30-1", nLeaves);
+    const uint32_t nPairs = nNodes - nLeaves;
     DevBuf<NodePair> pairs;
     DevBuf<uint2> leaves;
     CR_CUDA(pairs.alloc(nPairs));
     CR_CUDA(leaves.alloc(nLeaves));
-    kLayout<<<blocksFor(nNodes, 256), 256>>>(nodes.p, nNodes, leafPrefix.p, groupStart.p, pairs.p, leaves.p);
+    kLayout<<<blocksFor(nNodes, 256), 256>>>(nodes.p, nNodes, leafPrefix.p, pairs.p, leaves.p);
     CR_LAUNCH_CHECK();
     CR_CUDA(cudaMemcpy(&out.root, nodes.p, sizeof(BuildNode), cudaMemcpyDeviceToHost));
-    out.rootRef = kLeafBit;  // a leaf root: leaf-table entry 0
-    if (!out.root.info.z) {  // the root is node 0, the first group top (pair 0)
-        BuildNode ch[2];
-        CR_CUDA(cudaMemcpy(&ch[0], nodes.p + out.root.info.x, sizeof(BuildNode), cudaMemcpyDeviceToHost));
-        CR_CUDA(cudaMemcpy(&ch[1], nodes.p + out.root.info.y, sizeof(BuildNode), cudaMemcpyDeviceToHost));
-        out.rootRef = kGroupTopBit | (ch[0].info.z ? 0u : kGroupLeftBit) | (ch[1].info.z ? 0u : kGroupRightBit);
-    }
     out.pairs = pairs.release();
     out.nPairs = nPairs;
     out.leaves = leaves.release();
@@ -1144,7 +1151,7 @@ int buildBvh(cr_scene* s) {
     s->rootMin = mk3(root.lo.x, root.lo.y, root.lo.z);
     s->rootMax = mk3(root.hi.x, root.hi.y, root.hi.z);
     s->rootFlags = degenerateFlags(s->rootMin, s->rootMax);
-    s->rootRef = b.rootRef;
+    s->rootRef = root.info.z ? kLeafBit : 0u;
 
     const Counters& hc = b.counters;
     cr_bvh_stats& st = s->stats;
@@ -1200,7 +1207,7 @@ int buildSphereBvh(cr_scene* s) {
     s->sphRootMin = mk3(root.lo.x, root.lo.y, root.lo.z);
     s->sphRootMax = mk3(root.hi.x, root.hi.y, root.hi.z);
     s->sphRootFlags = degenerateFlags(s->sphRootMin, s->sphRootMax);
-    s->sphRootRef = b.rootRef;
+    s->sphRootRef = root.info.z ? kLeafBit : 0u;
     s->sphHasRoot = 1;
     return CR_OK;
 }
@@ -1329,18 +1336,11 @@ int importBvh(cr_scene* s, const cr_bvh_node* in, uint32_t nodeCount, const uint
         leavesBefore += n.is_leaf;
     }
     const uint32_t nPairs = nodeCount - nLeaves;
-    if (nPairs > kMaxPairs) return fail(CR_ERR_UNSUPPORTED, "%u interior nodes; the limit is 2^28", nPairs);
-    std::vector<uint32_t> groupStart(nodeCount);
-    uint32_t pairsBefore = 0;
-    for (uint32_t k = 0; k < nodeCount; k++) {
-        groupStart[k] = pairsBefore;
-        pairsBefore += groupSize(nodes.data(), k);
-    }
     std::vector<NodePair> pairs(std::max<uint32_t>(nPairs, 1));
     std::vector<uint2> leaves(std::max<uint32_t>(nLeaves, 1));
     for (uint32_t k = 0; k < nodeCount; k++) {
         if (nodes[k].info.z) leaves[leafPrefix[k]] = make_uint2(nodes[k].info.x, nodes[k].info.y);
-        else writeGroup(nodes.data(), leafPrefix.data(), groupStart.data(), k, pairs.data());
+        else pairs[k - leafPrefix[k]] = pairOf(nodes.data(), leafPrefix.data(), k);
     }
     DevBuf<NodePair> dPairs;
     DevBuf<uint2> dLeaves;
@@ -1360,9 +1360,10 @@ int importBvh(cr_scene* s, const cr_bvh_node* in, uint32_t nodeCount, const uint
     CR_LAUNCH_CHECK();
     CR_CUDA(cudaDeviceSynchronize());
     // the new tree is complete: drop the old one (cudaFree waits for queries still using it)
-    void* old[] = {s->pairs, s->leaves, s->tris, s->slotToPrim, s->buildNodes};
+    void* old[] = {s->pairs, s->leaves, s->tris, s->slotToPrim, s->buildNodes, s->groupPairs};
     for (void* p : old)
         if (p) cudaFree(p);
+    s->groupPairs = nullptr;
     const BuildNode& root = nodes[0];
     s->pairs = dPairs.release();
     s->nPairs = nPairs;
@@ -1375,7 +1376,7 @@ int importBvh(cr_scene* s, const cr_bvh_node* in, uint32_t nodeCount, const uint
     s->rootMin = mk3(root.lo.x, root.lo.y, root.lo.z);
     s->rootMax = mk3(root.hi.x, root.hi.y, root.hi.z);
     s->rootFlags = degenerateFlags(s->rootMin, s->rootMax);
-    s->rootRef = root.info.z ? kLeafBit : topRef(nodes.data(), groupStart.data(), 0);
+    s->rootRef = root.info.z ? kLeafBit : 0u;
     s->hasRoot = 1;
     cr_bvh_stats& st = s->stats;
     st = cr_bvh_stats{};
@@ -1391,6 +1392,44 @@ int importBvh(cr_scene* s, const cr_bvh_node* in, uint32_t nodeCount, const uint
     }
     st.build_ms = 0.0;
     st.device_bytes = (uint64_t)nPairs * sizeof(NodePair) + (uint64_t)nLeaves * sizeof(uint2) + nSlots * sizeof(TriBlock);
+    return s->traversal == CR_TRAVERSAL_TWO_LEVEL ? buildGroupedPairs(s) : CR_OK;
+}
+
+// The scene's pairs again, laid out in two-level groups for the two-level
+// step: from the kept build records (breadth-first, depths included), with
+// the same leaf table.  Replaces an earlier grouped copy.
+int buildGroupedPairs(cr_scene* s) {
+    if (s->groupPairs) cudaFree(s->groupPairs);
+    s->groupPairs = nullptr;
+    s->groupRootRef = s->rootRef;
+    if (!s->hasRoot || s->nPairs == 0) return CR_OK;  // a leaf root: nothing to group
+    if (s->nPairs > kMaxPairs)
+        return fail(CR_ERR_UNSUPPORTED, "the two-level step takes at most 2^28 interior nodes (the tree has %u)",
+                    s->nPairs);
+    const uint32_t n = s->nBuildNodes;
+    DevBuf<uint32_t> isLeaf, leafPrefix, group, groupStart, rootRef;
+    CR_CUDA(isLeaf.alloc(n));
+    CR_CUDA(leafPrefix.alloc(n));
+    CR_CUDA(group.alloc(n));
+    CR_CUDA(groupStart.alloc(n));
+    CR_CUDA(rootRef.alloc(1));
+    kGroupFlags<<<blocksFor(n, 256), 256>>>(s->buildNodes, n, isLeaf.p, group.p);
+    CR_LAUNCH_CHECK();
+    size_t scanBytes = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, scanBytes, isLeaf.p, leafPrefix.p, (int)n);
+    DevBuf<uint8_t> scanTemp;
+    CR_CUDA(scanTemp.alloc(scanBytes));
+    CR_CUDA(cub::DeviceScan::ExclusiveSum(scanTemp.p, scanBytes, isLeaf.p, leafPrefix.p, (int)n));
+    CR_CUDA(cub::DeviceScan::ExclusiveSum(scanTemp.p, scanBytes, group.p, groupStart.p, (int)n));
+    countLaunch(2);
+    DevBuf<NodePair> pairs;
+    CR_CUDA(pairs.alloc(s->nPairs));
+    kGroupLayout<<<blocksFor(n, 256), 256>>>(s->buildNodes, n, leafPrefix.p, groupStart.p, pairs.p, rootRef.p);
+    CR_LAUNCH_CHECK();
+    uint32_t rr = 0;
+    CR_CUDA(cudaMemcpy(&rr, rootRef.p, sizeof(rr), cudaMemcpyDeviceToHost));
+    s->groupPairs = pairs.release();
+    s->groupRootRef = rr;
     return CR_OK;
 }
 

@@ -103,7 +103,8 @@ void freeScene(cr_scene* s) {
     void* ptrs[] = {s->pos,  s->nrm,      s->uv,         s->idx,        s->primToMesh, s->meshes,
                     s->mats, s->emissive, s->pairs,      s->leaves,     s->tris,       s->slotToPrim,
                     s->buildNodes, s->errFlags, s->filmRgb, s->filmW, s->rayCounter, s->spheres, s->sphereEm,
-                    s->texels, s->texDescs, s->sphGeom, s->sphMat, s->sphPairs, s->sphLeaves, s->sphBlocks};
+                    s->texels, s->texDescs, s->sphGeom, s->sphMat, s->sphPairs, s->sphLeaves, s->sphBlocks,
+                    s->groupPairs};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     freeCacheBuffers(s->cacheBuffers);
@@ -439,6 +440,25 @@ int cr_scene_set_error_flags(cr_scene* scene, uint32_t flags) {
     CR_CUDA(cudaMemcpy(&err, scene->errFlags, sizeof(err), cudaMemcpyDeviceToHost));
     err |= flags;
     CR_CUDA(cudaMemcpy(scene->errFlags, &err, sizeof(err), cudaMemcpyHostToDevice));
+    return CR_OK;
+}
+
+int cr_scene_set_traversal(cr_scene* scene, uint32_t mode) {
+    clearError();
+    if (!scene) return fail(CR_ERR_INVALID_ARGUMENT, "scene is NULL");
+    if (mode != CR_TRAVERSAL_ONE_LEVEL && mode != CR_TRAVERSAL_TWO_LEVEL)
+        return fail(CR_ERR_INVALID_ARGUMENT, "traversal mode %u (CR_TRAVERSAL_ONE_LEVEL or CR_TRAVERSAL_TWO_LEVEL)",
+                    mode);
+    CR_CUDA(cudaSetDevice(scene->device));
+    if (mode == CR_TRAVERSAL_TWO_LEVEL && !scene->groupPairs) {
+        int rc = buildGroupedPairs(scene);
+        if (rc) return rc;
+    } else if (mode == CR_TRAVERSAL_ONE_LEVEL && scene->groupPairs) {
+        CR_CUDA(cudaDeviceSynchronize());  // queries still in flight may read the copy
+        cudaFree(scene->groupPairs);
+        scene->groupPairs = nullptr;
+    }
+    scene->traversal = mode;
     return CR_OK;
 }
 

@@ -136,23 +136,21 @@ struct CameraGpu {
     uint32_t width, height;
 };
 
-// Child refs.  Bit 31 set: a leaf.  A leaf of 1 to 7 slots that start below
-// 2^27 carries its range in the ref itself (bit 30 set, count in bits 27-29,
-// first slot in bits 0-26), so that opening it needs no load; any other leaf
-// has bit 30 clear and bits 0-29 index the leaf table (first slot, count).
+// Child refs.  Bit 31 clear: the pair index of an interior child.  Bit 31
+// set: a leaf.  A leaf of 1 to 7 slots that start below 2^27 carries its
+// range in the ref itself (bit 30 set, count in bits 27-29, first slot in
+// bits 0-26), so that opening it needs no load; any other leaf has bit 30
+// clear and bits 0-29 index the leaf table (first slot, count).
 //
-// Bit 31 clear: an interior child, whose pair index is bits 0-27.  The pairs
-// are laid out in groups (treelets of two levels): the pair of every
-// interior node at even depth (the root's depth is 0) is followed directly
-// by the pairs of its interior children, left before right.  A ref to the
-// top of a group has bit 30 set, bit 29 when the node's left child is
-// interior (its pair is the next one) and bit 28 when its right child is
-// (the pair after that, or the next one when the left child is a leaf).  A
-// ref to the second pair of a group carries no flags.  So a traversal that
-// reaches a group top knows, before any load, where both children's pairs
-// lie: the two levels of a group can be fetched at once.  A traversal that
-// walks one level at a time masks the flags off and sees a plain binary
-// tree.
+// The grouped copy of the pairs (built for the two-level traversal step,
+// cr_scene_set_traversal) stores them in two-level groups instead: the pair
+// of every interior node at even depth (the root's depth is 0) is followed
+// directly by the pairs of its interior children, left before right.  There
+// an interior ref holds the pair index in bits 0-27; a ref to the top of a
+// group has bit 30 set, bit 29 when the node's left child is interior (its
+// pair is the next one) and bit 28 when its right child is (the pair after
+// that, or the next one when the left child is a leaf); a ref to the second
+// pair of a group carries no flags.  Leaf refs are the same in both layouts.
 constexpr uint32_t kLeafBit = 0x80000000u;
 constexpr uint32_t kInlineLeafBit = 0x40000000u;
 constexpr uint32_t kInlineSlotMask = (1u << 27) - 1u;
@@ -235,6 +233,9 @@ struct cr_scene {
     uint32_t rootRef = 0, rootFlags = 0, hasRoot = 0;
     float3 rootMin{0, 0, 0}, rootMax{0, 0, 0};
     cr_bvh_stats stats{};
+    uint32_t traversal = CR_TRAVERSAL_ONE_LEVEL;  // of the ray-cast queries
+    cr::NodePair* groupPairs = nullptr;           // the grouped copy (two-level step only)
+    uint32_t groupRootRef = 0;
     uint32_t* errFlags = nullptr;
     // camera + film
     bool hasCamera = false;
@@ -320,6 +321,7 @@ int buildBvh(cr_scene* s);
 int buildSphereBvh(cr_scene* s);
 int exportBvh(const cr_scene* s, cr_bvh_node* nodes, uint32_t* primMap);
 int importBvh(cr_scene* s, const cr_bvh_node* nodes, uint32_t nodeCount, const uint32_t* primMap);
+int buildGroupedPairs(cr_scene* s);
 // implemented in cr_trace.cu
 // mayAllocate = false: no device allocation (the no-allocation entry point)
 int traceClosestDevice(cr_scene* s, const cr_ray* rays, uint64_t n, cr_hit* hits, cudaStream_t st,

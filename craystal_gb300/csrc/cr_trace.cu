@@ -26,6 +26,9 @@ constexpr int kTraceThreads = kStackBlock;  // the top of the stack is in shared
 // the triangle traversal then starts from the sphere hit's distance.  A
 // separate instance keeps the triangle-only kernel free of the sphere code.
 //
+// kTwoLevel: the two-level step (travStep), chosen per scene with
+// cr_scene_set_traversal.
+//
 // counter != nullptr: one zeroed device counter over all n rays, which
 // keeps every SM busy to the end (12 % faster than one ray per thread on the
 // 16M-ray cast).  nullptr: block b takes rays [b * chunk, (b + 1) * chunk)
@@ -34,7 +37,7 @@ constexpr int kTraceThreads = kStackBlock;  // the top of the stack is in shared
 // one-slot-per-step traversal.
 constexpr int kRefill = 4;
 
-template <bool kAnyHit, bool kSpheres>
+template <bool kAnyHit, bool kSpheres, bool kTwoLevel>
 __global__ void __launch_bounds__(kTraceThreads) kTraceDyn(const SceneView sc, const cr_ray* __restrict__ rays,
                                                            uint64_t n, cr_hit* __restrict__ hits,
                                                            uint8_t* __restrict__ occ,
@@ -104,7 +107,7 @@ __global__ void __launch_bounds__(kTraceThreads) kTraceDyn(const SceneView sc, c
             if (exhausted) break;
             continue;  // every lane idle: the next round refills all 32
         }
-        if (active && !travStep<kAnyHit>(cur, stack, bv, sc.errFlags, leaf, r, h)) {
+        if (active && !travStep<kAnyHit, TriLeaf<kAnyHit>, TravStack<kSharedStack>, kTwoLevel>(cur, stack, bv, sc.errFlags, leaf, r, h)) {
             finish(cur.isHit);
             active = false;
         }
@@ -115,19 +118,19 @@ __global__ void __launch_bounds__(kTraceThreads) kTraceDyn(const SceneView sc, c
 // asked).  Host threads may call at once: each entry is an atomic, and two
 // threads that both ask store the same value.
 constexpr int kOccDevices = 64;
-std::atomic<int> gOccupancy[kOccDevices][4];
+std::atomic<int> gOccupancy[kOccDevices][8];
 
-template <bool kAnyHit, bool kSpheres>
+template <bool kAnyHit, bool kSpheres, bool kTwoLevel>
 int traceDynBlocks(uint64_t n) {
     int dev = 0, sms = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    constexpr int kKind = (kAnyHit ? 1 : 0) + (kSpheres ? 2 : 0);
+    constexpr int kKind = (kAnyHit ? 1 : 0) + (kSpheres ? 2 : 0) + (kTwoLevel ? 4 : 0);
     int occ = 0;
     if (dev >= 0 && dev < kOccDevices) occ = gOccupancy[dev][kKind].load(std::memory_order_relaxed);
     if (!occ) {
         int b = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kTraceDyn<kAnyHit, kSpheres>, kTraceThreads, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kTraceDyn<kAnyHit, kSpheres, kTwoLevel>, kTraceThreads, 0);
         occ = b > 0 ? b : 1;
         if (dev >= 0 && dev < kOccDevices) gOccupancy[dev][kKind].store(occ, std::memory_order_relaxed);
     }
@@ -143,7 +146,6 @@ constexpr uint64_t kMaxRaysPerLaunch = 0x7fffffffull * kTraceThreads;
 template <bool kAnyHit>
 int launchTrace(cr_scene* s, const cr_ray* rays, uint64_t n, cr_hit* hits, uint8_t* occ, cudaStream_t st,
                 bool mayAllocate) {
-    const SceneView v = s->view();
     for (uint64_t off = 0; off < n; off += kMaxRaysPerLaunch) {
         const uint64_t m = std::min(n - off, kMaxRaysPerLaunch);
         unsigned long long* counter = nullptr;
@@ -151,12 +153,26 @@ int launchTrace(cr_scene* s, const cr_ray* rays, uint64_t n, cr_hit* hits, uint8
             CR_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&counter), sizeof(unsigned long long), st));
             CR_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st));
         }
-        if (s->sphHasRoot)
-            kTraceDyn<kAnyHit, true><<<traceDynBlocks<kAnyHit, true>(m), kTraceThreads, 0, st>>>(
-                v, rays + off, m, hits ? hits + off : nullptr, occ ? occ + off : nullptr, counter);
+        cr_hit* h = hits ? hits + off : nullptr;
+        uint8_t* o = occ ? occ + off : nullptr;
+        const bool two = s->traversal == CR_TRAVERSAL_TWO_LEVEL && s->groupPairs;
+        SceneView v = s->view();
+        if (two) {
+            v.pairs = s->groupPairs;
+            v.rootRef = s->groupRootRef;
+        }
+        if (s->sphHasRoot && two)
+            kTraceDyn<kAnyHit, true, true><<<traceDynBlocks<kAnyHit, true, true>(m), kTraceThreads, 0, st>>>(
+                v, rays + off, m, h, o, counter);
+        else if (s->sphHasRoot)
+            kTraceDyn<kAnyHit, true, false><<<traceDynBlocks<kAnyHit, true, false>(m), kTraceThreads, 0, st>>>(
+                v, rays + off, m, h, o, counter);
+        else if (two)
+            kTraceDyn<kAnyHit, false, true><<<traceDynBlocks<kAnyHit, false, true>(m), kTraceThreads, 0, st>>>(
+                v, rays + off, m, h, o, counter);
         else
-            kTraceDyn<kAnyHit, false><<<traceDynBlocks<kAnyHit, false>(m), kTraceThreads, 0, st>>>(
-                v, rays + off, m, hits ? hits + off : nullptr, occ ? occ + off : nullptr, counter);
+            kTraceDyn<kAnyHit, false, false><<<traceDynBlocks<kAnyHit, false, false>(m), kTraceThreads, 0, st>>>(
+                v, rays + off, m, h, o, counter);
         CR_LAUNCH_CHECK();
         if (counter) CR_CUDA(cudaFreeAsync(counter, st));
     }

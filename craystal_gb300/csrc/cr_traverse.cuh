@@ -184,9 +184,6 @@ __device__ __forceinline__ Float8 ldg32(const void* p) {
     return r;
 }
 
-// Starts moving the line holding p towards L2 (no register result).
-__device__ __forceinline__ void prefetchL2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
-
 // The slot range [first, first + count) of a leaf ref: from the ref itself
 // (kInlineLeafBit) or from the leaf table.
 __device__ __forceinline__ void openLeaf(const uint2* leaves, uint32_t ref, uint32_t& ts, uint32_t& te) {
@@ -208,12 +205,6 @@ __device__ __forceinline__ void openLeaf(const uint2* leaves, uint32_t ref, uint
 template <bool kAnyHit>
 struct TriLeaf {
     const TriBlock* tris;
-    // the 128-byte lines of slots [ts, te) towards L2
-    __device__ __forceinline__ void prefetch(uint32_t ts, uint32_t te) const {
-        const uintptr_t a = reinterpret_cast<uintptr_t>(tris + ts) & ~uintptr_t(127);
-        const uintptr_t e = reinterpret_cast<uintptr_t>(tris + te);
-        for (uintptr_t x = a; x < e; x += 128) prefetchL2(reinterpret_cast<const void*>(x));
-    }
     __device__ __forceinline__ bool operator()(const TRay& r, THit& h, bool& isHit, uint32_t slot) const {
         float3 v0, e1, e2;
         uint32_t prim;
@@ -275,7 +266,6 @@ __device__ __forceinline__ float2 sphereUV(float4 s, const TRay& r, float t) {
 template <bool kAnyHit>
 struct SphereLeaf {
     const SphereBlock* blocks;
-    __device__ __forceinline__ void prefetch(uint32_t, uint32_t) const {}
     __device__ __forceinline__ bool operator()(const TRay& r, THit& h, bool& isHit, uint32_t slot) const {
         const float4* p = reinterpret_cast<const float4*>(blocks + slot);
         const float4 g = __ldg(p);
@@ -359,68 +349,39 @@ __device__ __forceinline__ int nodeLevel(const Float8& w0, const Float8& w1, Tra
 
 // One step; false once the traversal is over (an any-hit query that found
 // a hit stops at once).
-template <bool kAnyHit, class Leaf, class Stack>
+//
+// kTwoLevel: the view's pairs are the grouped copy (kGroupTopBit).  At a
+// group top whose near child is interior, the near child's level runs in
+// the same step, on the next pair of the group: two binary levels per step,
+// fetched from adjacent records.  Nothing
+// changes closestT between the two levels, so the reference's pop-time cull
+// of the near child (Core/BVH.cu:34-36) never fires there and the visiting
+// order, the culling and the hits are those of the one-level step.  Measured
+// on GB300 it is slower than one level per step at every tree size tried
+// (the one-level step is the default; cr_scene_set_traversal).
+template <bool kAnyHit, class Leaf, class Stack, bool kTwoLevel = false>
 __device__ __forceinline__ bool travStep(TravState& s, Stack& stack, const BvhView& bv, uint32_t* errFlags,
                                          const Leaf& leaf, const TRay& r, THit& h) {
     bool pop = true;
     const bool culled = __uint_as_float(s.e.y) > h.t;
     if (s.ts < s.te || (s.e.x & kLeafBit) || culled) {
-        if (s.ts >= s.te && (s.e.x & kLeafBit) && !culled) {
-            openLeaf(bv.leaves, s.e.x, s.ts, s.te);
-#ifdef CR_EXP_PF_LEAF
-            leaf.prefetch(s.ts, s.te);
-#endif
-        }
+        if (s.ts >= s.te && (s.e.x & kLeafBit) && !culled) openLeaf(bv.leaves, s.e.x, s.ts, s.te);
         if (s.ts < s.te) {
             if (leaf(r, h, s.isHit, s.ts)) return false;
             pop = ++s.ts >= s.te;
         }
     } else {
         const uint32_t ref = s.e.x;
-        const NodePair* np = bv.pairs + (ref & kPairIndexMask);
-        const Float8 w0 = ldg32(&np->p0), w1 = ldg32(&np->p2);
-#ifdef CR_EXP_WIDE
-        // a group top: both children's pairs follow it; load them with its own
-        const bool top = (ref & kGroupTopBit) != 0u;
-        const NodePair* rp = np + ((ref & kGroupLeftBit) ? 2 : 1);
-        Float8 l0, l1, r0, r1;
-        if (top && (ref & kGroupLeftBit)) {
-            l0 = ldg32(&np[1].p0);
-            l1 = ldg32(&np[1].p2);
-        }
-        if (top && (ref & kGroupRightBit)) {
-            r0 = ldg32(&rp->p0);
-            r1 = ldg32(&rp->p2);
-        }
-#endif
-#ifdef CR_EXP_PF_CHILD
-        if (ref & kGroupTopBit) {
-            if (ref & (kGroupLeftBit | kGroupRightBit)) prefetchL2(np + 1);
-            if ((ref & kGroupLeftBit) && (ref & kGroupRightBit)) prefetchL2(np + 2);
-        }
-#endif
+        const NodePair* np = bv.pairs + (kTwoLevel ? ref & kPairIndexMask : ref);
         const float ct = h.t;
-        int st = nodeLevel(w0, w1, s, stack, errFlags, r, ct);
+        int st = nodeLevel(ldg32(&np->p0), ldg32(&np->p2), s, stack, errFlags, r, ct);
         if (st < 0) return false;
-#if defined(CR_EXP_WIDE) || defined(CR_EXP_WIDE_DEP)
-        // the near child is an interior node of this group: its level in the
-        // same step (nothing changes closestT in between, so the reference's
-        // pop-time cull of the near child never fires)
-#ifdef CR_EXP_WIDE_DEP
-        const bool top = (ref & kGroupTopBit) != 0u;
-#endif
-        if (st > 0 && top && !(s.e.x & kLeafBit)) {
-            const bool nearLeft = (ref & kGroupLeftBit) && s.e.x == (ref & kPairIndexMask) + 1u;
-#ifdef CR_EXP_WIDE
-            st = nearLeft ? nodeLevel(l0, l1, s, stack, errFlags, r, ct) : nodeLevel(r0, r1, s, stack, errFlags, r, ct);
-#else
+        if (kTwoLevel && st > 0 && (ref & kGroupTopBit) && !(s.e.x & kLeafBit)) {
+            // s.e is now the near child, a second-level pair of this group
             const NodePair* cp = bv.pairs + s.e.x;
-            (void)nearLeft;
             st = nodeLevel(ldg32(&cp->p0), ldg32(&cp->p2), s, stack, errFlags, r, ct);
-#endif
             if (st < 0) return false;
         }
-#endif
         pop = st == 0;
     }
     if (pop) {

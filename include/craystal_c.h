@@ -197,6 +197,25 @@ int cr_scene_bvh_export(const cr_scene* scene, cr_bvh_node* nodes,
 int cr_scene_bvh_import(cr_scene* scene, const cr_bvh_node* nodes,
                         uint32_t node_count, const uint32_t* prim_map);
 
+/* How the ray-cast queries (cr_trace_closest, cr_trace_occluded, their
+ * "_device" forms and cr_trace_closest_noalloc) step through the BVH.  No
+ * counterpart in the reference, whose traversal (Core/BVH.cu:13-84) visits
+ * one binary level per loop iteration.  CR_TRAVERSAL_ONE_LEVEL (the
+ * default) tests one node pair per step.  CR_TRAVERSAL_TWO_LEVEL builds a
+ * second copy of the scene's node pairs laid out in two-level groups (each
+ * interior node at even depth followed by its interior children's pairs; 64
+ * bytes per interior node, at most 2^28 interior nodes) and also tests the
+ * near child's pair of a group in the same step, from the adjacent record;
+ * switching back frees the copy.  Both modes visit nodes and leaves in the
+ * reference's order with its culling, so the hits are the same bit for bit;
+ * on GB300 the one-level step is the faster of the two at every tree size
+ * measured.  Returns CR_ERR_INVALID_ARGUMENT for another mode.  The path
+ * tracers always use the one-level step.  Not thread-safe with queries in
+ * flight on the scene from other threads. */
+#define CR_TRAVERSAL_ONE_LEVEL 0u
+#define CR_TRAVERSAL_TWO_LEVEL 1u
+int cr_scene_set_traversal(cr_scene* scene, uint32_t mode);
+
 /* Errors that kernels detect (a traversal stack that would overflow) set
  * bits of the scene's device error word.  cr_trace_closest,
  * cr_trace_occluded, cr_trace_closest_noalloc and cr_film_read read it when

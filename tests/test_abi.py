@@ -65,3 +65,4 @@ def test_invalid_arguments_are_rejected():
     assert b"NULL" in lib.cr_last_error()
     assert lib.cr_film_clear(None) == 1
     assert lib.cr_trace_closest(None, None, 0, None) == 1
+    assert lib.cr_scene_set_traversal(None, 0) == 1

@@ -228,6 +228,68 @@ def test_full_size_ray_cast(gpu_lib):
     assert_same_hits(gh, oh, ties)
 
 
+def _set_two_level(g):
+    g.set_traversal("two_level")
+    return g
+
+
+@pytest.mark.parametrize("case", ["random", "large_leaves", "cornell", "spheres"])
+def test_two_level_traversal_same_hits(gpu_lib, case):
+    """The two-level step (the near child's pair of a group tested in the
+    same step) visits the reference's nodes in the reference's order: its
+    closest hits equal the one-level step's bit for bit and the oracle's,
+    and its occlusion answers are the oracle's, on a random soup, on leaves
+    too large for the child ref, on the Cornell box with flat boxes and
+    axis-parallel rays, and with analytic spheres in their own tree."""
+    rng = np.random.default_rng(7)
+    if case == "random":
+        data = scenes.random_triangle_scene(100000, seed=50)
+        rays = scenes.random_rays(400000, seed=51)
+    elif case == "large_leaves":
+        from craystal_gb300.api import MaterialData, MeshData, SceneData
+        pos = np.concatenate([_star_cluster(150, (0.5, 0.5, 0.5), rng),
+                              scenes.random_triangles(3000, seed=52)[0]]).astype(np.float32)
+        data = SceneData(meshes=[MeshData(position=pos, index=np.arange(len(pos), dtype=np.uint32))],
+                         materials=[MaterialData()])
+        rays = scenes.random_rays(200000, seed=53)
+    elif case == "cornell":
+        data = scenes.cornell_box()[0]
+        rays = scenes.random_rays(200000, seed=54)
+        rays["o"] *= np.float32(0.45)
+        d = rays["d"].copy()
+        d[rng.random((len(d), 3)) < 0.3] = 0.0
+        d[(d == 0).all(1), 1] = -1.0
+        rays["d"] = d
+    else:
+        from craystal_gb300.api import SphereData
+        data = scenes.random_triangle_scene(20000, seed=55)
+        c, r = rng.random((300, 3)), rng.uniform(0.005, 0.03, 300)
+        data.spheres = [SphereData(tuple(ci), float(ri), 0) for ci, ri in zip(c, r)]
+        rays = scenes.random_rays(200000, seed=56)
+    g, o = both(data)
+    one = g.trace_closest(rays)
+    _set_two_level(g)
+    two = g.trace_closest(rays)
+    assert np.array_equal(one.view(np.uint32), two.view(np.uint32))
+    oh, ties = o.trace_closest(rays)
+    if case == "spheres":  # sphere (u, v) come from acosf / atan2f: prim and t only
+        assert ((two["prim"] == oh["prim"]) | ties).all()
+        assert np.array_equal(two["t"].view(np.uint32), oh["t"].view(np.uint32))
+        assert (two["prim"] >= 0x80000000).sum() > 1000
+    else:
+        assert_same_hits(two, oh, ties, 1e-2)
+    if case == "random":  # an imported tree gets its grouped copy too
+        g.bvh_import(*o.bvh_export())
+        assert np.array_equal(g.trace_closest(rays).view(np.uint32), one.view(np.uint32))
+    rays["tmax"] = np.float32(1.0)
+    occ = o.trace_occluded(rays)
+    assert np.array_equal(g.trace_occluded(rays), occ)
+    g.set_traversal("one_level")  # frees the grouped copy
+    assert np.array_equal(g.trace_occluded(rays), occ)
+    with pytest.raises(Exception):
+        g.set_traversal("four_level")
+
+
 @pytest.mark.parametrize("n", [1, 31, 33, 1000, 123457])
 def test_dynamic_fetch_sizes(gpu_lib, n):
     """The persistent ray cast hands rays to lanes as they free up; every
