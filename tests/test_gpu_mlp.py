@@ -51,10 +51,13 @@ def test_inference_matches_fp64(net):
     np.testing.assert_allclose(out, y, rtol=1e-3, atol=1e-3 * np.abs(y).max())
 
 
-@pytest.mark.parametrize("n", [1, 127, 128, 129, 383, 385, 70001])
+@pytest.mark.parametrize("n", [1, 127, 128, 129, 383, 385, 70001, 233549])
 def test_inference_ragged_batches(net, n):
     """Tensor-core inference over partial tiles (128 queries per tile, three
-    tiles per CTA in flight) and over grids of one CTA up to one per SM."""
+    tiles per CTA in flight), over grids of one CTA up to one per SM, and
+    with several tiles per warpgroup (233,549 queries: four or more each, the
+    inputs of every whole tile staged by a bulk copy a tile ahead through two
+    alternating buffers)."""
     from craystal_gb300._lib import check, load, ptr
     x, _ = _inputs(n, 10 + n)
     out = np.full((n, 3), np.nan, np.float32)
@@ -127,6 +130,24 @@ def test_adam_step_matches_fp64(net):
     m = np.abs(g) > 1e-6
     assert m.mean() > 0.5
     np.testing.assert_allclose(p1[m], expect[m], rtol=1e-5, atol=1e-6)
+
+
+def test_inference_unaligned_device_inputs(net):
+    """Device inputs that do not start on a 16-byte boundary cannot be staged
+    by bulk copies; they are read directly and give the same outputs."""
+    import torch
+    from craystal_gb300._lib import check, load, ptr
+    x, _ = _inputs(50001, 12)
+    ref_out = np.zeros((len(x), 3), np.float32)
+    check(load().cr_mlp_infer(net, ptr(x), len(x), ptr(ref_out)))
+    buf = torch.zeros(len(x) * 7 + 1, dtype=torch.float32, device="cuda")
+    buf[1:] = torch.from_numpy(x.reshape(-1)).cuda()
+    assert (buf.data_ptr() + 4) % 16 != 0
+    dout = torch.empty((len(x), 3), dtype=torch.float32, device="cuda")
+    s = torch.cuda.current_stream()
+    check(load().cr_mlp_infer_device(net, buf.data_ptr() + 4, len(x), dout.data_ptr(), s.cuda_stream))
+    s.synchronize()
+    assert np.array_equal(dout.cpu().numpy(), ref_out)
 
 
 def test_device_forms_match_host_forms(gpu_lib):
