@@ -647,7 +647,7 @@ def mlp_extra(torch):
             "train_step": {"records": n_tr, "ms": round(ms_tr, 4), "tflops": round(tr_tf, 1),
                            "frac": round(tr_tf / peak, 4)},
             "peak_tflops": peak, "peak_source": f"{src} dense bf16 (burst)",
-            "instruction": {"inference": "tcgen05.mma kind::f16, M128, TMEM accumulators, weights and each tile's inputs (a tile ahead) by cp.async.bulk",
+            "instruction": {"inference": "tcgen05.mma kind::f16, M128, TMEM accumulators, weights by cp.async.bulk",
                             "training": "tcgen05.mma kind::f16, M128: forward, backward data gradients and "
                                         "MN-major weight gradients accumulated in TMEM over each CTA's tiles"}}
 

@@ -110,16 +110,10 @@ constexpr int kTcSmemBar = kTcSmemW + kTcWeightBytes;    // 192,512: mbarriers, 
 // The allocation extends 4 KB past the barriers, so that every operand read
 // stays inside it even under the other assignment of the two descriptor
 // strides.
-// Past that margin, each slot's two input staging buffers: one tile of raw
-// inputs (128 rows of 7 floats) brought in by one bulk copy a tile ahead.
-constexpr int kTcInBytes = kTile * kIn * 4;              // 3,584 per tile
-constexpr int kTcSmemIn = 196608;
-constexpr int kTcSmem = kTcSmemIn + kSlots * 2 * kTcInBytes;  // 218,112
-constexpr int kTcBarIn = 40;                             // input barriers [slot][buffer], after barW, barM, TMEM slot
+constexpr int kTcSmem = 196608;
 constexpr uint32_t kTcCols = 256;                        // 64 per slot, a power of two
 constexpr uint32_t kTcSpin = 1u << 20;                   // bounded waits (try_wait rounds)
-static_assert(kTcSmemBar + kTcBarIn + 16 * kSlots <= kTcSmemIn, "tensor-core inference shared memory");
-static_assert(kTcInBytes % 16 == 0, "bulk copies move multiples of 16 bytes");
+static_assert(kTcSmemBar + 8 + 8 * kSlots + 4 <= kTcSmem, "tensor-core inference shared memory");
 
 __device__ __forceinline__ uint32_t smemAddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -197,14 +191,14 @@ __device__ __forceinline__ bool wgAnd(int g, bool v) {
     return r != 0;
 }
 
-// Encodes one row of inputs (input d from input(d)) into row lt of a
-// layer-0 operand at sA: chunk 3d + q holds f = 4q .. 4q+3 of input d;
-// chunk 21 (features 168..175) is zero.
-template <class Input>
-__device__ __forceinline__ void encodeRowTc(const Input& input, uint32_t sA, int lt) {
+// Encodes row `row` of the inputs (zeros past n) into row lt of a layer-0
+// operand at sA: chunk 3d + q holds f = 4q .. 4q+3 of input d; chunk 21
+// (features 168..175) is zero.
+__device__ __forceinline__ void encodeRowTc(const float* __restrict__ in, uint64_t n, uint64_t row, uint32_t sA,
+                                            int lt) {
 #pragma unroll 1
     for (int d = 0; d < kIn; d++) {
-        const float xd = input(d);
+        const float xd = row < n ? in[row * kIn + d] : 0.0f;
 #pragma unroll
         for (int q = 0; q < kFreq / 4; q++) {
             float sn, cs;
@@ -222,13 +216,8 @@ __device__ __forceinline__ void encodeRowTc(const Input& input, uint32_t sA, int
 }
 
 // Persistent: CTA b's warpgroup g takes tiles b * kSlots + g, stepping by
-// gridDim.x * kSlots.  When the inputs are 16-byte aligned, the inputs of
-// every whole tile arrive in the warpgroup's shared-memory staging buffer by
-// one bulk copy, issued while the tile before it is in flight (two buffers,
-// one mbarrier each); a ragged last tile, or unaligned inputs, are read from
-// global memory directly.  A wait that runs out (it should never) sets bit 0
-// of *err, ends the warpgroup's loop, waits (bounded) for its own copy still
-// in flight and still frees the TMEM.
+// gridDim.x * kSlots.  A wait that runs out (it should never) sets bit 0 of
+// *err, ends the warpgroup's loop and still frees the TMEM.
 __global__ void __launch_bounds__(kTile * kSlots, 1) kInferTc(const uint8_t* __restrict__ wTc,
                                                               const float* __restrict__ in, uint64_t n,
                                                               float* __restrict__ out, int clampNonNeg,
@@ -237,11 +226,9 @@ __global__ void __launch_bounds__(kTile * kSlots, 1) kInferTc(const uint8_t* __r
     const int tid = threadIdx.x, g = tid / kTile, lt = tid % kTile, warp = tid >> 5, quarter = warp & 3;
     const uint32_t sA = smemAddr(sm + g * kTcABytes), sW = smemAddr(sm + kTcSmemW);
     const uint32_t barW = smemAddr(sm + kTcSmemBar), barM = barW + 8 + 8 * g, slot = barW + 8 + 8 * kSlots;
-    const uint32_t barIn = barW + kTcBarIn + 16 * g, sIn = smemAddr(sm + kTcSmemIn + g * 2 * kTcInBytes);
     if (tid == 0) {
         mbarInit(barW, 1);
         for (int i = 0; i < kSlots; i++) mbarInit(barW + 8 + 8 * i, 1);
-        for (int i = 0; i < 2 * kSlots; i++) mbarInit(barW + kTcBarIn + 8 * i, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
@@ -268,51 +255,10 @@ __global__ void __launch_bounds__(kTile * kSlots, 1) kInferTc(const uint8_t* __r
     }
     bool ok = wgAnd(g, mbarWait(barW, 0));
     uint32_t phase = 0;
-    const uint64_t tiles = (n + kTile - 1) / kTile, stride = (uint64_t)gridDim.x * kSlots;
-    const bool staged = (reinterpret_cast<uintptr_t>(in) & 15u) == 0;
-    auto whole = [&](uint64_t t) { return staged && t < tiles && (t + 1) * kTile <= n; };
-    // one bulk copy of tile t's inputs into buffer b (thread lt == 0 only); the
-    // generic-proxy reads of that buffer (two tiles ago) are ordered first
-    auto stage = [&](uint64_t t, int b) {
-        proxyFence();
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(barIn + 8 * b),
-                     "r"((uint32_t)kTcInBytes)
-                     : "memory");
-        asm volatile(
-            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                sIn + b * kTcInBytes),
-            "l"(in + t * kTile * kIn), "r"((uint32_t)kTcInBytes), "r"(barIn + 8 * b)
-            : "memory");
-    };
-    const uint64_t first = (uint64_t)blockIdx.x * kSlots + g;
-    int pending = -1;  // the k of the copy issued and not yet waited for (lt == 0's view)
-    if (lt == 0 && ok && whole(first)) {
-        stage(first, 0);
-        pending = 0;
-    }
-    int k = 0;
-    for (uint64_t tile = first; ok && tile < tiles; tile += stride, k++) {
+    const uint64_t tiles = (n + kTile - 1) / kTile;
+    for (uint64_t tile = (uint64_t)blockIdx.x * kSlots + g; ok && tile < tiles; tile += (uint64_t)gridDim.x * kSlots) {
         const uint64_t row = tile * kTile + lt;
-        const int b = k & 1;
-        if (lt == 0 && whole(tile + stride)) {
-            stage(tile + stride, b ^ 1);
-            pending = k + 1;
-        }
-        if (whole(tile)) {
-            ok = wgAnd(g, mbarWait(barIn + 8 * b, (uint32_t)(k >> 1) & 1u));
-            if (!ok) break;
-            if (pending == k) pending = -1;
-            const uint32_t src = sIn + b * kTcInBytes + lt * (kIn * 4);
-            encodeRowTc(
-                [&](int d) {
-                    float v;
-                    asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(src + 4 * d) : "memory");
-                    return v;
-                },
-                sA, lt);
-        } else {
-            encodeRowTc([&](int d) { return row < n ? in[row * kIn + d] : 0.0f; }, sA, lt);
-        }
+        encodeRowTc(in, n, row, sA, lt);
         proxyFence();
         tcBefore();
         wgSync(g);
@@ -366,9 +312,6 @@ __global__ void __launch_bounds__(kTile * kSlots, 1) kInferTc(const uint8_t* __r
             wgSync(g);
         }
     }
-    // a copy issued for a tile this warpgroup no longer reaches (a wait ran
-    // out): let it land before the CTA's shared memory goes away
-    if (lt == 0 && pending >= 0) mbarWait(barIn + 8 * (pending & 1), (uint32_t)(pending >> 1) & 1u);
     tcBefore();
     __syncthreads();
     tcAfter();
@@ -500,7 +443,7 @@ __global__ void __launch_bounds__(kTrThreads, 1) kTrainTc(const uint8_t* __restr
     bool first = true;
     for (uint64_t tile = blockIdx.x; ok && tile < tiles; tile += gridDim.x) {
         const uint64_t row = tile * kTile + tid;
-        encodeRowTc([&](int d) { return row < n ? in[row * kIn + d] : 0.0f; }, base + trA(0), tid);
+        encodeRowTc(in, n, row, base + trA(0), tid);
         proxyFence();
         tcBefore();
         __syncthreads();

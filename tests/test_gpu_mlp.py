@@ -55,9 +55,7 @@ def test_inference_matches_fp64(net):
 def test_inference_ragged_batches(net, n):
     """Tensor-core inference over partial tiles (128 queries per tile, three
     tiles per CTA in flight), over grids of one CTA up to one per SM, and
-    with several tiles per warpgroup (233,549 queries: four or more each, the
-    inputs of every whole tile staged by a bulk copy a tile ahead through two
-    alternating buffers)."""
+    with several tiles per warpgroup (233,549 queries: four or more each)."""
     from craystal_gb300._lib import check, load, ptr
     x, _ = _inputs(n, 10 + n)
     out = np.full((n, 3), np.nan, np.float32)
@@ -133,8 +131,8 @@ def test_adam_step_matches_fp64(net):
 
 
 def test_inference_unaligned_device_inputs(net):
-    """Device inputs that do not start on a 16-byte boundary cannot be staged
-    by bulk copies; they are read directly and give the same outputs."""
+    """Device inputs that start off a 16-byte boundary (each query's 7 floats
+    are read as plain 4-byte loads) give the host form's outputs."""
     import torch
     from craystal_gb300._lib import check, load, ptr
     x, _ = _inputs(50001, 12)
