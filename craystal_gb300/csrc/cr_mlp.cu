@@ -95,7 +95,7 @@ __device__ __forceinline__ void doubleAngle(float& s, float& c) {
 //   B (layer l's weights as N x K, K-major): core (n/8, k/8) at
 //     ((k/8) * (Npad/8) + n/8) * 128; K stride Npad * 16 B, N stride 128 B.
 constexpr int kTile = 128;                     // queries per tile (the MMA's M)
-constexpr int kSlots = 3;                      // warpgroups per CTA, one tile each
+constexpr int kSlots = 7;                      // warpgroups per CTA, one tile each
 __host__ __device__ constexpr int layerNpad(int l) { return l == kLayers - 1 ? 16 : kHid; }
 __host__ __device__ constexpr int tcBytes(int l) { return layerK(l) * layerNpad(l) * 2; }
 __host__ __device__ constexpr int tcOffset(int l) {
@@ -104,16 +104,26 @@ __host__ __device__ constexpr int tcOffset(int l) {
     return o;
 }
 constexpr int kTcWeightBytes = tcOffset(kLayers);        // 57,344
-constexpr int kTcABytes = kTile * kFeat * 2;             // 45,056 per slot
+// A slot's operand buffer holds one part of layer 0's input (chunks 0..11,
+// inputs 0..3, or chunks 12..21, inputs 4..6 and the zero chunk) or a hidden
+// layer's input (8 chunks): 12 chunks of 2048 B.  Layer 0 runs as two MMA
+// groups, K = 96 then K = 80, accumulating into the same TMEM columns, so
+// that six tiles fit in flight per SM instead of three with whole 176-wide
+// layer-0 operands.
+constexpr int kTcPart0Chunks = 12;
+constexpr int kTcPart0Steps = kTcPart0Chunks / 2;        // K16 steps of the first group
+constexpr int kTcABytes = kTcPart0Chunks * 2048;         // 24,576 per slot
 constexpr int kTcSmemW = kSlots * kTcABytes;             // the A buffers come first
-constexpr int kTcSmemBar = kTcSmemW + kTcWeightBytes;    // 192,512: mbarriers, TMEM address
-// The allocation extends 4 KB past the barriers, so that every operand read
-// stays inside it even under the other assignment of the two descriptor
-// strides.
-constexpr int kTcSmem = 196608;
-constexpr uint32_t kTcCols = 256;                        // 64 per slot, a power of two
+constexpr int kTcSmemBar = kTcSmemW + kTcWeightBytes;    // 204,800: mbarriers, TMEM address
+// The allocation extends to the per-block maximum, about 3 KB past the
+// barriers.
+constexpr int kTcSmem = 232448;
+constexpr uint32_t kTcCols = 512;                        // 64 per slot, a power of two
 constexpr uint32_t kTcSpin = 1u << 20;                   // bounded waits (try_wait rounds)
 static_assert(kTcSmemBar + 8 + 8 * kSlots + 4 <= kTcSmem, "tensor-core inference shared memory");
+static_assert(kTcSmem <= 232448, "tensor-core inference shared memory");
+static_assert(64u * kSlots <= kTcCols, "TMEM columns");
+static_assert(kFeat / 8 - kTcPart0Chunks <= kTcPart0Chunks, "layer-0 parts");
 
 __device__ __forceinline__ uint32_t smemAddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -193,11 +203,15 @@ __device__ __forceinline__ bool wgAnd(int g, bool v) {
 
 // Encodes row `row` of the inputs (zeros past n) into row lt of a layer-0
 // operand at sA: chunk 3d + q holds f = 4q .. 4q+3 of input d; chunk 21
-// (features 168..175) is zero.
+// (features 168..175) is zero.  part -1 writes all 22 chunks; part 0 only
+// chunks 0..11 (inputs 0..3) and part 1 chunks 12..21 (inputs 4..6, then the
+// zero chunk), each part to chunk positions 0.. of sA.
 __device__ __forceinline__ void encodeRowTc(const float* __restrict__ in, uint64_t n, uint64_t row, uint32_t sA,
-                                            int lt) {
+                                            int lt, int part = -1) {
+    const int d0 = part == 1 ? kTcPart0Chunks / 3 : 0, d1 = part == 0 ? kTcPart0Chunks / 3 : kIn;
+    const int shift = part == 1 ? kTcPart0Chunks : 0;
 #pragma unroll 1
-    for (int d = 0; d < kIn; d++) {
+    for (int d = d0; d < d1; d++) {
         const float xd = row < n ? in[row * kIn + d] : 0.0f;
 #pragma unroll
         for (int q = 0; q < kFreq / 4; q++) {
@@ -209,15 +223,17 @@ __device__ __forceinline__ void encodeRowTc(const float* __restrict__ in, uint64
                 if (r) doubleAngle(sn, cs);
                 v[r] = pack2(sn, cs);
             }
-            stShared4(sA + (d * 3 + q) * 2048 + lt * 16, v[0], v[1], v[2], v[3]);
+            stShared4(sA + (d * 3 + q - shift) * 2048 + lt * 16, v[0], v[1], v[2], v[3]);
         }
     }
-    stShared4(sA + (kFeat / 8 - 1) * 2048 + lt * 16, 0u, 0u, 0u, 0u);
+    if (part != 0) stShared4(sA + (kFeat / 8 - 1 - shift) * 2048 + lt * 16, 0u, 0u, 0u, 0u);
 }
 
 // Persistent: CTA b's warpgroup g takes tiles b * kSlots + g, stepping by
-// gridDim.x * kSlots.  A wait that runs out (it should never) sets bit 0 of
-// *err, ends the warpgroup's loop and still frees the TMEM.
+// gridDim.x * kSlots.  A tile runs seven MMA groups: layer 0 in two parts
+// (its operand encoded part by part into the slot's buffer), then layers
+// 1..5.  A wait that runs out (it should never) sets bit 0 of *err, ends the
+// warpgroup's loop and still frees the TMEM.
 __global__ void __launch_bounds__(kTile * kSlots, 1) kInferTc(const uint8_t* __restrict__ wTc,
                                                               const float* __restrict__ in, uint64_t n,
                                                               float* __restrict__ out, int clampNonNeg,
@@ -258,26 +274,32 @@ __global__ void __launch_bounds__(kTile * kSlots, 1) kInferTc(const uint8_t* __r
     const uint64_t tiles = (n + kTile - 1) / kTile;
     for (uint64_t tile = (uint64_t)blockIdx.x * kSlots + g; ok && tile < tiles; tile += (uint64_t)gridDim.x * kSlots) {
         const uint64_t row = tile * kTile + lt;
-        encodeRowTc(in, n, row, sA, lt);
+        encodeRowTc(in, n, row, sA, lt, 0);
         proxyFence();
         tcBefore();
         wgSync(g);
 #pragma unroll 1
-        for (int l = 0; l < kLayers; l++) {
+        for (int grp = 0; grp <= kLayers; grp++) {
+            const int l = grp == 0 ? 0 : grp - 1;  // groups 0 and 1 are layer 0's two parts
             if (lt == 0) {
                 tcAfter();
-                const int K = layerK(l), Np = layerNpad(l);
+                const int Np = layerNpad(l);
+                const int k0 = grp == 1 ? kTcPart0Steps : 0, k1 = grp == 0 ? kTcPart0Steps : layerK(l) / 16;
                 const uint32_t idesc = tcInstr(kTile, Np), wl = sW + tcOffset(l);
-                for (int k = 0; k < K / 16; k++)
-                    tcMma(tmem, tcDesc(sA + k * 2 * 2048, 2048, 128), tcDesc(wl + k * 2 * (Np * 16), Np * 16, 128),
-                          idesc, k > 0 ? 1u : 0u);
+                for (int k = k0; k < k1; k++)
+                    tcMma(tmem, tcDesc(sA + (k - k0) * 2 * 2048, 2048, 128),
+                          tcDesc(wl + k * 2 * (Np * 16), Np * 16, 128), idesc, k > 0 ? 1u : 0u);
                 tcCommit(barM);
             }
             ok = wgAnd(g, mbarWait(barM, phase));
             phase ^= 1u;
             tcAfter();
             if (!ok) break;
-            if (l < kLayers - 1) {
+            if (grp == 0) {
+                // the first part is consumed: the second part into the same buffer
+                encodeRowTc(in, n, row, sA, lt, 1);
+                proxyFence();
+            } else if (l < kLayers - 1) {
                 // ReLU, FP16, and into A as the next layer's input (chunks 0..7)
 #pragma unroll
                 for (int h = 0; h < 2; h++) {
