@@ -79,7 +79,7 @@ inline int ensureWavefrontBuffers(void*& slot, uint32_t cap, uint32_t nKeys, WfB
         CR_CUDA(wfAlloc(b->qb, cap));
         CR_CUDA(wfAlloc(b->keys, cap));
         CR_CUDA(wfAlloc(b->sorted, cap));
-        CR_CUDA(wfAlloc(b->counts, 3));  // live paths, next queue, extension fetch counter
+        CR_CUDA(wfAlloc(b->counts, 4));  // live paths, next queue, extension and shade fetch counters
         CR_CUDA(wfAlloc(b->hist, nKeys));
         b->cap = cap;
         b->keyCap = nKeys;
@@ -355,42 +355,68 @@ __global__ void __launch_bounds__(kWfThreads) kWfExtend(const __grid_constant__ 
     addRays(src.raysOf(rayItem), pending);
 }
 
-// Blocks of the persistent extension kernel: as many as stay resident.
-template <class Src>
-unsigned wfExtendBlocks() {
-    static int occ = 0;
-    if (!occ) {
-        int b = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kWfExtend<Src>, kWfThreads, 0);
-        occ = b > 0 ? b : 1;
-    }
+// Resident blocks of kernel K across the current device's SMs (cached per
+// kernel and device ordinal; host threads that both ask store the same
+// value).
+constexpr int kWfOccDevices = 64;
+template <auto K>
+unsigned residentBlocks() {
+    static std::atomic<int> occ[kWfOccDevices];
     int dev = 0, sms = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    return (unsigned)(sms * occ);
+    int o = dev >= 0 && dev < kWfOccDevices ? occ[dev].load(std::memory_order_relaxed) : 0;
+    if (!o) {
+        int b = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, K, kWfThreads, 0);
+        o = b > 0 ? b : 1;
+        if (dev >= 0 && dev < kWfOccDevices) occ[dev].store(o, std::memory_order_relaxed);
+    }
+    return (unsigned)(sms * o);
+}
+
+// Blocks of the persistent extension kernel: as many as stay resident.
+template <class Src>
+unsigned wfExtendBlocks() {
+    return residentBlocks<kWfExtend<Src>>();
+}
+
+// The capped grid of the histogram and scatter: 64 rounds of resident
+// blocks (their per-path work is uniform; waves of up to several million
+// paths keep one block per 128 paths).
+template <auto K>
+unsigned bounceBlocks() {
+    return 64u * residentBlocks<K>();
 }
 
 // Counting sort of the live paths by key.  Keys beyond kSmemKeys bins fall
 // back to global atomics per path.
 constexpr uint32_t kSmemKeys = 2048;
 
+//
+// The per-path kernels of a bounce run capped grids on large waves (the
+// histogram and the scatter stride over the live paths, bounceBlocks; the
+// shade stage's resident blocks take chunks from a counter): the live count
+// is known only on the device, and a grid sized for the whole wave would
+// launch, in the late bounces of a 2^26-path wave, half a million blocks that
+// read the count and exit.
 __global__ void __launch_bounds__(kWfThreads) kWfHistogram(const uint32_t* __restrict__ keys,
                                                            const uint32_t* __restrict__ count, uint32_t nKeys,
                                                            uint32_t* __restrict__ hist) {
     __shared__ uint32_t local[kSmemKeys];
     const uint32_t n = *count;
     if (blockIdx.x * blockDim.x >= n) return;
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t stride = gridDim.x * blockDim.x;
     const bool smem = nKeys <= kSmemKeys;
     if (smem) {
         for (uint32_t k = threadIdx.x; k < nKeys; k += blockDim.x) local[k] = 0;
         __syncthreads();
-        if (i < n) atomicAdd(&local[keys[i]], 1u);
+        for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) atomicAdd(&local[keys[i]], 1u);
         __syncthreads();
         for (uint32_t k = threadIdx.x; k < nKeys; k += blockDim.x)
             if (local[k]) atomicAdd(&hist[k], local[k]);
-    } else if (i < n) {
-        atomicAdd(&hist[keys[i]], 1u);
+    } else {
+        for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) atomicAdd(&hist[keys[i]], 1u);
     }
 }
 
@@ -429,23 +455,27 @@ __global__ void __launch_bounds__(kWfThreads) kWfScatter(const uint32_t* __restr
                                                          uint32_t* __restrict__ sorted) {
     __shared__ uint32_t local[kSmemKeys];
     const uint32_t n = *count;
-    if (blockIdx.x * blockDim.x >= n) return;
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (nKeys <= kSmemKeys) {
-        for (uint32_t k = threadIdx.x; k < nKeys; k += blockDim.x) local[k] = 0;
-        __syncthreads();
-        uint32_t key = 0, rank = 0;
-        if (i < n) {
-            key = keys[i];
-            rank = atomicAdd(&local[key], 1u);
+    const uint32_t stride = gridDim.x * blockDim.x;
+    // block-uniform loop over chunks of blockDim.x paths
+    for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
+        const uint32_t i = i0 + threadIdx.x;
+        if (nKeys <= kSmemKeys) {
+            for (uint32_t k = threadIdx.x; k < nKeys; k += blockDim.x) local[k] = 0;
+            __syncthreads();
+            uint32_t key = 0, rank = 0;
+            if (i < n) {
+                key = keys[i];
+                rank = atomicAdd(&local[key], 1u);
+            }
+            __syncthreads();
+            for (uint32_t k = threadIdx.x; k < nKeys; k += blockDim.x)
+                if (local[k]) local[k] = atomicAdd(&offsets[k], local[k]);
+            __syncthreads();
+            if (i < n) sorted[local[key] + rank] = queue[i];
+            __syncthreads();  // local[] is cleared for the next chunk
+        } else if (i < n) {
+            sorted[atomicAdd(&offsets[keys[i]], 1u)] = queue[i];
         }
-        __syncthreads();
-        for (uint32_t k = threadIdx.x; k < nKeys; k += blockDim.x)
-            if (local[k]) local[k] = atomicAdd(&offsets[k], local[k]);
-        __syncthreads();
-        if (i < n) sorted[local[key] + rank] = queue[i];
-    } else if (i < n) {
-        sorted[atomicAdd(&offsets[keys[i]], 1u)] = queue[i];
     }
 }
 
@@ -457,67 +487,85 @@ __global__ void kWfAdvance(uint32_t* __restrict__ counts, uint32_t* __restrict__
         counts[0] = counts[1];
         counts[1] = 0;
         counts[2] = 0;
+        counts[3] = 0;
     }
 }
 
 // The bounce after the query, for the live paths in material order.  Mode
 // supplies the hooks of shadeBounce (with their per-path state in st.aux)
 // and what happens to a path that ends.
-template <class Src, class Mode>
+template <class Src, class Mode, bool kDynamicFetch = false>
 __global__ void __launch_bounds__(kWfThreads, Src::kShadeMinBlocks) kWfShade(const __grid_constant__ Src src, WfState st,
                                                        const __grid_constant__ Mode mode,
                                                        const uint32_t* __restrict__ order,
-                                                       const uint32_t* __restrict__ count, uint32_t depth,
+                                                       uint32_t* __restrict__ counts, uint32_t depth,
                                                        uint32_t* __restrict__ next,
                                                        uint32_t* __restrict__ nextCount) {
-    const uint32_t n = *count;
-    if (blockIdx.x * blockDim.x >= n) return;
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    bool push = false;
-    uint32_t k = 0, item = 0, rays = 0;
-    if (i < n) {
-        k = order[i];
-        item = st.item[k];
-        const Params& p = src.paramsOf(item);
-        PathCtx c{src.sceneOf(item), 0u, SpectralPath{}};
-        const uint4 meta = st.meta[k];
-        c.spec = makeSpectralPath(p.spectral != 0, meta.x, meta.y, meta.z);
-        Sampler smp = Sampler::resume(meta.w, st.inc[k]);
-        const float4 o = st.ro[k], d = st.rd[k], b = st.beta[k], r = st.rad[k], hv = st.hit[k];
-        float3 ro = mk3(o.x, o.y, o.z), rd = mk3(d.x, d.y, d.z);
-        Spec beta = sp(b.x, b.y, b.z), radiance = sp(r.x, r.y, r.z);
-        THit h;
-        h.prim = __float_as_uint(hv.x);
-        h.t = hv.y;
-        h.u = hv.z;
-        h.v = hv.w;
-        typename Mode::Hooks hk = mode.hooks(st, k, meta);
-        const bool alive = shadeBounce<typename Mode::Hooks, false>(c, p, smp, depth, h, ro, rd, beta, radiance, hk);
-        if (alive && depth + 1 < p.maxDepth) {
-            push = true;
-            st.ro[k] = make_float4(ro.x, ro.y, ro.z, o.w);
-            st.rd[k] = make_float4(rd.x, rd.y, rd.z, d.w);
-            st.beta[k] = make_float4(beta.r, beta.g, beta.b, __uint_as_float(depth + 1));
-            st.rad[k] = make_float4(radiance.r, radiance.g, radiance.b, 0.0f);
-            st.meta[k] = make_uint4(meta.x, meta.y, meta.z, smp.state);
-            mode.keep(st, k, hk);
-        } else {
-            mode.end(src, item, st, k, meta, c, radiance, make_float2(o.w, d.w), hk);
+    // kDynamicFetch = false: block b shades live paths [128 b, 128 b + 128) (a
+    // grid of one block per 128 paths of the wave).  true (waves too large
+    // for that grid to be cheap in their late bounces): the resident blocks
+    // take chunks of 128 live paths from counts[3] (zeroed before the launch)
+    // as they free up, until none are left.
+    __shared__ uint32_t chunk;
+    const uint32_t n = counts[0];
+    for (uint32_t round = 0;; round++) {
+        uint32_t i0 = blockIdx.x * blockDim.x;
+        if (kDynamicFetch) {
+            if (threadIdx.x == 0) chunk = atomicAdd(counts + 3, 1u);
+            __syncthreads();
+            i0 = chunk * blockDim.x;
+            __syncthreads();  // every thread has read chunk before thread 0 overwrites it
+        } else if (round) {
+            break;
         }
-        rays = c.rays;
+        if (i0 >= n) break;
+        const uint32_t i = i0 + threadIdx.x;
+        bool push = false;
+        uint32_t k = 0, item = 0, rays = 0;
+        if (i < n) {
+            k = order[i];
+            item = st.item[k];
+            const Params& p = src.paramsOf(item);
+            PathCtx c{src.sceneOf(item), 0u, SpectralPath{}};
+            const uint4 meta = st.meta[k];
+            c.spec = makeSpectralPath(p.spectral != 0, meta.x, meta.y, meta.z);
+            Sampler smp = Sampler::resume(meta.w, st.inc[k]);
+            const float4 o = st.ro[k], d = st.rd[k], b = st.beta[k], r = st.rad[k], hv = st.hit[k];
+            float3 ro = mk3(o.x, o.y, o.z), rd = mk3(d.x, d.y, d.z);
+            Spec beta = sp(b.x, b.y, b.z), radiance = sp(r.x, r.y, r.z);
+            THit h;
+            h.prim = __float_as_uint(hv.x);
+            h.t = hv.y;
+            h.u = hv.z;
+            h.v = hv.w;
+            typename Mode::Hooks hk = mode.hooks(st, k, meta);
+            const bool alive = shadeBounce<typename Mode::Hooks, false>(c, p, smp, depth, h, ro, rd, beta, radiance, hk);
+            if (alive && depth + 1 < p.maxDepth) {
+                push = true;
+                st.ro[k] = make_float4(ro.x, ro.y, ro.z, o.w);
+                st.rd[k] = make_float4(rd.x, rd.y, rd.z, d.w);
+                st.beta[k] = make_float4(beta.r, beta.g, beta.b, __uint_as_float(depth + 1));
+                st.rad[k] = make_float4(radiance.r, radiance.g, radiance.b, 0.0f);
+                st.meta[k] = make_uint4(meta.x, meta.y, meta.z, smp.state);
+                mode.keep(st, k, hk);
+            } else {
+                mode.end(src, item, st, k, meta, c, radiance, make_float2(o.w, d.w), hk);
+            }
+            rays = c.rays;
+        }
+        // warp-aggregated append to the next queue
+        const unsigned act = __activemask();
+        const unsigned m = __ballot_sync(act, push);
+        if (m) {
+            const int lane = threadIdx.x & 31;
+            const int leader = __ffs(m) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(nextCount, (uint32_t)__popc(m));
+            base = __shfl_sync(act, base, leader);
+            if (push) next[base + __popc(m & ((1u << lane) - 1u))] = k;
+        }
+        addRays(src.raysOf(item), rays);
     }
-    // warp-aggregated append to the next queue
-    const unsigned act = __activemask();
-    const unsigned m = __ballot_sync(act, push);
-    if (m) {
-        const int lane = threadIdx.x & 31;
-        const int leader = __ffs(m) - 1;
-        uint32_t base = 0;
-        if (lane == leader) base = atomicAdd(nextCount, (uint32_t)__popc(m));
-        base = __shfl_sync(act, base, leader);
-        if (push) next[base + __popc(m & ((1u << lane) - 1u))] = k;
-    }
-    addRays(src.raysOf(item), rays);
 }
 
 // Paths whose scene allows no bounce (max depth 0) end with zero radiance.
@@ -603,6 +651,7 @@ __global__ void kWfStart(uint32_t* __restrict__ counts, uint32_t* __restrict__ h
         counts[0] = 0;
         counts[1] = 0;
         counts[2] = 0;
+        counts[3] = 0;
     }
 }
 
@@ -634,19 +683,32 @@ int runWave(const Src& src, const Mode& mode, WfBuffers* b, uint64_t base, uint3
     CR_LAUNCH_CHECK();
     uint32_t* live = b->qa;
     uint32_t* nextQ = b->qb;
+    // measured on GB300: one block per 128 paths is faster up to waves of a
+    // few million paths (1M: 2.94 against 2.89 ms per Cornell render; 4M box
+    // clutter: 32.1 against 30.9 ms); beyond, half a million mostly empty
+    // blocks per late bounce cost more (1080p x 64 spp in 2^26-path waves:
+    // 0.140 against 0.161 s)
+    const unsigned shadeResident = residentBlocks<kWfShade<Src, Mode, true>>();
+    const bool shadeDynamic = blocks(n) > 64u * shadeResident;
     const uint32_t bounces = std::min(maxDepth, finishFrom);
     for (uint32_t depth = 0; depth < bounces; depth++) {
         kWfExtend<Src><<<std::min(blocks(n), wfExtendBlocks<Src>()), kWfThreads, 0, stream>>>(src, st, live,
                                                                                               b->counts, b->keys);
         CR_LAUNCH_CHECK();
-        kWfHistogram<<<blocks(n), kWfThreads, 0, stream>>>(b->keys, b->counts, nKeys, b->hist);
+        kWfHistogram<<<std::min(blocks(n), bounceBlocks<kWfHistogram>()), kWfThreads, 0, stream>>>(b->keys, b->counts,
+                                                                                                 nKeys, b->hist);
         CR_LAUNCH_CHECK();
         kWfScan<<<1, 1024, 0, stream>>>(b->hist, nKeys);
         CR_LAUNCH_CHECK();
-        kWfScatter<<<blocks(n), kWfThreads, 0, stream>>>(b->keys, live, b->counts, nKeys, b->hist, b->sorted);
+        kWfScatter<<<std::min(blocks(n), bounceBlocks<kWfScatter>()), kWfThreads, 0, stream>>>(b->keys, live, b->counts,
+                                                                                             nKeys, b->hist, b->sorted);
         CR_LAUNCH_CHECK();
-        kWfShade<Src, Mode><<<blocks(n), kWfThreads, 0, stream>>>(src, st, mode, b->sorted, b->counts, depth, nextQ,
-                                                                   b->counts + 1);
+        if (shadeDynamic)
+            kWfShade<Src, Mode, true><<<shadeResident, kWfThreads, 0, stream>>>(src, st, mode, b->sorted, b->counts,
+                                                                                 depth, nextQ, b->counts + 1);
+        else
+            kWfShade<Src, Mode, false><<<blocks(n), kWfThreads, 0, stream>>>(src, st, mode, b->sorted, b->counts, depth,
+                                                                              nextQ, b->counts + 1);
         CR_LAUNCH_CHECK();
         kWfAdvance<<<1, 256, 0, stream>>>(b->counts, b->hist, nKeys);
         CR_LAUNCH_CHECK();
