@@ -3,7 +3,7 @@ material, shade per bounce) traces the same paths as the megakernel
 (CR_RENDER_MEGAKERNEL) with the same arithmetic and sampler sequence: films
 equal up to the order of the float atomics, ray counts exactly equal.
 Covered: MIS on and off, spectral mode, spheres + textures + an
-environment, several waves (more paths than one wave holds), max depth 0,
+environment, a wave large enough for the large-wave grids, max depth 0,
 the automatic choice, and a wavefront render captured in a CUDA graph."""
 import numpy as np
 import pytest
@@ -55,7 +55,9 @@ def test_wavefront_several_waves_and_depth_zero(gpu_lib):
     data, cam = scenes.cornell_box(seed=7, width=2048, height=2048)
     sc = Scene(data)
     sc.setCamera(cam)
-    compare(sc, spp=9)  # 37.7 M paths: two waves of at most 2^25
+    # 37.7 M paths in one wave: its bounces run the large-wave grids (the shade
+    # stage's blocks take chunks from a counter, the sort kernels stride)
+    compare(sc, spp=9)
     rgb, w, rays = compare(sc, depth=0, spp=2)
     assert rays == 0 and w.sum() > 0 and not rgb.any()
 
@@ -91,3 +93,20 @@ def test_auto_schedule_and_graph_capture(gpu_lib):
     np.testing.assert_allclose(rgb, ref[0], rtol=2e-4, atol=2e-4)
     with pytest.raises(Exception):
         check(lib.cr_render(sc.handle, ctypes.byref(CrIntegratorConfig(8, 0.05, 1, 6)), 1, 0, None))
+
+
+def test_wavefront_two_waves(gpu_lib):
+    """More paths than one wave holds (2048^2 x 17 spp = 71.3M > 2^26): the
+    render runs as two waves, and its film equals the sum of two renders of
+    9 and 8 spp (one wave each) over the same sample indices."""
+    data, cam = scenes.cornell_box(seed=8, width=2048, height=2048)
+    sc = Scene(data)
+    sc.setCamera(cam)
+    cfg = PathTraceIntegrator.Configs(maxDepth=6, rrThreshold=0.05, useMIS=True)
+    integ = PathTraceIntegrator(cfg, compat=False, wavefront=True)
+    whole = film_of(sc, integ, 17, first=11)
+    a = film_of(sc, integ, 9, first=11)
+    b = film_of(sc, integ, 8, first=20)
+    np.testing.assert_allclose(whole[1], a[1] + b[1], rtol=1e-5, atol=1e-5)
+    np.testing.assert_allclose(whole[0], a[0] + b[0], rtol=2e-4, atol=2e-4)
+    assert whole[2] == a[2] + b[2]
