@@ -50,6 +50,13 @@ def test_sphere_queries_match_oracle(gpu_lib):
     r2 = rays.copy()
     r2["tmax"] = np.random.default_rng(11).uniform(0.01, 1.5, len(r2)).astype(np.float32)
     np.testing.assert_array_equal(sc.trace_occluded(r2), osc.trace_occluded(r2))
+    # the persistent kernel's per-block ray ranges (the form of the entry point
+    # that allocates nothing) give the same hits on a sphere scene
+    from craystal_gb300 import _lib
+    few = rays[: _lib.CR_NOALLOC_MAX_RAYS]
+    na = np.zeros(len(few), gh.dtype)
+    assert _lib.load().cr_trace_closest_noalloc(sc.handle, _lib.ptr(few), len(few), _lib.ptr(na), None) == 0
+    assert np.array_equal(na.view(np.uint32), gh[: len(few)].view(np.uint32))
 
 
 def cornell_with_spheres(res=48):
