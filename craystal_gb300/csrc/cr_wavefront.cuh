@@ -381,12 +381,14 @@ unsigned wfExtendBlocks() {
     return residentBlocks<kWfExtend<Src>>();
 }
 
-// The capped grid of the histogram and scatter: 64 rounds of resident
-// blocks (their per-path work is uniform; waves of up to several million
-// paths keep one block per 128 paths).
+// The capped grid of the histogram and scatter: four rounds of resident
+// blocks striding over the live paths (their per-path work is uniform, so a
+// fixed assignment balances; waves of up to about 1.2M paths keep one block
+// per 128 paths).  With 64 rounds, the late bounces of a 2^26-path wave still
+// spent 80 us per launch on empty blocks.
 template <auto K>
 unsigned bounceBlocks() {
-    return 64u * residentBlocks<K>();
+    return 4u * residentBlocks<K>();
 }
 
 // Counting sort of the live paths by key.  Keys beyond kSmemKeys bins fall
