@@ -626,12 +626,19 @@ __global__ void __launch_bounds__(kWfThreads) kWfEndUntraced(const __grid_consta
 // are left: a wavefront bounce per remaining depth would cost six launches
 // for a few thousand paths each.  The same operations in the same order as
 // the bounce-by-bounce form, so the results are those of kWfShade.
+//
+// fewMax > 0: only when at most fewMax paths are live (the tail of a wave,
+// where each further bounce would cost its launches and the latency of its
+// slowest query for a handful of paths); kWfDrainIfFew then empties the
+// queue, so that the remaining launches of the wave find no live path.
 template <class Src, class Mode>
 __global__ void __launch_bounds__(kWfThreads) kWfFinish(const __grid_constant__ Src src, WfState st,
                                                         const __grid_constant__ Mode mode,
                                                         const uint32_t* __restrict__ queue,
-                                                        const uint32_t* __restrict__ count, uint32_t depth0) {
+                                                        const uint32_t* __restrict__ count, uint32_t depth0,
+                                                        uint32_t fewMax = 0) {
     const uint32_t n = *count;
+    if (fewMax && n > fewMax) return;
     if (blockIdx.x * blockDim.x >= n) return;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t item = 0, rays = 0;
@@ -659,6 +666,10 @@ __global__ void __launch_bounds__(kWfThreads) kWfFinish(const __grid_constant__ 
 }
 
 __global__ void kWfNextWave(uint64_t* __restrict__ waveBase, uint32_t cap) { *waveBase += cap; }
+
+__global__ void kWfDrainIfFew(uint32_t* __restrict__ counts, uint32_t fewMax) {
+    if (counts[0] <= fewMax) counts[0] = 0;
+}
 
 __global__ void kWfStart(uint32_t* __restrict__ counts, uint32_t* __restrict__ hist, uint32_t nKeys) {
     for (uint32_t k = threadIdx.x; k < nKeys; k += blockDim.x) hist[k] = 0;
@@ -688,11 +699,13 @@ inline bool allTraced(const ManyScenes&) { return false; }
 // that the same launch sequence (a captured graph) replays wave after wave.
 //
 // finishFrom < maxDepth: the bounces from finishFrom on run as one kWfFinish
-// launch over the paths still live then.
+// launch over the paths still live then.  fewMax > 0: before each bounce
+// after the first, the live paths finish in one kWfFinish launch once at most
+// fewMax of them are left.
 template <class Src, class Mode>
 int runWave(const Src& src, const Mode& mode, WfBuffers* b, uint64_t base, uint32_t n, uint32_t maxDepth,
             uint32_t nKeys, cudaStream_t stream, uint64_t* waveBase = nullptr, uint64_t total = 0,
-            uint32_t finishFrom = 0xffffffffu) {
+            uint32_t finishFrom = 0xffffffffu, uint32_t fewMax = 0) {
     const WfState st{b->ro, b->rd, b->beta, b->rad, b->meta, b->inc, b->hit, b->aux, b->item};
     kWfInit<Src><<<blocks(n), kWfThreads, 0, stream>>>(src, st, base, n, waveBase, total);
     CR_LAUNCH_CHECK();
@@ -713,6 +726,13 @@ int runWave(const Src& src, const Mode& mode, WfBuffers* b, uint64_t base, uint3
     const bool shadeDynamic = blocks(n) > 64u * shadeResident;
     const uint32_t bounces = std::min(maxDepth, finishFrom);
     for (uint32_t depth = 0; depth < bounces; depth++) {
+        if (fewMax && depth > 0) {
+            kWfFinish<Src, Mode><<<blocks(std::min(n, fewMax)), kWfThreads, 0, stream>>>(src, st, mode, live, b->counts,
+                                                                                         depth, fewMax);
+            CR_LAUNCH_CHECK();
+            kWfDrainIfFew<<<1, 1, 0, stream>>>(b->counts, fewMax);
+            CR_LAUNCH_CHECK();
+        }
         kWfExtend<Src><<<std::min(blocks(n), wfExtendBlocks<Src>()), kWfThreads, 0, stream>>>(src, st, live,
                                                                                               b->counts, b->keys);
         CR_LAUNCH_CHECK();
