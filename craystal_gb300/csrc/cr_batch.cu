@@ -204,7 +204,10 @@ int buildWavefront(cr_batch* b, cudaStream_t st) {
     b->wfWaves = (uint32_t)((total + cap - 1) / cap);
     const ManyScenes src{b->dWf, (uint32_t)b->scenes.size()};
     CR_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    rc = runWave(src, PlainMode{}, wb, 0, cap, maxDepth, keys, st, b->dWaveBase, total);
+    // the shared waves finish their tails in one launch as single-scene
+    // waves of at least 2M paths do (renderWavefront)
+    rc = runWave(src, PlainMode{}, wb, 0, cap, maxDepth, keys, st, b->dWaveBase, total, 0xffffffffu,
+                 cap >= (1u << 21) ? 65536u : 0u);
     cudaError_t e = cudaStreamEndCapture(st, &b->graph);
     if (rc) return rc;
     if (e != cudaSuccess) return fail(CR_ERR_CUDA, "cudaStreamEndCapture: %s", cudaGetErrorString(e));
