@@ -44,6 +44,32 @@ def test_batch_equals_per_scene_renders(gpu_lib, tile, run, wave):
         assert sc.render_ray_count() == r
 
 
+def test_batch_large_shared_wave(gpu_lib):
+    """Three 512x512 scenes at 4 spp share one wave of 3.1M paths (wave_log2
+    22): a wave that large finishes its tail in one launch once few paths
+    are live; each film still equals the scene's own render (1M paths, a
+    wave that keeps its bounce-by-bounce tail), and so do the ray counts."""
+    params, scs, integs = [], [], []
+    for i, depth in enumerate((8, 12, 16)):
+        data, cam = scenes.box_clutter(40 + i, 20000, 512, 512)
+        sc = Scene(data)
+        sc.setCamera(cam)
+        scs.append(sc)
+        integs.append(PathTraceIntegrator(PathTraceIntegrator.Configs(maxDepth=depth, rrThreshold=0.05), compat=False))
+    b = BatchRenderer(scs, integs, [4] * 3, first_sample=[5] * 3)
+    b.set_tuning(16, 4, wave_log2=22)
+    b.render()
+    batch = [sc.film_read() for sc in scs]
+    rays = [sc.render_ray_count() for sc in scs]
+    for sc, integ, (rgb, w), r in zip(scs, integs, batch, rays):
+        sc.film_clear()
+        integ.dispatch(sc, 4, first_sample=5, readback=False)
+        rgb2, w2 = sc.film_read()
+        np.testing.assert_allclose(w, w2, rtol=1e-5, atol=1e-6)
+        np.testing.assert_allclose(rgb, rgb2, rtol=1e-4, atol=1e-5)
+        assert sc.render_ray_count() == r
+
+
 @pytest.mark.parametrize("wave", [0, 17])
 def test_batch_replays_advance_samples(gpu_lib, wave):
     params, scs, integs = make_batch(3)
