@@ -515,6 +515,30 @@ def c1_parity_extra(torch, chunks=128, chunk_spp=512, crop=(120, 136), crop_spp=
     return out
 
 
+def c3_plain_extra(torch):
+    """The radiance-cache config's scene rendered plain once, 1920x1080 at 64
+    spp (after a 1-spp warm-up): the command its per-bounce launch list is
+    taken from."""
+    from craystal_gb300 import scenes
+    from craystal_gb300.api import PathTraceIntegrator, Scene
+    cfg = PathTraceIntegrator.Configs(maxDepth=16, rrThreshold=0.05, useMIS=True)
+    plain = PathTraceIntegrator(cfg, compat=False)
+    data, cam, env, sph = scenes.cache_scene(seed=0, width=1920, height=1080)
+    sc = Scene(data)
+    sc.setCamera(cam)
+    sc.set_environment(env)
+    sc.set_sphere_lights(sph)
+    plain.dispatch(sc, 1, readback=False)
+    sc.film_clear()
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    plain.dispatch(sc, 64, readback=False)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t
+    return {"config": "8 displaced icospheres (2.6M tris), 1920x1080, 64 spp, depth 16, plain", "s": round(dt, 4),
+            "Mpaths_s": round(1920 * 1080 * 64 / dt / 1e6, 1), "rays": int(sc.render_ray_count())}
+
+
 def c3_extra(torch, res=(1920, 1080), budgets=(16, 64), trials=5):
     """The radiance-cache config: 8 displaced icospheres (2.6M triangles),
     Principled materials, constant environment 0.5 and one sphere light, max
@@ -1273,6 +1297,8 @@ def run_only(args):
         r = mlp_extra(torch)
     elif args.only == "radiance_cache_scene":
         r = c3_extra(torch)
+    elif args.only == "radiance_cache_scene_plain":
+        r = c3_plain_extra(torch)
     elif args.only == "hbm_raycast":
         r = hbm_raycast_extra(torch, n_rays=args.hbm_rays, with_oracle=not args.skip_cpu)
         l2, hbm_read = l2_peak_gbs()
@@ -1296,7 +1322,8 @@ def main():
     ap.add_argument("--traversal", choices=["one_level", "two_level"], default="one_level",
                     help="traversal step of the headline ray cast (profiling the two-level step)")
     ap.add_argument("--only", choices=["path_tracer", "c1_parity", "hbm_raycast", "wavefront", "radiance_cache", "cache_frames", "batched_scenes",
-                                       "large_scene", "radiance_cache_scene", "radiance_cache_network"],
+                                       "large_scene", "radiance_cache_scene", "radiance_cache_scene_plain",
+                                       "radiance_cache_network"],
                     help="run one secondary workload alone and print its figures (profiling)")
     ap.add_argument("--cache-res", type=int, default=512, help="radiance-cache workload resolution")
     ap.add_argument("--batch-scenes", type=int, default=64, help="scenes in the batched workload")
