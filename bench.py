@@ -539,6 +539,30 @@ def c3_plain_extra(torch):
             "Mpaths_s": round(1920 * 1080 * 64 / dt / 1e6, 1), "rays": int(sc.render_ray_count())}
 
 
+def c3_cached_frames_extra(torch, frames=32):
+    """Cached frames of the radiance-cache config alone (1920x1080, depth 16,
+    2^16 training records per frame), after 16 warm-up frames: ms per frame,
+    the command the cached frames' launch list is taken from."""
+    from craystal_gb300 import scenes
+    from craystal_gb300.api import CachedPathTraceIntegrator, PathTraceIntegrator, RadianceCache, Scene
+    cfg = PathTraceIntegrator.Configs(maxDepth=16, rrThreshold=0.05, useMIS=True)
+    data, cam, env, sph = scenes.cache_scene(seed=0, width=1920, height=1080)
+    sc = Scene(data)
+    sc.setCamera(cam)
+    sc.set_environment(env)
+    sc.set_sphere_lights(sph)
+    integ = CachedPathTraceIntegrator(cfg, train_samples=1 << 16, cache=RadianceCache(seed=1))
+    integ.dispatch(sc, 16, first_sample=2_000_000, readback=False)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    integ.dispatch(sc, frames, first_sample=3_000_000, readback=False)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t
+    return {"config": "8 displaced icospheres (2.6M tris), 1920x1080, depth 16, cached frames, 2^16 records",
+            "frames": frames, "ms_per_cached_frame": round(1e3 * dt / frames, 3),
+            "train_every_reached": int(integ.stats.last_train_every)}
+
+
 def c3_extra(torch, res=(1920, 1080), budgets=(16, 64), trials=5):
     """The radiance-cache config: 8 displaced icospheres (2.6M triangles),
     Principled materials, constant environment 0.5 and one sphere light, max
@@ -1299,6 +1323,8 @@ def run_only(args):
         r = c3_extra(torch)
     elif args.only == "radiance_cache_scene_plain":
         r = c3_plain_extra(torch)
+    elif args.only == "radiance_cache_scene_frames":
+        r = c3_cached_frames_extra(torch)
     elif args.only == "hbm_raycast":
         r = hbm_raycast_extra(torch, n_rays=args.hbm_rays, with_oracle=not args.skip_cpu)
         l2, hbm_read = l2_peak_gbs()
@@ -1323,7 +1349,7 @@ def main():
                     help="traversal step of the headline ray cast (profiling the two-level step)")
     ap.add_argument("--only", choices=["path_tracer", "c1_parity", "hbm_raycast", "wavefront", "radiance_cache", "cache_frames", "batched_scenes",
                                        "large_scene", "radiance_cache_scene", "radiance_cache_scene_plain",
-                                       "radiance_cache_network"],
+                                       "radiance_cache_scene_frames", "radiance_cache_network"],
                     help="run one secondary workload alone and print its figures (profiling)")
     ap.add_argument("--cache-res", type=int, default=512, help="radiance-cache workload resolution")
     ap.add_argument("--batch-scenes", type=int, default=64, help="scenes in the batched workload")
