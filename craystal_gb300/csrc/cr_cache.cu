@@ -217,6 +217,7 @@ struct WfCacheHooks {
 
 struct CachedMode {
     using Hooks = WfCacheHooks;
+    static constexpr bool kAllowLean = false;
     CacheParams cp;
     uint32_t width, height;
     uint32_t first;    // sample index of the wave's first frame

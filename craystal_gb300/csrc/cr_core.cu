@@ -150,6 +150,7 @@ int createScene(const float* pos, const float* nrm, const float* uv, uint64_t nv
     for (uint32_t m = 0; m < nMats; m++) {
         if (mats[m].type > CR_MATERIAL_PHONG) return fail(CR_ERR_INVALID_ARGUMENT, "material %u type %u", m, mats[m].type);
         gm[m] = deriveMaterial(mats[m]);
+        if (mats[m].type == CR_MATERIAL_PRINCIPLED) s->hasPrincipled = true;
     }
     std::vector<float> zeros;
     s->nv = nv;
@@ -345,7 +346,11 @@ int cr_scene_set_diffuse_textures(cr_scene* scene, const cr_texture* textures, u
     CR_CUDA(cudaDeviceSynchronize());
     std::vector<MaterialGpu> mats(nMats);
     if (nMats) CR_CUDA(cudaMemcpy(mats.data(), scene->mats, nMats * sizeof(MaterialGpu), cudaMemcpyDeviceToHost));
-    for (uint32_t m = 0; m < nMats; m++) mats[m].tex = matTex[m];
+    bool textured = false;
+    for (uint32_t m = 0; m < nMats; m++) {
+        mats[m].tex = matTex[m];
+        textured |= matTex[m] != CR_NO_TEXTURE;
+    }
     if (scene->texels) cudaFree(scene->texels);
     if (scene->texDescs) cudaFree(scene->texDescs);
     scene->texels = nullptr;
@@ -361,6 +366,7 @@ int cr_scene_set_diffuse_textures(cr_scene* scene, const cr_texture* textures, u
     }
     scene->nTex = nTex;
     if (nMats) CR_CUDA(cudaMemcpy(scene->mats, mats.data(), nMats * sizeof(MaterialGpu), cudaMemcpyHostToDevice));
+    scene->hasTextures = textured && nTex > 0;
     return CR_OK;
 }
 

@@ -234,6 +234,8 @@ struct cr_scene {
     float3 rootMin{0, 0, 0}, rootMax{0, 0, 0};
     cr_bvh_stats stats{};
     uint32_t traversal = CR_TRAVERSAL_ONE_LEVEL;  // of the ray-cast queries
+    bool hasPrincipled = false;                   // a material of type CR_MATERIAL_PRINCIPLED
+    bool hasTextures = false;                     // a material with a diffuse texture
     cr::NodePair* groupPairs = nullptr;           // the grouped copy (two-level step only)
     uint32_t groupRootRef = 0;
     uint32_t* errFlags = nullptr;

@@ -350,37 +350,45 @@ struct Bsdf {
         return wi;
     }
 
-    // dispatch, Material/BSDF.h:30-57 and Material/BSDF.cu:36-103
+    // dispatch, Material/BSDF.h:30-57 and Material/BSDF.cu:36-103.
+    // kPrincipled = false: code for a scene without Principled materials,
+    // whose shading kernels then carry only the Lambertian and Phong lobes.
+    template <bool kPrincipled = true>
     __device__ __forceinline__ Spec evalLocal(float3 wo, float3 wi) const {
         Spec f;
         if (type == CR_MATERIAL_PHONG) f = phongEval(wo, wi);
-        else if (type == CR_MATERIAL_PRINCIPLED) f = princEval(wo, wi);
+        else if (kPrincipled && type == CR_MATERIAL_PRINCIPLED) f = princEval(wo, wi);
         else f = mul(kd, kInvPi);
         return mul(f, fabsf(wi.z));
     }
+    template <bool kPrincipled = true>
     __device__ __forceinline__ float pdfLocal(float3 wo, float3 wi) const {
         if (type == CR_MATERIAL_PHONG) return phongPdf(wo, wi);
-        if (type == CR_MATERIAL_PRINCIPLED) return princPdf(wo, wi);
+        if (kPrincipled && type == CR_MATERIAL_PRINCIPLED) return princPdf(wo, wi);
         return cosinePdf(wi);
     }
+    template <bool kPrincipled = true>
     __device__ __forceinline__ float3 sampleLocal(float3 wo, float2 u, float& pdf) const {
         if (type == CR_MATERIAL_PHONG) return phongSample(wo, u, pdf);
-        if (type == CR_MATERIAL_PRINCIPLED) return princSample(wo, u, pdf);
+        if (kPrincipled && type == CR_MATERIAL_PRINCIPLED) return princSample(wo, u, pdf);
         const float3 wi = cosineSampleHemisphere(u);
         pdf = cosinePdf(wi);
         return wi;
     }
+    template <bool kPrincipled = true>
     __device__ __forceinline__ Spec evaluate(float3 wo, float3 wi) const {
-        return evalLocal(frame.toLocal(wo), frame.toLocal(wi));
+        return evalLocal<kPrincipled>(frame.toLocal(wo), frame.toLocal(wi));
     }
+    template <bool kPrincipled = true>
     __device__ __forceinline__ float evaluatePdf(float3 wo, float3 wi) const {
-        return pdfLocal(frame.toLocal(wo), frame.toLocal(wi));
+        return pdfLocal<kPrincipled>(frame.toLocal(wo), frame.toLocal(wi));
     }
+    template <bool kPrincipled = true>
     __device__ __forceinline__ Spec sampleEvaluate(float2 u, float3 wo, float3& wi, float& pdf) const {
         const float3 woL = frame.toLocal(wo);
         pdf = 0.0f;
-        const float3 wiL = sampleLocal(woL, u, pdf);
-        const Spec f = evalLocal(woL, wiL);
+        const float3 wiL = sampleLocal<kPrincipled>(woL, u, pdf);
+        const Spec f = evalLocal<kPrincipled>(woL, wiL);
         wi = frame.toWorld(wiL);
         return f;
     }

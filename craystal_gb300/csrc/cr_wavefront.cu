@@ -41,9 +41,12 @@ int renderWavefront(cr_scene* s, const cr_integrator_config* cfg, uint32_t spp, 
     if (rc) return rc;
     clearError();
     const OneScene src = oneScene(s, p);
+    // the lean shade stage when the scene needs neither Principled lobes,
+    // diffuse textures nor analytic spheres
+    const bool lean = !s->hasPrincipled && !s->hasTextures && !s->sphHasRoot;
     for (uint64_t base = 0; base < total; base += cap) {
         rc = runWave(src, PlainMode{}, b, base, (uint32_t)std::min<uint64_t>(cap, total - base), p.maxDepth,
-                     s->nMats + 2, stream, nullptr, 0, 0xffffffffu, cap >= kFewMinWave ? kFewPaths : 0u);
+                     s->nMats + 2, stream, nullptr, 0, 0xffffffffu, cap >= kFewMinWave ? kFewPaths : 0u, lean);
         if (rc) return rc;
     }
     return CR_OK;

@@ -142,6 +142,7 @@ __device__ __forceinline__ void addRays(unsigned long long* counter, uint32_t ra
 // One scene: path g is pixel g mod (w h) at sample p.first + g / (w h).
 struct OneScene {
     static constexpr int kShadeMinBlocks = 5;  // 96 registers: spills a little, 2 % faster than 4 blocks of 128
+    static constexpr bool kAllowLean = true;   // its shade stage has a lean form (kFullScene = false)
     SceneView view;
     CameraGpu cam;
     Params p;
@@ -185,6 +186,7 @@ struct __align__(16) WfScene {
 struct ManyScenes {
     // 128 registers: it spills there, but 3 blocks of 168 measured 10 % slower
     static constexpr int kShadeMinBlocks = 4;
+    static constexpr bool kAllowLean = false;
     const WfScene* scenes;
     uint32_t n;
     __device__ __forceinline__ const SceneView& sceneOf(uint32_t i) const { return scenes[i].view; }
@@ -499,7 +501,7 @@ __global__ void kWfAdvance(uint32_t* __restrict__ counts, uint32_t* __restrict__
 // The bounce after the query, for the live paths in material order.  Mode
 // supplies the hooks of shadeBounce (with their per-path state in st.aux)
 // and what happens to a path that ends.
-template <class Src, class Mode, bool kDynamicFetch = false>
+template <class Src, class Mode, bool kDynamicFetch = false, bool kFullScene = true>
 __global__ void __launch_bounds__(kWfThreads, Src::kShadeMinBlocks) kWfShade(const __grid_constant__ Src src, WfState st,
                                                        const __grid_constant__ Mode mode,
                                                        const uint32_t* __restrict__ order,
@@ -544,7 +546,8 @@ __global__ void __launch_bounds__(kWfThreads, Src::kShadeMinBlocks) kWfShade(con
             h.u = hv.z;
             h.v = hv.w;
             typename Mode::Hooks hk = mode.hooks(st, k, meta);
-            const bool alive = shadeBounce<typename Mode::Hooks, false>(c, p, smp, depth, h, ro, rd, beta, radiance, hk);
+            const bool alive =
+                shadeBounce<typename Mode::Hooks, false, kFullScene>(c, p, smp, depth, h, ro, rd, beta, radiance, hk);
             if (alive && depth + 1 < p.maxDepth) {
                 push = true;
                 st.ro[k] = make_float4(ro.x, ro.y, ro.z, o.w);
@@ -705,7 +708,7 @@ inline bool allTraced(const ManyScenes&) { return false; }
 template <class Src, class Mode>
 int runWave(const Src& src, const Mode& mode, WfBuffers* b, uint64_t base, uint32_t n, uint32_t maxDepth,
             uint32_t nKeys, cudaStream_t stream, uint64_t* waveBase = nullptr, uint64_t total = 0,
-            uint32_t finishFrom = 0xffffffffu, uint32_t fewMax = 0) {
+            uint32_t finishFrom = 0xffffffffu, uint32_t fewMax = 0, bool lean = false) {
     const WfState st{b->ro, b->rd, b->beta, b->rad, b->meta, b->inc, b->hit, b->aux, b->item};
     kWfInit<Src><<<blocks(n), kWfThreads, 0, stream>>>(src, st, base, n, waveBase, total);
     CR_LAUNCH_CHECK();
@@ -744,12 +747,27 @@ int runWave(const Src& src, const Mode& mode, WfBuffers* b, uint64_t base, uint3
         kWfScatter<<<std::min(blocks(n), bounceBlocks<kWfScatter>()), kWfThreads, 0, stream>>>(b->keys, live, b->counts,
                                                                                              nKeys, b->hist, b->sorted);
         CR_LAUNCH_CHECK();
-        if (shadeDynamic)
-            kWfShade<Src, Mode, true><<<shadeResident, kWfThreads, 0, stream>>>(src, st, mode, b->sorted, b->counts,
-                                                                                 depth, nextQ, b->counts + 1);
-        else
-            kWfShade<Src, Mode, false><<<blocks(n), kWfThreads, 0, stream>>>(src, st, mode, b->sorted, b->counts, depth,
-                                                                              nextQ, b->counts + 1);
+        bool launched = false;
+        if constexpr (Src::kAllowLean && Mode::kAllowLean) {
+            if (lean) {
+                if (shadeDynamic)
+                    kWfShade<Src, Mode, true, false><<<residentBlocks<kWfShade<Src, Mode, true, false>>(), kWfThreads, 0,
+                                                       stream>>>(src, st, mode, b->sorted, b->counts, depth, nextQ,
+                                                                 b->counts + 1);
+                else
+                    kWfShade<Src, Mode, false, false><<<blocks(n), kWfThreads, 0, stream>>>(
+                        src, st, mode, b->sorted, b->counts, depth, nextQ, b->counts + 1);
+                launched = true;
+            }
+        }
+        if (!launched) {
+            if (shadeDynamic)
+                kWfShade<Src, Mode, true><<<shadeResident, kWfThreads, 0, stream>>>(src, st, mode, b->sorted, b->counts,
+                                                                                     depth, nextQ, b->counts + 1);
+            else
+                kWfShade<Src, Mode, false><<<blocks(n), kWfThreads, 0, stream>>>(src, st, mode, b->sorted, b->counts,
+                                                                                  depth, nextQ, b->counts + 1);
+        }
         CR_LAUNCH_CHECK();
         kWfAdvance<<<1, 256, 0, stream>>>(b->counts, b->hist, nKeys);
         CR_LAUNCH_CHECK();
@@ -770,6 +788,7 @@ int runWave(const Src& src, const Mode& mode, WfBuffers* b, uint64_t base, uint3
 // scene's film (SensorData::addSample, Core/Sensor.cu:19-43).
 struct PlainMode {
     using Hooks = NoHooks;
+    static constexpr bool kAllowLean = true;
     __device__ __forceinline__ Hooks hooks(const WfState&, uint32_t, const uint4&) const { return NoHooks{}; }
     __device__ __forceinline__ void keep(const WfState&, uint32_t, const Hooks&) const {}
     template <class Src>
