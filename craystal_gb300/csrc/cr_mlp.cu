@@ -9,15 +9,15 @@
 //
 // Kernels
 //   kInferTc   fused forward on the 5th-generation tensor cores: each of
-//              three warpgroups of a persistent CTA carries a tile of 128
+//              seven warpgroups of a persistent CTA carries a tile of 128
 //              queries through all six layers.  The weights are brought into
 //              shared memory once per CTA by bulk asynchronous copies; each
 //              layer is tcgen05.mma (M 128, N 64 or 16, K 16 per instruction)
 //              from shared-memory operands into a 64-column TMEM accumulator
 //              per warpgroup, read back with tcgen05.ld, ReLU'd and written as
-//              the next layer's FP16 operand.  Three tiles in flight per SM
-//              overlap one warpgroup's encoding and epilogue with another's
-//              MMAs.
+//              the next layer's FP16 operand.  Seven tiles in flight per SM
+//              overlap some warpgroups' encoding and epilogues with the
+//              others' MMAs.
 //   kTrainTc   one training pass on the 5th-generation tensor cores: a
 //              persistent CTA per SM carries tiles of 128 records through the
 //              forward, the loss gradient, the backward data gradients and
@@ -108,7 +108,7 @@ constexpr int kTcWeightBytes = tcOffset(kLayers);        // 57,344
 // inputs 0..3, or chunks 12..21, inputs 4..6 and the zero chunk) or a hidden
 // layer's input (8 chunks): 12 chunks of 2048 B.  Layer 0 runs as two MMA
 // groups, K = 96 then K = 80, accumulating into the same TMEM columns, so
-// that six tiles fit in flight per SM instead of three with whole 176-wide
+// that seven tiles fit in flight per SM instead of three with whole 176-wide
 // layer-0 operands.
 constexpr int kTcPart0Chunks = 12;
 constexpr int kTcPart0Steps = kTcPart0Chunks / 2;        // K16 steps of the first group
