@@ -530,9 +530,8 @@ int cachedFinishWave(CachedJob& j, cudaStream_t st) {
             if (r1 <= r0) continue;
             j.lastTrain = r1 - r0;
             for (uint32_t q = 0; q < j.steps; q++) {
-                rc = mlpGradDevice(j.mlp, b->tIn + (size_t)r0 * kMlpInputs, b->tTarget + (size_t)r0 * 3, r1 - r0, st);
-                if (rc) return rc;
-                rc = mlpAdamDevice(j.mlp, st);
+                rc = mlpTrainStepDevice(j.mlp, b->tIn + (size_t)r0 * kMlpInputs, b->tTarget + (size_t)r0 * 3,
+                                        r1 - r0, st);
                 if (rc) return rc;
             }
         }

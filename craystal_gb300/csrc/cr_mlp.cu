@@ -22,10 +22,13 @@
 //              persistent CTA per SM carries tiles of 128 records through the
 //              forward, the loss gradient, the backward data gradients and
 //              the weight gradients (the last accumulated in TMEM over all
-//              the CTA's tiles); kReduceGrad sums the CTAs' partials.
-//   kAdam      Adam on FP32 master weights; kPackWeights refreshes the FP16
-//              core-matrix tiles of the weights (W_l for the forward, W_l^T
-//              for the backward data gradients).
+//              the CTA's tiles).
+//   kReduceAdam the rest of a training step in one launch: the CTAs'
+//              partials summed, Adam on the FP32 master weights and the
+//              FP16 core-matrix tiles of the weights refreshed (W_l for the
+//              forward, W_l^T for the backward data gradients).
+//              kReduceGrad sums the partials alone (gradient queries);
+//              kPackWeights refreshes every tile (weights set by the caller).
 
 #include <cstring>
 #include <vector>
@@ -454,9 +457,12 @@ __global__ void __launch_bounds__(kTrThreads, 1) kTrainTc(const uint8_t* __restr
     bool ok = __syncthreads_and(mbarWait(barW, 0));
     uint32_t phase = 0;
     float lossLocal = 0.0f;
-    // waits for the MMAs committed so far; false when the wait runs out
+    // waits for the MMAs committed so far; false when the wait runs out.  Each
+    // thread waits for itself: the barrier at the end of the phase that
+    // follows makes the outcome uniform (one barrier per phase instead of two,
+    // 2 % of a step)
     auto waitMma = [&]() {
-        const bool done = __syncthreads_and(mbarWait(barM, phase));
+        const bool done = mbarWait(barM, phase);
         phase ^= 1u;
         tcAfter();
         return done;
@@ -481,8 +487,7 @@ __global__ void __launch_bounds__(kTrThreads, 1) kTrainTc(const uint8_t* __restr
                           tcDesc(wl + k * 2 * (Np * 16), Np * 16, 128), idesc, k > 0 ? 1u : 0u);
                 tcCommit(barM);
             }
-            ok = waitMma();
-            if (!ok) break;
+            const bool done = waitMma();
             if (l < kLayers - 1) {
                 const uint32_t dst = base + trA(l + 1) + tid * 16;
 #pragma unroll
@@ -523,7 +528,7 @@ __global__ void __launch_bounds__(kTrThreads, 1) kTrainTc(const uint8_t* __restr
             }
             proxyFence();
             tcBefore();
-            __syncthreads();
+            ok = __syncthreads_and(done);
         }
         // backward: weight and data gradients, layers 5..1
 #pragma unroll 1
@@ -542,8 +547,7 @@ __global__ void __launch_bounds__(kTrThreads, 1) kTrainTc(const uint8_t* __restr
                           tcInstr(kTile, kHid), k > 0 ? 1u : 0u);
                 tcCommit(barM);
             }
-            ok = waitMma();
-            if (!ok) break;
+            const bool done = waitMma();
             const uint32_t a = base + trA(l) + tid * 16;
 #pragma unroll
             for (int h = 0; h < 2; h++) {
@@ -565,7 +569,7 @@ __global__ void __launch_bounds__(kTrThreads, 1) kTrainTc(const uint8_t* __restr
             }
             proxyFence();
             tcBefore();
-            __syncthreads();
+            ok = __syncthreads_and(done);
         }
         if (!ok) break;
         // dW_0 += A_0^T dY_0 (dY_0 is over A_1), input features in two groups of 128
@@ -578,24 +582,28 @@ __global__ void __launch_bounds__(kTrThreads, 1) kTrainTc(const uint8_t* __restr
                           tcDesc(base + trA(1) + k * 256, 128, kTrChunk), idw, (first && k == 0) ? 0u : 1u);
             tcCommit(barM);
         }
-        ok = waitMma();
-        tcBefore();
-        __syncthreads();
+        {
+            const bool done = waitMma();
+            tcBefore();
+            ok = __syncthreads_and(done);
+        }
         first = false;
     }
     tcBefore();
     __syncthreads();
     tcAfter();
-    // this CTA's dW partials: lane = input feature, column = output
+    // this CTA's dW partials: lane = input feature k, column = output n,
+    // stored output-major (slot paramOffset(l) + n K_l + k, partialSlotParam)
+    // so that a warp's 32 lanes write 128 contiguous bytes per column
     if (ok) {
         float* p = part + (size_t)blockIdx.x * kParams;
         const int lane = tid & 31;
 #pragma unroll 1
         for (int l = 0; l < kLayers; l++) {
-            const int groups = l == 0 ? 2 : 1, N = layerN(l);
+            const int groups = l == 0 ? 2 : 1, K = layerK(l);
             for (int grp = 0; grp < groups; grp++) {
                 const int k = grp * 128 + warp * 32 + lane;
-                const bool valid = k < layerK(l);
+                const bool valid = k < K;
                 const uint32_t col = tq + trDwCol(l, grp);
                 if (l < kLayers - 1) {
 #pragma unroll
@@ -604,9 +612,9 @@ __global__ void __launch_bounds__(kTrThreads, 1) kTrainTc(const uint8_t* __restr
                         tcLoad32(col + h * 32, v);
                         tcLoadWait();
                         if (valid) {
-                            float* dst = p + paramOffset(l) + k * N + h * 32;
+                            float* dst = p + paramOffset(l) + h * 32 * K + k;
 #pragma unroll
-                            for (int j = 0; j < 32; j++) dst[j] = __uint_as_float(v[j]);
+                            for (int j = 0; j < 32; j++) dst[j * K] = __uint_as_float(v[j]);
                         }
                     }
                 } else {
@@ -614,7 +622,7 @@ __global__ void __launch_bounds__(kTrThreads, 1) kTrainTc(const uint8_t* __restr
                     tcLoad4(col, v);
                     tcLoadWait();
                     if (valid)
-                        for (int j = 0; j < 3; j++) p[paramOffset(l) + k * 3 + j] = __uint_as_float(v[j]);
+                        for (int j = 0; j < 3; j++) p[paramOffset(l) + j * K + k] = __uint_as_float(v[j]);
                 }
             }
         }
@@ -629,42 +637,93 @@ __global__ void __launch_bounds__(kTrThreads, 1) kTrainTc(const uint8_t* __restr
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTrCols) : "memory");
 }
 
-// grad += scale * (sum of the CTAs' partials), one thread per parameter
-__global__ void kReduceGrad(const float* __restrict__ part, int parts, float scale, float* __restrict__ grad) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= kParams) return;
+// The parameter (k-major index paramOffset(l) + k N_l + n) of partial slot
+// paramOffset(l) + n K_l + k.  Every layer's slots start on a multiple of 32,
+// so a warp's 32 slots lie in one layer.
+__device__ __forceinline__ int partialSlotParam(int slot) {
+    int l = 0;
+    while (l < kLayers - 1 && slot >= paramOffset(l + 1)) l++;
+    const int K = layerK(l), local = slot - paramOffset(l);
+    return paramOffset(l) + (local % K) * layerN(l) + local / K;
+}
+static_assert(paramOffset(1) % 32 == 0 && paramOffset(kLayers - 1) % 32 == 0 && kParams % 32 == 0,
+              "whole warps of partial slots per layer");
+
+// Sum over the CTAs' weight-gradient partials for slots 32 b .. 32 b + 31
+// (block b of kRedThreads): warp w adds partials w, w + kRedWarps, ..., the
+// lanes one 128-byte row each, and warp 0 adds the warps' sums in a fixed
+// order (so the result depends only on the partials).  Valid in warp 0.
+constexpr int kRedWarps = 8;
+constexpr int kRedThreads = kRedWarps * 32;
+
+__device__ __forceinline__ float sumPartials(const float* __restrict__ part, int parts, int i) {
+    __shared__ float red[kRedWarps][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     float s = 0.0f;
-    for (int b = 0; b < parts; b++) s += part[(size_t)b * kParams + i];
-    grad[i] += s * scale;
+#pragma unroll 4
+    for (int b = w; b < parts; b += kRedWarps) s += part[(size_t)b * kParams + i];
+    red[w][lane] = s;
+    __syncthreads();
+    float t = 0.0f;
+    if (w == 0)
+        for (int k = 0; k < kRedWarps; k++) t += red[k][lane];
+    return t;
 }
 
-__global__ void kAdam(float* __restrict__ w, float* __restrict__ m, float* __restrict__ v, float* __restrict__ grad,
-                      int count, float lr, float b1, float b2, float eps, float c1, float c2) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= count) return;
-    const float gr = grad[i];
-    const float mi = b1 * m[i] + (1.0f - b1) * gr;
-    const float vi = b2 * v[i] + (1.0f - b2) * gr * gr;
-    m[i] = mi;
-    v[i] = vi;
-    w[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
-    grad[i] = 0.0f;
-}
-
-// Refreshes the FP16 core-matrix tiles of the weights: W_l for inference and
-// the training forward, W_l^T for the training backward (the padding, zeroed
-// once, is never written).
-__global__ void kPackWeights(const float* __restrict__ w, __half* __restrict__ tc, __half* __restrict__ tcT) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= kParams) return;
+// FP16 core-matrix tiles of parameter i: W_l for inference and the training
+// forward, W_l^T for the training backward (the padding, zeroed once, is
+// never written).
+__device__ __forceinline__ void packParam(int i, float wi, __half* __restrict__ tc, __half* __restrict__ tcT) {
     int l = 0;
     while (l < kLayers - 1 && i >= paramOffset(l + 1)) l++;
     const int N = layerN(l);
     const int local = i - paramOffset(l), k = local / N, n = local % N;
-    const __half h = __float2half_rn(w[i]);
+    const __half h = __float2half_rn(wi);
     tc[(tcOffset(l) + ((k >> 3) * (layerNpad(l) >> 3) + (n >> 3)) * 128 + (n & 7) * 16 + (k & 7) * 2) / 2] = h;
     // backward-data operand W_l^T: N = input k, K = output n
     if (l > 0) tcT[(tcBwdOffset(l) + ((n >> 3) * (kHid >> 3) + (k >> 3)) * 128 + (k & 7) * 16 + (n & 7) * 2) / 2] = h;
+}
+
+// grad += scale * (sum of the CTAs' partials)
+__global__ void __launch_bounds__(kRedThreads) kReduceGrad(const float* __restrict__ part, int parts, float scale,
+                                                           float* __restrict__ grad) {
+    const int slot = blockIdx.x * 32 + (threadIdx.x & 31);
+    const float t = sumPartials(part, parts, slot);
+    if (threadIdx.x < 32) grad[partialSlotParam(slot)] += t * scale;
+}
+
+struct AdamArgs {
+    float lr, b1, b2, eps, c1, c2;  // c1, c2: the bias corrections 1 - beta^step
+};
+
+// One training step's tail in one launch: the gradient (grad + scale * the
+// partials' sum), Adam on the FP32 master weights, the gradient cleared for
+// the next step and the weight's FP16 tiles refreshed.
+__global__ void __launch_bounds__(kRedThreads) kReduceAdam(const float* __restrict__ part, int parts, float scale,
+                                                           float* __restrict__ grad, float* __restrict__ w,
+                                                           float* __restrict__ m, float* __restrict__ v,
+                                                           const AdamArgs a, __half* __restrict__ tc,
+                                                           __half* __restrict__ tcT) {
+    const int slot = blockIdx.x * 32 + (threadIdx.x & 31);
+    const float t = sumPartials(part, parts, slot);
+    if (threadIdx.x >= 32) return;
+    const int i = partialSlotParam(slot);
+    const float gr = grad[i] + t * scale;
+    const float mi = a.b1 * m[i] + (1.0f - a.b1) * gr;
+    const float vi = a.b2 * v[i] + (1.0f - a.b2) * gr * gr;
+    m[i] = mi;
+    v[i] = vi;
+    const float wi = w[i] - a.lr * (mi / a.c1) / (sqrtf(vi / a.c2) + a.eps);
+    w[i] = wi;
+    grad[i] = 0.0f;
+    packParam(i, wi, tc, tcT);
+}
+
+// Refreshes the FP16 tiles of every weight (after the weights are set).
+__global__ void kPackWeights(const float* __restrict__ w, __half* __restrict__ tc, __half* __restrict__ tcT) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kParams) return;
+    packParam(i, w[i], tc, tcT);
 }
 
 inline unsigned cdiv(uint64_t a, uint64_t b) { return (unsigned)((a + b - 1) / b); }
@@ -786,29 +845,46 @@ int mlpCheck(MlpState* s) {
     return CR_OK;
 }
 
-// Accumulates dW of the mean relative L2 loss over n samples into s->grad.
-int mlpGradDevice(MlpState* s, const float* in, const float* target, uint64_t n, cudaStream_t st) {
-    if (n == 0) return CR_OK;
+// kTrainTc over n samples: the CTAs' weight-gradient partials of the mean
+// relative L2 loss in s->part (returns the CTA count), the loss sum in s->loss.
+int trainPartials(MlpState* s, const float* in, const float* target, uint64_t n, cudaStream_t st,
+                  unsigned& blocks) {
     CR_CUDA(cudaMemsetAsync(s->loss, 0, sizeof(float), st));
     // one persistent CTA per SM (its shared memory admits one), each with at least one tile
-    const unsigned blocks = std::min<unsigned>(cdiv(n, kTile), (unsigned)s->sms);
+    blocks = std::min<unsigned>(cdiv(n, kTile), (unsigned)s->sms);
     kTrainTc<<<blocks, kTrThreads, kTrSmem, st>>>(reinterpret_cast<const uint8_t*>(s->wTc),
                                                  reinterpret_cast<const uint8_t*>(s->wTcT), in, target, n, s->part,
                                                  s->loss, s->err);
     CR_LAUNCH_CHECK();
-    kReduceGrad<<<cdiv(kParams, 256), 256, 0, st>>>(s->part, (int)blocks, 1.0f / (3.0f * (float)n), s->grad);
+    return CR_OK;
+}
+
+// Accumulates dW of the mean relative L2 loss over n samples into s->grad.
+int mlpGradDevice(MlpState* s, const float* in, const float* target, uint64_t n, cudaStream_t st) {
+    if (n == 0) return CR_OK;
+    unsigned blocks = 0;
+    int rc = trainPartials(s, in, target, n, st, blocks);
+    if (rc) return rc;
+    kReduceGrad<<<kParams / 32, kRedThreads, 0, st>>>(s->part, (int)blocks, 1.0f / (3.0f * (float)n), s->grad);
     CR_LAUNCH_CHECK();
     return CR_OK;
 }
 
-int mlpAdamDevice(MlpState* s, cudaStream_t st) {
+// One Adam step on s->grad + dW of n samples (n may be 0): two launches,
+// kTrainTc and kReduceAdam.  Leaves s->grad zeroed.
+int mlpTrainStepDevice(MlpState* s, const float* in, const float* target, uint64_t n, cudaStream_t st) {
+    unsigned blocks = 0;
+    if (n) {
+        int rc = trainPartials(s, in, target, n, st, blocks);
+        if (rc) return rc;
+    }
     s->step++;
-    const float c1 = 1.0f - std::pow(s->cfg.beta1, (float)s->step);
-    const float c2 = 1.0f - std::pow(s->cfg.beta2, (float)s->step);
-    kAdam<<<cdiv(kParams, 256), 256, 0, st>>>(s->w, s->m, s->v, s->grad, kParams, s->cfg.lr, s->cfg.beta1,
-                                               s->cfg.beta2, s->cfg.eps, c1, c2);
+    const AdamArgs a{s->cfg.lr, s->cfg.beta1, s->cfg.beta2, s->cfg.eps,
+                     1.0f - std::pow(s->cfg.beta1, (float)s->step), 1.0f - std::pow(s->cfg.beta2, (float)s->step)};
+    kReduceAdam<<<kParams / 32, kRedThreads, 0, st>>>(s->part, (int)blocks, n ? 1.0f / (3.0f * (float)n) : 0.0f,
+                                                       s->grad, s->w, s->m, s->v, a, s->wTc, s->wTcT);
     CR_LAUNCH_CHECK();
-    return pack(s, st);
+    return CR_OK;
 }
 
 float* mlpLossPtr(MlpState* s) { return s->loss; }
@@ -882,7 +958,7 @@ static int gradOrTrain(cr_mlp* m, const float* inputs, const float* targets, uin
     CR_CUDA(cudaMemcpy(s->stageIn, inputs, n * kIn * sizeof(float), cudaMemcpyHostToDevice));
     CR_CUDA(cudaMemcpy(s->stageOut, targets, n * 3 * sizeof(float), cudaMemcpyHostToDevice));
     CR_CUDA(cudaMemset(s->grad, 0, kParams * sizeof(float)));
-    rc = mlpGradDevice(s, s->stageIn, s->stageOut, n, 0);
+    rc = step ? mlpTrainStepDevice(s, s->stageIn, s->stageOut, n, 0) : mlpGradDevice(s, s->stageIn, s->stageOut, n, 0);
     if (rc) return rc;
     if (grads) CR_CUDA(cudaMemcpy(grads, s->grad, kParams * sizeof(float), cudaMemcpyDeviceToHost));
     if (loss) {
@@ -890,12 +966,7 @@ static int gradOrTrain(cr_mlp* m, const float* inputs, const float* targets, uin
         CR_CUDA(cudaMemcpy(&l, s->loss, sizeof(float), cudaMemcpyDeviceToHost));
         *loss = l / (3.0f * (float)n);
     }
-    if (step) {
-        rc = mlpAdamDevice(s, 0);
-        if (rc) return rc;
-    } else {
-        CR_CUDA(cudaMemset(s->grad, 0, kParams * sizeof(float)));
-    }
+    if (!step) CR_CUDA(cudaMemset(s->grad, 0, kParams * sizeof(float)));
     CR_CUDA(cudaDeviceSynchronize());
     return mlpCheck(s);
 }
@@ -912,11 +983,8 @@ int cr_mlp_train_step_device(cr_mlp* m, const float* inputs, const float* target
     if (!m || (n && (!inputs || !targets))) return fail(CR_ERR_INVALID_ARGUMENT, "NULL argument");
     if (n == 0) return CR_OK;
     CR_CUDA(cudaSetDevice(m->s->device));
-    // kAdam leaves the gradient zeroed, so every step starts from zero
-    const cudaStream_t st = (cudaStream_t)stream;
-    int rc = mlpGradDevice(m->s, inputs, targets, n, st);
-    if (rc) return rc;
-    return mlpAdamDevice(m->s, st);
+    // each step leaves the gradient zeroed, so every step starts from zero
+    return mlpTrainStepDevice(m->s, inputs, targets, n, (cudaStream_t)stream);
 }
 
 int cr_mlp_gradients(cr_mlp* m, const float* inputs, const float* targets, uint64_t n, float* grads, float* loss) {

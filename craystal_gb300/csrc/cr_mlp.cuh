@@ -16,7 +16,8 @@ void mlpDestroy(MlpState* s);
 int mlpInferDevice(MlpState* s, const float* in, uint64_t n, float* out, bool clampNonNeg, cudaStream_t st);
 // adds dW of the mean relative L2 loss of n samples; loss sum in mlpLossPtr
 int mlpGradDevice(MlpState* s, const float* in, const float* target, uint64_t n, cudaStream_t st);
-int mlpAdamDevice(MlpState* s, cudaStream_t st);
+// one Adam step on the accumulated gradient plus dW of n samples; clears it
+int mlpTrainStepDevice(MlpState* s, const float* in, const float* target, uint64_t n, cudaStream_t st);
 float* mlpLossPtr(MlpState* s);
 // reports a tensor-core wait of the inference that ran out (synchronises)
 int mlpCheck(MlpState* s);

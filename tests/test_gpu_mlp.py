@@ -174,12 +174,10 @@ def test_device_forms_match_host_forms(gpu_lib):
         check(lib.cr_mlp_train_step_device(nets[1], dx.data_ptr(), dt.data_ptr(), len(x), s.cuda_stream))
         torch.cuda.synchronize()
         p0, p1 = _params(nets[0]), _params(nets[1])
-        # gradients are summed with float atomics, so compare where |g| is
-        # well above their noise; elsewhere both moved by at most 2 lr
-        m = np.abs(g) > 1e-6
-        assert m.mean() > 0.5
-        np.testing.assert_allclose(p1[m], p0[m], rtol=1e-5, atol=1e-6)
-        assert np.abs(p1 - p0).max() <= 2.0 * 1e-2 + 1e-6
+        # the CTAs' gradient partials are summed in a fixed order, so the two
+        # forms take the same step bit for bit
+        assert np.array_equal(p1.view(np.uint32), p0.view(np.uint32))
+        assert (np.abs(g) > 1e-6).mean() > 0.5
         # a second device step keeps training: the loss goes down
         for _ in range(50):
             check(lib.cr_mlp_train_step_device(nets[1], dx.data_ptr(), dt.data_ptr(), len(x), s.cuda_stream))
