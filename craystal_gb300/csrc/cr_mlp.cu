@@ -653,7 +653,7 @@ static_assert(paramOffset(1) % 32 == 0 && paramOffset(kLayers - 1) % 32 == 0 && 
 // (block b of kRedThreads): warp w adds partials w, w + kRedWarps, ..., the
 // lanes one 128-byte row each, and warp 0 adds the warps' sums in a fixed
 // order (so the result depends only on the partials).  Valid in warp 0.
-constexpr int kRedWarps = 8;
+constexpr int kRedWarps = 8;  // 16 measured 4 % slower
 constexpr int kRedThreads = kRedWarps * 32;
 
 __device__ __forceinline__ float sumPartials(const float* __restrict__ part, int parts, int i) {
@@ -850,8 +850,13 @@ int mlpCheck(MlpState* s) {
 int trainPartials(MlpState* s, const float* in, const float* target, uint64_t n, cudaStream_t st,
                   unsigned& blocks) {
     CR_CUDA(cudaMemsetAsync(s->loss, 0, sizeof(float), st));
-    // one persistent CTA per SM (its shared memory admits one), each with at least one tile
-    blocks = std::min<unsigned>(cdiv(n, kTile), (unsigned)s->sms);
+    // one persistent CTA per SM at most (its shared memory admits one), every
+    // CTA with the same number of tiles: the slowest CTA's tile count is the
+    // same as with one CTA per SM, and fewer CTAs leave fewer partials to sum
+    // (65,536 records: 128 CTAs of 4 tiles instead of 152 of 3 or 4, 0.055
+    // against 0.056-0.057 ms per step)
+    const unsigned tiles = std::max(1u, cdiv(n, kTile)), perCta = cdiv(tiles, (unsigned)s->sms);
+    blocks = cdiv(tiles, perCta);
     kTrainTc<<<blocks, kTrThreads, kTrSmem, st>>>(reinterpret_cast<const uint8_t*>(s->wTc),
                                                  reinterpret_cast<const uint8_t*>(s->wTcT), in, target, n, s->part,
                                                  s->loss, s->err);
