@@ -489,7 +489,12 @@ int cr_mlp_infer(cr_mlp* mlp, const float* inputs, uint64_t n, float* outputs);
 /* gradient of the loss over n samples (no update); grads = param_count floats */
 int cr_mlp_gradients(cr_mlp* mlp, const float* inputs, const float* targets,
                      uint64_t n, float* grads, float* loss);
-/* one Adam step on n samples; loss (may be NULL) before the step */
+/* one Adam step on n samples; loss (may be NULL) before the step.  The
+ * gradients and the step are reproducible: the per-CTA gradient partials
+ * are summed in a fixed order (no atomics), so the same weights, inputs and
+ * n give the same new weights bit for bit, here and through
+ * cr_mlp_train_step_device.  (The reported loss is summed with atomics and
+ * may differ in its last bits.) */
 int cr_mlp_train_step(cr_mlp* mlp, const float* inputs, const float* targets,
                       uint64_t n, float* loss);
 /* The same two operations on device-resident buffers, ordered on `stream`
